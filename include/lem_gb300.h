@@ -1,0 +1,186 @@
+/*
+ * lem_gb300.h -- C ABI of the GB300 per-timestep landscape-evolution path.
+ *
+ * One handle holds one DEM and its whole model state resident in HBM.  A step
+ * is the reference's three host calls in its timestep loop (lem.cpp:83-97):
+ *   flow direction    cuFlowDirection          FD_kernels/routeflow.cu:686-975
+ *   flow accumulation computeRunOffWeights     MOD_kernels/runoffweight.cu:61-113
+ *                     calcpropsSFD / calcprops MOD_kernels/runoffweight.cu:115-354
+ *                     correctmfdflow           FA_kernels/mfd_simple.cu:238-384
+ *   process update    erosionGPU               MOD_kernels/erosion.cu:69-186
+ * The per-stage buffers that the reference mallocs, uploads, downloads and frees
+ * around every call (MEM_kernels/memory_dev.cu:33-240) stay on the device for
+ * the life of the handle; host mirrors are filled only by lem_get_field.
+ *
+ * Every entry point returns lem_status and never exits the process.  Calls on
+ * one handle are issued on the handle's own CUDA stream; they are asynchronous
+ * unless stated otherwise.  One handle must not be used from two host threads
+ * at once.
+ */
+#ifndef LEM_GB300_H
+#define LEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lem_status {
+    LEM_OK = 0,
+    LEM_ERR_INVALID = 1,     /* bad argument or unsupported combination            */
+    LEM_ERR_CAPACITY = 2,    /* a fixed-capacity table or worklist overflowed      */
+    LEM_ERR_NOCONVERGE = 3,  /* a sweep or worklist hit its iteration cap          */
+    LEM_ERR_CUDA = 4,        /* a CUDA runtime call failed                         */
+    LEM_ERR_NOMEM = 5,       /* device or host allocation failed                   */
+    LEM_ERR_STATE = 6        /* call out of order (e.g. step before the DEM is set) */
+} lem_status;
+
+/* Grid geometry: MapInfo (headers/MapInfo.h:4-12).  cellsize is the ESRI
+ * header value; the direction kernels use (int)cellsize like routeflow.cu:716. */
+typedef struct lem_grid_desc {
+    int32_t width;      /* ncols */
+    int32_t height;     /* nrows */
+    double cellsize;
+} lem_grid_desc;
+
+/* Model coefficients: default.par lines 11 and 16-35 as read by readinpar
+ * (MEM_kernels/io.cpp:469-568).  Field names follow the Data members. */
+typedef struct lem_params {
+    int32_t flow_direction_type;  /* Data.flowdirectiontype: 0 = SFD, 1 = MFD            */
+    int32_t mfd_proportions;      /* 0 = calcpropsSFD (prop 1 on every direction),
+                                     1 = calcprops (slope-proportional MFD partition)      */
+    int32_t soil_struct;          /* Data.soil_struct                                    */
+    int32_t profile_permeability; /* Data.profile_permeability                           */
+    double q_threshold;           /* Data.Qthreshold                                     */
+    double g_slope;               /* Data.Gslope                                         */
+    double kappa;                 /* Data.kappa                                          */
+    double g_flowlim;             /* Data.Gflowlim                                       */
+    double flow_a;                /* Data.Flow_A                                         */
+    double flow_b;                /* Data.Flow_B                                         */
+    double max_incision;          /* Data.max_incision                                   */
+    double ddk;                   /* Data.ddk (clamped to 0.95 as mfd_accum.cu:406)      */
+    double dck;                   /* Data.dck (clamped to 0.9 as mfd_accum.cu:407)       */
+    double dgk;                   /* Data.dgk                                            */
+    double temp_inflex;           /* Data.temp_inflex                                    */
+    double temp_sens;             /* Data.temp_sens                                      */
+} lem_params;
+
+/* Climate of one step.  recompute = 1 is SetClimateMatrices(data, i) before the
+ * step (MEM_kernels/Data.cpp:211-303, lem.cpp:79-81): rain and temperature
+ * grids are rebuilt from these scalars and the DEM at the start of the step.
+ * recompute = 0 keeps the grids of the previous call; before any recompute the
+ * grids are the ones built at lem_create from the initial rain/temperature and
+ * the DEM first uploaded (the run-in of lem.cpp:71).  A recompute = 0 step after
+ * a recompute = 1 step is rejected with LEM_ERR_STATE. */
+typedef struct lem_climate {
+    double rain;
+    double temp;
+    int32_t recompute;
+} lem_climate;
+
+/* Per-step totals: the budgets CSV row (MEM_kernels/io.cpp:233-263). */
+typedef struct lem_totals {
+    double tot_e;            /* Data.totE, sum of diffuse erosion            */
+    double tot_i;            /* Data.totI, sum of concentrated erosion       */
+    double tot_g;            /* Data.totG, sum of gelifluction               */
+    double tot_d;            /* Data.totD, sum of deposition                 */
+    double tot_weather_c;    /* Data.totweatherC                             */
+    double tot_weather_p;    /* Data.totweatherP                             */
+    double tot_bio;          /* Data.totbio                                  */
+    double fa_max;           /* Data.FA_max                                  */
+    double rain;             /* Data.rain of the step                        */
+    double temp;             /* Data.temp of the step                        */
+    int32_t sinkcount;       /* Data.sinkcount                               */
+    int32_t outlet;          /* Data.outletcellidx after the step            */
+    int32_t initial_sinks;   /* FlowDirs sink counter (routeflow.cu:778)     */
+    int32_t initial_flats;   /* FlowDirs flat counter (routeflow.cu:779)     */
+    int32_t plateau_sweeps;  /* relaxation rounds of the plateau routing     */
+    int32_t flood_edges;     /* distinct basin pairs of the sink flooding    */
+    int32_t fa_uncomputed;   /* masked-in cells left out of accumulation     */
+    int32_t sed_uncomputed;  /* masked-in cells left out of sediment routing */
+} lem_totals;
+
+/* Grid fields.  Element type per field: D = double[W*H], I = int32[W*H],
+ * D8 = double[8*W*H] (cell-major, direction index 0..7 = N,NE,E,SE,S,SW,W,NW
+ * as newflow.cu:71,99-106). */
+typedef enum lem_field {
+    LEM_F_DEM = 0,        /* D  Data.dem (nodata = -9999)                          */
+    LEM_F_MASK = 1,       /* I  Data.mask (1 in catchment, 0 outside); read only   */
+    LEM_F_FD = 2,         /* I  Data.fd after the FD epilogue (routeflow.cu:938-953) */
+    LEM_F_SFD = 3,        /* I  Data.SFD                                            */
+    LEM_F_SLOPES = 4,     /* D8 Data.Slopes                                         */
+    LEM_F_SLOPEPTR = 5,   /* D  Data.SlopePtr (aveslope)                            */
+    LEM_F_FA = 6,         /* D  Data.fa                                             */
+    LEM_F_RUNOFF = 7,     /* D  Data.runoffweight                                   */
+    LEM_F_STONE = 8,      /* D  Data.stonePtr                                       */
+    LEM_F_FINES = 9,      /* D  Data.finesPtr                                       */
+    LEM_F_SOILT = 10,     /* D  Data.soilTPtr                                       */
+    LEM_F_SOILM = 11,     /* D  Data.soilMPtr                                       */
+    LEM_F_SOILB = 12,     /* D  Data.soilBPtr                                       */
+    LEM_F_NUT = 13,       /* D  Data.nutPtr                                         */
+    LEM_F_TOTB = 14,      /* D  Data.TotBPtr                                        */
+    LEM_F_ERO = 15,       /* D  Data.eroPtr                                         */
+    LEM_F_INCI = 16,      /* D  Data.inciPtr                                        */
+    LEM_F_GELI = 17,      /* D  Data.geliPtr                                        */
+    LEM_F_DEPO = 18,      /* D  Data.depoPtr                                        */
+    LEM_F_DZ = 19,        /* D  Data.dz        (needs LEM_STEP_KEEP_DIAGNOSTICS)    */
+    LEM_F_WEATHER_C = 20, /* D  Data.weatherC  (needs LEM_STEP_KEEP_DIAGNOSTICS)    */
+    LEM_F_WEATHER_P = 21, /* D  Data.weatherP  (needs LEM_STEP_KEEP_DIAGNOSTICS)    */
+    LEM_F_CONTRIB = 22,   /* I  contributing cells incl. self along the SFD codes
+                                (needs LEM_STEP_CONTRIB)                             */
+    LEM_F_WATERSHED = 23, /* I  basin label of the last sink flooding (0 = drains
+                                off the grid or to nodata)                           */
+    LEM_F_COUNT = 24
+} lem_field;
+
+/* Step flags. */
+#define LEM_STEP_SET_OUTLET_FROM_FA  0x1u  /* correctmfdflow's first-iteration branch
+                                              (mfd_simple.cu:336-349): the outlet moves
+                                              to the cell of largest accumulation       */
+#define LEM_STEP_KEEP_DIAGNOSTICS    0x2u  /* store dz, weatherC, weatherP             */
+#define LEM_STEP_CONTRIB             0x4u  /* also count contributing cells (int32)    */
+
+typedef struct lem_handle lem_handle;
+
+/* Allocates the resident state of one grid on the current CUDA device.
+ * init_rain / init_temp are the run-in scalars of default.par lines 12-13; they
+ * also serve as the "last" climate of grow_vegetation (updates.cu:90-92). */
+lem_status lem_create(const lem_grid_desc* grid, const lem_params* params,
+                      double init_rain, double init_temp, lem_handle** out);
+lem_status lem_destroy(lem_handle* h);
+
+/* Host <-> device copies of one field (synchronous).  The first LEM_F_DEM upload
+ * also fixes the mask (dem != -9999, createmask in MEM_kernels/memory.cu:217-242)
+ * and the DEM that the initial climate grids were built from. */
+lem_status lem_set_field(lem_handle* h, lem_field f, const void* host);
+lem_status lem_get_field(lem_handle* h, lem_field f, void* host);
+lem_status lem_set_outlet(lem_handle* h, int32_t cell);  /* init_setoutletcell result */
+
+/* One stage each; the argument order follows the reference calls. */
+lem_status lem_flow_direction(lem_handle* h);                          /* cuFlowDirection */
+lem_status lem_flow_accumulation(lem_handle* h, uint32_t flags);       /* runoff + props + correctmfdflow */
+lem_status lem_erosion(lem_handle* h, uint32_t flags);                 /* erosionGPU */
+lem_status lem_set_climate(lem_handle* h, const lem_climate* c);       /* SetClimateMatrices */
+
+/* One whole timestep: lem_set_climate + the three stages. */
+lem_status lem_step(lem_handle* h, const lem_climate* c, uint32_t flags);
+
+/* Blocks until the handle's stream is idle; returns the first device-side error
+ * (capacity, convergence) raised since the previous call. */
+lem_status lem_synchronize(lem_handle* h);
+lem_status lem_get_totals(lem_handle* h, lem_totals* out);            /* synchronous */
+
+/* The handle's cudaStream_t, for callers that order their own work after it. */
+void* lem_stream(lem_handle* h);
+
+/* Kernel launches issued by this handle since creation (for launch accounting). */
+uint64_t lem_launch_count(lem_handle* h);
+
+const char* lem_status_string(lem_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LEM_GB300_H */

@@ -1,0 +1,501 @@
+// lem_api.cu -- the C ABI of include/lem_gb300.h: handle life cycle, field
+// transfers, climate state and stage orchestration.
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "lem_ctx.cuh"
+
+namespace lem {
+
+extern const void* fd_coop_kernels[];
+extern const int fd_coop_kernel_count;
+extern const void* fa_coop_kernels[];
+extern const int fa_coop_kernel_count;
+extern const void* mod_coop_kernels[];
+extern const int mod_coop_kernel_count;
+
+static thread_local std::string g_last_error;
+
+lem_status cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    g_last_error = buf;
+    return LEM_ERR_CUDA;
+}
+
+}  // namespace lem
+
+using namespace lem;
+
+struct lem_handle {
+    DevState s{};
+    ModelConsts k{};
+    ClimateNow c{};
+    lem_params p{};
+    cudaStream_t st = nullptr;
+    int device = 0;
+    bool dem_set = false;
+    size_t N = 0;
+    uint64_t launches = 0;
+    std::vector<void*> allocs;
+    void* staging = nullptr;  // pinned host buffer of 8*N floats / doubles
+    size_t staging_bytes = 0;
+    DevScalars* host_sc = nullptr;  // pinned mirror of the device scalars
+};
+
+namespace {
+
+template <class T>
+lem_status dalloc(lem_handle* h, T** p, size_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc", __FILE__, __LINE__) == LEM_ERR_CUDA ? LEM_ERR_NOMEM : LEM_ERR_NOMEM;
+    h->allocs.push_back(q);
+    e = cudaMemsetAsync(q, 0, sizeof(T) * (count ? count : 1), h->st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync", __FILE__, __LINE__);
+    *p = static_cast<T*>(q);
+    return LEM_OK;
+}
+
+// log10(K1*KC*KH / (4*K2*gammaCa*gammaHCO3^2)) of weathering (eroincidep.cu:435-447,
+// :470) in the reference's double arithmetic, tabulated over temperature.
+void dreybrodt_table(std::vector<float>& tab) {
+    tab.resize(kTabN);
+    for (int j = 0; j < kTabN; ++j) {
+        const double T = (double)kTabT0 + j * (double)kTabStep;
+        const double t_abs = T + 273.16;
+        const double t2 = t_abs * t_abs;
+        const double ltemp = log10(t_abs);
+        const double DHA = -0.4883 + 8.074e-4 * T;
+        const double DHB = -0.3241 + 1.600e-4 * T;
+        const double sqI = sqrt(0.1);
+        const double denom1 = (-4. * DHA * sqI) / (1. + 5.e-8 * DHB * sqI);
+        const double gammCa = pow(10., denom1);
+        const double gammHCO3 = pow(10., (-DHA * sqI) / (1. + 5.4e-8 * DHB * sqI));
+        const double K1 = pow(10., -356.3094 - 0.06091964 * t_abs + 21834.37 / t_abs + 126.8339 * ltemp - 1684915 / t2);
+        const double K2 = pow(10., -107.8871 - 0.03252849 * t_abs + 5151.79 / t_abs + 38.92561 * ltemp - 563713.9 / t2);
+        const double KC = pow(10., -171.9065 - 0.077993 * t_abs + 2839.319 / t_abs + 71.595 * ltemp);
+        const double KH = pow(10., 108.3865 + 0.01985076 * t_abs - 6919.53 / t_abs - 40.45154 * ltemp + 669365.0 / t2);
+        tab[j] = (float)log10((K1 * KC * KH) / (4. * K2 * gammCa * gammHCO3 * gammHCO3));
+    }
+}
+
+bool field_is_int(lem_field f) {
+    return f == LEM_F_MASK || f == LEM_F_FD || f == LEM_F_SFD || f == LEM_F_CONTRIB || f == LEM_F_WATERSHED;
+}
+
+float* float_field(lem_handle* h, lem_field f) {
+    DevState& s = h->s;
+    switch (f) {
+        case LEM_F_RUNOFF: return s.w;
+        case LEM_F_SLOPEPTR: return s.slopeptr;
+        case LEM_F_STONE: return s.stone;
+        case LEM_F_FINES: return s.fines;
+        case LEM_F_SOILT: return s.soilT;
+        case LEM_F_SOILM: return s.soilM;
+        case LEM_F_SOILB: return s.soilB;
+        case LEM_F_NUT: return s.nut;
+        case LEM_F_TOTB: return s.totB;
+        case LEM_F_ERO: return s.ero;
+        case LEM_F_INCI: return s.inci;
+        case LEM_F_GELI: return s.geli;
+        case LEM_F_DEPO: return s.depo;
+        case LEM_F_DZ: return s.dz;
+        case LEM_F_WEATHER_C: return s.wc;
+        case LEM_F_WEATHER_P: return s.wp;
+        default: return nullptr;
+    }
+}
+
+lem_status sync_scalars(lem_handle* h) {
+    LEM_CUDA_TRY(cudaMemcpyAsync(h->host_sc, h->s.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->st));
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    return LEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lem_status_string(lem_status s) {
+    switch (s) {
+        case LEM_OK: return "ok";
+        case LEM_ERR_INVALID: return "invalid argument";
+        case LEM_ERR_CAPACITY: return "capacity exceeded";
+        case LEM_ERR_NOCONVERGE: return "iteration cap reached";
+        case LEM_ERR_CUDA: return g_last_error.empty() ? "CUDA error" : g_last_error.c_str();
+        case LEM_ERR_NOMEM: return "out of memory";
+        case LEM_ERR_STATE: return "call out of order";
+    }
+    return "unknown status";
+}
+
+lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, double init_rain, double init_temp,
+                      lem_handle** out) {
+    if (!grid || !params || !out) return LEM_ERR_INVALID;
+    *out = nullptr;
+    if (grid->width < 1 || grid->height < 1 || !(grid->cellsize > 0)) return LEM_ERR_INVALID;
+    const size_t N = (size_t)grid->width * grid->height;
+    if (N >= (size_t)0x7ffffff0) return LEM_ERR_INVALID;  // int32 cell indices
+    if ((int)grid->cellsize < 1) return LEM_ERR_INVALID;
+    lem_handle* h = new lem_handle();
+    h->N = N;
+    h->p = *params;
+    // mfd_accum.cu:406-407 clamps the travel distances before the first use
+    if (h->p.ddk > 0.95) h->p.ddk = 0.95;
+    if (h->p.dck > 0.9) h->p.dck = 0.9;
+    cudaGetDevice(&h->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete h;
+        return cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
+    }
+    ModelConsts& k = h->k;
+    k.W = grid->width;
+    k.H = grid->height;
+    k.csize = (int)grid->cellsize;
+    k.flow_type = params->flow_direction_type;
+    k.mfd_props = params->mfd_proportions;
+    k.soil_struct = params->soil_struct;
+    k.profile_permeability = params->profile_permeability;
+    for (int d = 0; d < 8; ++d) {
+        const float L = (float)k.csize * ((d % 2 == 0) ? 1.0f : 1.41f);  // newflow.cu:108-117
+        k.len[d] = (double)L;
+        k.inv_len[d] = (float)(1.0 / (double)L);
+    }
+    const double cs = grid->cellsize;
+    k.q_threshold = (float)h->p.q_threshold;
+    k.g_slope = (float)h->p.g_slope;
+    k.kappa = (float)h->p.kappa;
+    k.g_flowlim = (float)h->p.g_flowlim;
+    k.flow_a = (float)h->p.flow_a;
+    k.flow_b = (float)h->p.flow_b;
+    k.max_incision = (float)h->p.max_incision;
+    k.ddk = (float)h->p.ddk;
+    k.dck = (float)h->p.dck;
+    k.dgk = (float)h->p.dgk;
+    k.temp_inflex = (float)h->p.temp_inflex;
+    k.temp_sens = (float)h->p.temp_sens;
+    k.rescale_conc = (float)(1 / (10000 / (cs * cs)));
+    k.rescale_weather = (float)(10000 * (10000 / (cs * cs)));
+    k.rescale_veg = (float)(10000 / (cs * cs));
+    k.erod_const = (float)((0.043 * (params->soil_struct - 2.)) + (0.033 * (params->profile_permeability - 3.)));
+    ClimateNow& c = h->c;
+    c.rain = c.rain0 = init_rain;
+    c.temp = c.temp0 = init_temp;
+    c.rain_inc = c.rain0_inc = (init_rain * 2 - init_rain) / grid->height;
+    c.from_current_dem = 0;
+
+    DevState& s = h->s;
+    lem_status r = LEM_OK;
+#define ALLOC(ptr, n)                             \
+    if ((r = dalloc(h, &(ptr), (n))) != LEM_OK) { \
+        lem_destroy(h);                           \
+        return r;                                 \
+    }
+    ALLOC(s.z, N);
+    ALLOC(s.zf, N);
+    ALLOC(s.z_init, N);
+    ALLOC(s.mask, N);
+    ALLOC(s.slopes, 8 * N);
+    ALLOC(s.sfd, N);
+    ALLOC(s.mfd, N);
+    ALLOC(s.fd, N);
+    ALLOC(s.sp, N);
+    ALLOC(s.ws, N);
+    ALLOC(s.pending, N);
+    ALLOC(s.list_a, N);
+    ALLOC(s.list_b, N);
+    ALLOC(s.mark, N);
+    ALLOC(s.fa, N);
+    ALLOC(s.w, N);
+    ALLOC(s.slopeptr, N);
+    ALLOC(s.stone, N);
+    ALLOC(s.fines, N);
+    ALLOC(s.soilT, N);
+    ALLOC(s.soilM, N);
+    ALLOC(s.soilB, N);
+    ALLOC(s.nut, N);
+    ALLOC(s.totB, N);
+    ALLOC(s.ero, N);
+    ALLOC(s.inci, N);
+    ALLOC(s.geli, N);
+    ALLOC(s.depo, N);
+    ALLOC(s.dz, N);
+    ALLOC(s.wc, N);
+    ALLOC(s.wp, N);
+    ALLOC(s.contrib, N);
+    if (params->flow_direction_type != 0 && params->mfd_proportions) {
+        ALLOC(s.prop, 8 * N);
+    }
+    int64_t cap = 1024;
+    while (cap < (int64_t)(N / 2)) cap <<= 1;
+    s.ecap = cap;
+    ALLOC(s.ekey, (size_t)cap);
+    ALLOC(s.ewt, (size_t)cap);
+    ALLOC(s.edge_a, (size_t)cap);
+    ALLOC(s.edge_b, (size_t)cap);
+    ALLOC(s.edge_w, (size_t)cap);
+    ALLOC(s.raise, N + 1);
+    ALLOC(s.label_seen, N + 1);
+    ALLOC(s.sc, 1);
+    ALLOC(s.temp_tab, (size_t)kTabN);
+#undef ALLOC
+    std::vector<float> tab;
+    dreybrodt_table(tab);
+    e = cudaMemcpyAsync(s.temp_tab, tab.data(), sizeof(float) * kTabN, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaMallocHost(&h->host_sc, sizeof(DevScalars));
+    h->staging_bytes = 8 * N * sizeof(double);
+    if (e == cudaSuccess) e = cudaMallocHost(&h->staging, h->staging_bytes);
+    if (e != cudaSuccess) {
+        lem_destroy(h);
+        return LEM_ERR_NOMEM;
+    }
+    std::memset(h->host_sc, 0, sizeof(DevScalars));
+    h->host_sc->round_id = 1;
+    h->host_sc->lowest_key = ~0ull;
+    e = cudaMemcpyAsync(s.sc, h->host_sc, sizeof(DevScalars), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) {
+        lem_destroy(h);
+        return cuda_fail(e, "initial upload", __FILE__, __LINE__);
+    }
+    int blocks = 1 << 30;
+    for (int i = 0; i < fd_coop_kernel_count; ++i) blocks = std::min(blocks, coop_blocks_for(fd_coop_kernels[i], 256, 0));
+    for (int i = 0; i < fa_coop_kernel_count; ++i) blocks = std::min(blocks, coop_blocks_for(fa_coop_kernels[i], 256, 0));
+    for (int i = 0; i < mod_coop_kernel_count; ++i) blocks = std::min(blocks, coop_blocks_for(mod_coop_kernels[i], 256, 0));
+    s.max_coop_blocks = blocks;
+    *out = h;
+    return LEM_OK;
+}
+
+lem_status lem_destroy(lem_handle* h) {
+    if (!h) return LEM_ERR_INVALID;
+    if (h->st) cudaStreamSynchronize(h->st);
+    for (void* q : h->allocs) cudaFree(q);
+    if (h->staging) cudaFreeHost(h->staging);
+    if (h->host_sc) cudaFreeHost(h->host_sc);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+    return LEM_OK;
+}
+
+lem_status lem_set_field(lem_handle* h, lem_field f, const void* host) {
+    if (!h || !host || f < 0 || f >= LEM_F_COUNT) return LEM_ERR_INVALID;
+    const size_t N = h->N;
+    DevState& s = h->s;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    if (f == LEM_F_DEM) {
+        const double* dem = static_cast<const double*>(host);
+        LEM_CUDA_TRY(cudaMemcpyAsync(s.z, dem, sizeof(double) * N, cudaMemcpyHostToDevice, h->st));
+        if (!h->dem_set) {
+            // createmask (MEM_kernels/memory.cu:229-238) and the DEM of the initial climate grids
+            uint8_t* m = static_cast<uint8_t*>(h->staging);
+            for (size_t i = 0; i < N; ++i) m[i] = (dem[i] == -9999) ? 0 : 1;
+            LEM_CUDA_TRY(cudaMemcpyAsync(s.mask, m, N, cudaMemcpyHostToDevice, h->st));
+            LEM_CUDA_TRY(cudaMemcpyAsync(s.z_init, dem, sizeof(double) * N, cudaMemcpyHostToDevice, h->st));
+            h->dem_set = true;
+        }
+        LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+        return LEM_OK;
+    }
+    if (f == LEM_F_SLOPES || f == LEM_F_FA) {
+        const double* src = static_cast<const double*>(host);
+        if (f == LEM_F_SLOPES) {
+            float* t = static_cast<float*>(h->staging);
+            for (size_t i = 0; i < 8 * N; ++i) t[i] = (float)src[i];
+            LEM_CUDA_TRY(cudaMemcpyAsync(s.slopes, t, sizeof(float) * 8 * N, cudaMemcpyHostToDevice, h->st));
+        } else {
+            float2* t = static_cast<float2*>(h->staging);
+            for (size_t i = 0; i < N; ++i) {
+                const float hi = (float)src[i];
+                t[i] = make_float2(hi, (float)(src[i] - (double)hi));
+            }
+            LEM_CUDA_TRY(cudaMemcpyAsync(s.fa, t, sizeof(float2) * N, cudaMemcpyHostToDevice, h->st));
+        }
+        LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+        return LEM_OK;
+    }
+    if (field_is_int(f)) return LEM_ERR_INVALID;  // codes and the mask are computed, not set
+    float* dst = float_field(h, f);
+    if (!dst) return LEM_ERR_INVALID;
+    const double* src = static_cast<const double*>(host);
+    float* t = static_cast<float*>(h->staging);
+    for (size_t i = 0; i < N; ++i) t[i] = (float)src[i];
+    LEM_CUDA_TRY(cudaMemcpyAsync(dst, t, sizeof(float) * N, cudaMemcpyHostToDevice, h->st));
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    return LEM_OK;
+}
+
+lem_status lem_get_field(lem_handle* h, lem_field f, void* host) {
+    if (!h || !host || f < 0 || f >= LEM_F_COUNT) return LEM_ERR_INVALID;
+    const size_t N = h->N;
+    DevState& s = h->s;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    switch (f) {
+        case LEM_F_DEM:
+            LEM_CUDA_TRY(cudaMemcpy(host, s.z, sizeof(double) * N, cudaMemcpyDeviceToHost));
+            return LEM_OK;
+        case LEM_F_MASK: {
+            uint8_t* m = static_cast<uint8_t*>(h->staging);
+            LEM_CUDA_TRY(cudaMemcpy(m, s.mask, N, cudaMemcpyDeviceToHost));
+            int32_t* o = static_cast<int32_t*>(host);
+            for (size_t i = 0; i < N; ++i) o[i] = m[i];
+            return LEM_OK;
+        }
+        case LEM_F_FD:
+        case LEM_F_SFD: {
+            uint8_t* buf = static_cast<uint8_t*>(h->staging);
+            LEM_CUDA_TRY(cudaMemcpy(buf, f == LEM_F_FD ? s.fd : s.sfd, N, cudaMemcpyDeviceToHost));
+            LEM_CUDA_TRY(cudaMemcpy(buf + N, s.mask, N, cudaMemcpyDeviceToHost));
+            const lem_status rs = sync_scalars(h);
+            if (rs != LEM_OK) return rs;
+            const int outlet = h->host_sc->outlet;
+            int32_t* o = static_cast<int32_t*>(host);
+            for (size_t i = 0; i < N; ++i) {
+                int32_t v = buf[N + i] ? (int32_t)buf[i] : -9999;  // masked cells hold -9999 (newflow.cu:74)
+                if (f == LEM_F_FD && (int)i == outlet) v = 16;       // routeflow.cu:953
+                o[i] = v;
+            }
+            return LEM_OK;
+        }
+        case LEM_F_CONTRIB:
+            LEM_CUDA_TRY(cudaMemcpy(host, s.contrib, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
+            return LEM_OK;
+        case LEM_F_WATERSHED:
+            LEM_CUDA_TRY(cudaMemcpy(host, s.ws, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
+            return LEM_OK;
+        case LEM_F_SLOPES: {
+            float* t = static_cast<float*>(h->staging);
+            LEM_CUDA_TRY(cudaMemcpy(t, s.slopes, sizeof(float) * 8 * N, cudaMemcpyDeviceToHost));
+            double* o = static_cast<double*>(host);
+            for (size_t i = 0; i < 8 * N; ++i) o[i] = t[i];
+            return LEM_OK;
+        }
+        case LEM_F_FA: {
+            float2* t = static_cast<float2*>(h->staging);
+            LEM_CUDA_TRY(cudaMemcpy(t, s.fa, sizeof(float2) * N, cudaMemcpyDeviceToHost));
+            double* o = static_cast<double*>(host);
+            for (size_t i = 0; i < N; ++i) o[i] = (double)t[i].x + (double)t[i].y;
+            return LEM_OK;
+        }
+        default: {
+            float* src = float_field(h, f);
+            if (!src) return LEM_ERR_INVALID;
+            float* t = static_cast<float*>(h->staging);
+            LEM_CUDA_TRY(cudaMemcpy(t, src, sizeof(float) * N, cudaMemcpyDeviceToHost));
+            double* o = static_cast<double*>(host);
+            for (size_t i = 0; i < N; ++i) o[i] = t[i];
+            return LEM_OK;
+        }
+    }
+}
+
+lem_status lem_set_outlet(lem_handle* h, int32_t cell) {
+    if (!h || cell < 0 || (size_t)cell >= h->N) return LEM_ERR_INVALID;
+    LEM_CUDA_TRY(cudaMemcpyAsync(&h->s.sc->outlet, &cell, sizeof(int32_t), cudaMemcpyHostToDevice, h->st));
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    return LEM_OK;
+}
+
+lem_status lem_set_climate(lem_handle* h, const lem_climate* c) {
+    if (!h || !c) return LEM_ERR_INVALID;
+    if (c->recompute) {
+        h->c.rain = c->rain;
+        h->c.temp = c->temp;
+        h->c.rain_inc = (c->rain * 2 - c->rain) / h->k.H;
+        h->c.from_current_dem = 1;
+    } else if (h->c.from_current_dem) {
+        return LEM_ERR_STATE;
+    }
+    return LEM_OK;
+}
+
+lem_status lem_flow_direction(lem_handle* h) {
+    if (!h) return LEM_ERR_INVALID;
+    if (!h->dem_set) return LEM_ERR_STATE;
+    return launch_flow_direction(h->s, h->k, h->st, &h->launches);
+}
+
+lem_status lem_flow_accumulation(lem_handle* h, uint32_t flags) {
+    if (!h) return LEM_ERR_INVALID;
+    if (!h->dem_set) return LEM_ERR_STATE;
+    return launch_flow_accumulation(h->s, h->k, h->c, flags, h->st, &h->launches);
+}
+
+lem_status lem_erosion(lem_handle* h, uint32_t flags) {
+    if (!h) return LEM_ERR_INVALID;
+    if (!h->dem_set) return LEM_ERR_STATE;
+    return launch_erosion(h->s, h->k, h->c, flags, h->st, &h->launches);
+}
+
+lem_status lem_step(lem_handle* h, const lem_climate* c, uint32_t flags) {
+    lem_status r;
+    if (c && (r = lem_set_climate(h, c)) != LEM_OK) return r;
+    if ((r = lem_flow_direction(h)) != LEM_OK) return r;
+    if ((r = lem_flow_accumulation(h, flags)) != LEM_OK) return r;
+    return lem_erosion(h, flags);
+}
+
+lem_status lem_synchronize(lem_handle* h) {
+    if (!h) return LEM_ERR_INVALID;
+    lem_status r = sync_scalars(h);
+    if (r != LEM_OK) return r;
+    const uint32_t err = h->host_sc->err;
+    if (err) {
+        uint32_t zero = 0;
+        LEM_CUDA_TRY(cudaMemcpy(&h->s.sc->err, &zero, sizeof zero, cudaMemcpyHostToDevice));
+        if (err & ErrFlags::kCapacity) return LEM_ERR_CAPACITY;
+        return LEM_ERR_NOCONVERGE;
+    }
+    return LEM_OK;
+}
+
+lem_status lem_get_totals(lem_handle* h, lem_totals* o) {
+    if (!h || !o) return LEM_ERR_INVALID;
+    lem_status r = sync_scalars(h);
+    if (r != LEM_OK) return r;
+    const DevScalars& d = *h->host_sc;
+    std::memset(o, 0, sizeof *o);
+    o->tot_e = d.tot_e;
+    o->tot_i = d.tot_i;
+    o->tot_g = d.tot_g;
+    o->tot_d = d.tot_d;
+    o->tot_weather_c = d.tot_wc;
+    o->tot_weather_p = d.tot_wp;
+    o->tot_bio = d.tot_bio;
+    {
+        // FA_max from its ordered key (the hi and lo words are ordered fp32 keys)
+        auto unkey = [](uint32_t k) {
+            uint32_t b = (k >> 31) ? (k & 0x7fffffffu) : ~k;
+            float f;
+            std::memcpy(&f, &b, 4);
+            return f;
+        };
+        const unsigned long long fk = d.fa_max_key;
+        double v = fk ? (double)unkey((uint32_t)(fk >> 32)) + (double)unkey((uint32_t)fk) : 0.0;
+        o->fa_max = v > 0.0 ? v : 0.0;
+    }
+    o->rain = h->c.rain;
+    o->temp = h->c.temp;
+    o->sinkcount = d.sinkcount;
+    o->outlet = d.outlet;
+    o->initial_sinks = d.sink_counter;
+    o->initial_flats = d.flat_counter;
+    o->plateau_sweeps = d.plateau_sweeps;
+    o->flood_edges = d.n_edges;
+    o->fa_uncomputed = d.n_active - d.fa_done;
+    o->sed_uncomputed = d.n_active - d.sed_done;
+    return LEM_OK;
+}
+
+void* lem_stream(lem_handle* h) { return h ? (void*)h->st : nullptr; }
+
+uint64_t lem_launch_count(lem_handle* h) { return h ? h->launches : 0; }
+
+}  // extern "C"

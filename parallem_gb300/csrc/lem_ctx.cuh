@@ -1,0 +1,83 @@
+// lem_ctx.cuh -- resident device state of one grid and the stage launchers.
+#pragma once
+
+#include "lem_common.cuh"
+
+namespace lem {
+
+// Dreybrodt temperature response table (see lem_mod.cu): log10 of
+// K1*KC*KH / (4*K2*gammaCa*gammaHCO3^2) sampled every kTabStep degrees.
+constexpr int kTabN = 3841;
+constexpr float kTabT0 = -60.0f;
+constexpr float kTabStep = 1.0f / 32.0f;
+
+struct ModelConsts {  // per-handle constants derived on the host in double
+    int32_t W, H;
+    int32_t csize;          // (int)cellsize, routeflow.cu:716
+    int32_t flow_type;      // Data.flowdirectiontype
+    int32_t mfd_props;      // calcprops instead of calcpropsSFD
+    int32_t soil_struct, profile_permeability;
+    float inv_len[8];       // 1 / (float)((float)csize * dc)
+    double len[8];          // (double)(float)((float)csize * dc)
+    float q_threshold, g_slope, kappa, g_flowlim, flow_a, flow_b, max_incision;
+    float ddk, dck, dgk, temp_inflex, temp_sens;
+    float rescale_conc;     // 1 / (10000 / cs^2)          eroincidep.cu:310
+    float rescale_weather;  // 10000 * (10000 / cs^2)      eroincidep.cu:628
+    float rescale_veg;      // 10000 / cs^2                Data.cpp:124
+    float erod_const;       // 0.043*(struct-2) + 0.033*(perm-3)
+};
+
+struct ClimateNow {  // the climate grids of the current step, generated on the fly
+    double rain, temp;      // scalars of the last SetClimateMatrices
+    double rain_inc;        // (2R - R) / H
+    double rain0, temp0;    // initial ("last") scalars
+    double rain0_inc;
+    int32_t from_current_dem; // 1: temperature from the DEM at step start, 0: from the initial DEM
+    int32_t pad;
+};
+
+struct DevState {
+    // grids
+    double* z;          // Data.dem
+    double* zf;         // DEM of the second flow-direction pass (raised)
+    double* z_init;     // DEM the run-in climate grids were built from
+    uint8_t* mask;
+    float* slopes;      // 8 per cell
+    uint8_t* sfd;       // SFD code (low byte; masked = 0xF1)
+    uint8_t* mfd;       // MFD code
+    uint8_t* fd;        // final code after the epilogue
+    float* sp;          // plateau distances
+    int32_t* ws;        // basin labels / pointers
+    int32_t* pending;   // wave in-degrees
+    int32_t* list_a;    // worklists
+    int32_t* list_b;
+    int32_t* mark;      // worklist de-duplication epochs
+    float2* fa;         // accumulation as an unevaluated fp32 pair (hi, lo)
+    float* w;           // runoff weight
+    float* slopeptr;
+    float* stone; float* fines; float* soilT; float* soilM; float* soilB; float* nut; float* totB;
+    float* ero; float* inci; float* geli; float* depo;
+    float* dz; float* wc; float* wp;  // diagnostics
+    float* prop;        // 8 per cell, MFD proportions (calcprops mode only)
+    int32_t* contrib;
+    // flooding tables
+    unsigned long long* ekey;   // hash keys (label pair)
+    unsigned long long* ewt;    // min boundary height key
+    int64_t ecap;               // capacity (power of two)
+    int32_t* edge_a; int32_t* edge_b; unsigned long long* edge_w;
+    unsigned long long* raise;  // per label (label = cell + 1), ordered keys
+    int32_t* label_seen;
+    DevScalars* sc;
+    float* temp_tab;
+    int32_t max_coop_blocks;    // co-resident blocks of the cooperative kernels
+};
+
+// stage launchers (stream-ordered, no host synchronisation)
+lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, cudaStream_t st, uint64_t* launches);
+lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
+                                    cudaStream_t st, uint64_t* launches);
+lem_status launch_erosion(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
+                          cudaStream_t st, uint64_t* launches);
+int coop_blocks_for(const void* kernel, int threads, size_t smem);
+
+}  // namespace lem

@@ -1,0 +1,818 @@
+// lem_fd.cu -- flow-direction stage: FlowDirs, plateau routing, sink flooding.
+//
+// Restates cuFlowDirection (FD_kernels/routeflow.cu:686-975) and its kernels in
+// FD_kernels/newflow.cu.  Elevations stay fp64 in HBM (the reference's state);
+// comparisons use order-preserving integer keys and slope magnitudes an fp32
+// approximation with a certified error bound, so the common path issues no FP64
+// instruction.  A cell whose steepest-descent choice cannot be certified (near
+// tie) recomputes the reference's fp64 quotients exactly.
+
+#include <cooperative_groups.h>
+
+#include "lem_ctx.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace lem {
+
+namespace {
+
+constexpr int FD_BX = 32;
+constexpr int FD_BY = 8;
+constexpr float kFar = 20000000.0f;  // shortest_paths_plateaus_initMFD (newflow.cu:252)
+constexpr int kMaxRounds = 1 << 20;
+
+__device__ __forceinline__ unsigned long long key_nodata() { return dkey(-9999.0); }
+
+__device__ __forceinline__ int warp_sum(int v) { return __reduce_add_sync(0xffffffffu, v); }
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = u < v ? u : v;
+    }
+    return v;
+}
+
+// Warp-aggregated append of `pred` lanes to list[*count].
+__device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t* list, int32_t* count, int cap,
+                                            uint32_t* err) {
+    unsigned ballot = __ballot_sync(0xffffffffu, pred);
+    if (!ballot) return;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(ballot) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pred) {
+        int pos = base + __popc(ballot & ((1u << lane) - 1));
+        if (pos < cap)
+            list[pos] = value;
+        else
+            atomicOr(err, ErrFlags::kCapacity);
+    }
+}
+
+// --------------------------------------------------------------------------
+// FlowDirs (newflow.cu:49-174) on a 32x8 tile with a one-cell halo in shared
+// memory.  Pass 1 writes the downslope slopes into the persistent 8-per-cell
+// array (other entries keep their stale values, newflow.cu:126-140) and the
+// sink/flat counters and lowest elevation; pass 2 writes codes only.
+__global__ void __launch_bounds__(FD_BX* FD_BY)
+    k_flowdirs(const double* __restrict__ z, const uint8_t* __restrict__ mask, float* __restrict__ slopes,
+               uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, ModelConsts k, DevScalars* sc, int pass) {
+    if (pass == 2 && sc->sinkcount_pass1 == 0) return;
+    __shared__ unsigned long long skey[FD_BY + 2][FD_BX + 2];
+    __shared__ float shi[FD_BY + 2][FD_BX + 2];
+    __shared__ float slo[FD_BY + 2][FD_BX + 2];
+    const int W = k.W, H = k.H;
+    const int x0 = blockIdx.x * FD_BX, y0 = blockIdx.y * FD_BY;
+    const int tid = threadIdx.y * FD_BX + threadIdx.x;
+    for (int t = tid; t < (FD_BX + 2) * (FD_BY + 2); t += FD_BX * FD_BY) {
+        int ly = t / (FD_BX + 2), lx = t % (FD_BX + 2);
+        int gx = x0 + lx - 1, gy = y0 + ly - 1;
+        unsigned long long key = 0;  // 0 = outside the grid
+        float hi = 0.f, lo = 0.f;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            double v = z[(size_t)gy * W + gx];
+            key = dkey(v);
+            dsplit(v, hi, lo);
+        }
+        skey[ly][lx] = key;
+        shi[ly][lx] = hi;
+        slo[ly][lx] = lo;
+    }
+    __syncthreads();
+
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
+    int is_sink = 0, is_flat = 0;
+    unsigned long long low = ~0ull;
+    if (x < W && y < H) {
+        const size_t self = (size_t)y * W + x;
+        uint8_t cs = kMaskedCode, cm = kMaskedCode;
+        if (mask[self]) {
+            const unsigned long long ks = skey[ly][lx];
+            const unsigned long long knd = key_nodata();
+            const float hs = shi[ly][lx], ls = slo[ly][lx];
+            low = ks;
+            int up = 0, flat = 0;
+            uint32_t aspect = 0, cand = 0;
+            float sv[8];
+            unsigned long long kn8[8];
+            int bestd = -1;
+            float best = -1.0f;
+#pragma unroll
+            for (int d = 0; d < 8; ++d) {
+                sv[d] = 0.f;
+                const unsigned long long kn = skey[ly + dir_dy(d)][lx + dir_dx(d)];
+                kn8[d] = kn;
+                if (kn == 0) continue;
+                if (ks < kn) up += 1;
+                if (ks == kn) flat += 1;
+                if (ks > kn && kn != knd) {
+                    const float dd = (hs - shi[ly + dir_dy(d)][lx + dir_dx(d)]) + (ls - slo[ly + dir_dy(d)][lx + dir_dx(d)]);
+                    const float s = dd * k.inv_len[d];
+                    sv[d] = s;
+                    cand |= 1u << d;
+                    aspect |= dir_bit(d);
+                    if (s > best) {
+                        best = s;
+                        bestd = d;
+                    }
+                }
+            }
+            if (cand) {
+                // certify the steepest direction against the exact fp64 quotients
+                const float zs_mag = fabsf(hs);
+                bool certain = true;
+                const float err_b = best * 1.0e-6f + fmaxf(zs_mag, 1.0f) * 1.0e-12f * k.inv_len[bestd];
+#pragma unroll
+                for (int d = 0; d < 8; ++d) {
+                    if (!((cand >> d) & 1u) || d == bestd) continue;
+                    const float err_d = sv[d] * 1.0e-6f + fmaxf(zs_mag, 1.0f) * 1.0e-12f * k.inv_len[d];
+                    if (sv[d] + err_d < best - err_b) continue;
+                    if (((d ^ bestd) & 1) == 0 && kn8[d] == kn8[bestd] && d > bestd) continue;  // exact tie
+                    certain = false;
+                }
+                if (!certain) {
+                    // the reference's arithmetic (newflow.cu:117,130-135)
+                    const double zs = dkey_inv(ks);
+                    double smax = 0.0;
+                    bestd = -1;
+                    for (int d = 0; d < 8; ++d) {
+                        if (!((cand >> d) & 1u)) continue;
+                        const double st = (zs - dkey_inv(kn8[d])) / k.len[d];
+                        sv[d] = (float)st;
+                        if (st > smax) {
+                            smax = st;
+                            bestd = d;
+                        }
+                    }
+                }
+                if (slopes) {
+                    float4* p = reinterpret_cast<float4*>(slopes + 8 * self);
+                    float4 a = p[0], b = p[1];
+                    if (cand & 0x01u) a.x = sv[0];
+                    if (cand & 0x02u) a.y = sv[1];
+                    if (cand & 0x04u) a.z = sv[2];
+                    if (cand & 0x08u) a.w = sv[3];
+                    if (cand & 0x10u) b.x = sv[4];
+                    if (cand & 0x20u) b.y = sv[5];
+                    if (cand & 0x40u) b.z = sv[6];
+                    if (cand & 0x80u) b.w = sv[7];
+                    p[0] = a;
+                    p[1] = b;
+                }
+            }
+            uint32_t asfd = bestd >= 0 ? dir_bit(bestd) : 0u;
+            if (up > 7) {
+                is_sink = 1;
+                aspect = asfd = 0;
+            }
+            if (flat + up > 7 && up <= 7) {
+                is_flat = 1;
+                aspect = asfd = 0;
+            }
+            cs = (uint8_t)asfd;
+            cm = (uint8_t)aspect;
+        }
+        sfd[self] = cs;
+        mfd[self] = cm;
+    }
+    if (pass == 1) {
+        const int s1 = warp_sum(is_sink), f1 = warp_sum(is_flat);
+        low = warp_min_u64(low);
+        if ((threadIdx.x & 31) == 0) {
+            if (s1) atomicAdd(&sc->sink_counter, s1);
+            if (f1) atomicAdd(&sc->flat_counter, f1);
+            if (low != ~0ull) atomicMin(&sc->lowest_key, low);
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// Plateau routing (newflow.cu:234-350).  Candidates are masked-in cells with no
+// downslope direction; their distance starts at 2e7, every other cell at 0.
+__global__ void k_plateau_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
+                               const uint8_t* __restrict__ mfd, float* __restrict__ sp, int32_t* cand, ModelConsts k,
+                               DevScalars* sc, int pass) {
+    if (pass == 2 && sc->sinkcount_pass1 == 0) return;
+    const size_t N = (size_t)k.W * k.H;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = base + threadIdx.x;
+        bool is_c = false;
+        if (c < N) {
+            float v = 0.f;
+            if (mask[c] && sfd[c] == 0 && mfd[c] == 0) {
+                v = kFar;
+                is_c = true;
+            }
+            sp[c] = v;
+        }
+        warp_append(is_c, (int32_t)c, cand, &sc->n_cand, (int)N, &sc->err);
+    }
+}
+
+__device__ __forceinline__ float ld_sp(const float* sp, size_t i) { return __ldcg(sp + i); }
+
+// Least fixpoint of sp = min(sp, sp[n] + dc) over equal-height in-grid
+// neighbours (the route_plateausMFD loop, routeflow.cu:854-872), by a pull sweep
+// over all candidates followed by push rounds from the cells that improved.
+__global__ void k_plateau_relax(const double* __restrict__ z, float* sp, const int32_t* __restrict__ cand,
+                                int32_t* list_a, int32_t* list_b, int32_t* mark, ModelConsts k, DevScalars* sc,
+                                int pass) {
+    if (pass == 2 && sc->sinkcount_pass1 == 0) return;
+    cg::grid_group grid = cg::this_grid();
+    const int W = k.W, H = k.H;
+    const int n = sc->n_cand;
+    const size_t gstride = (size_t)gridDim.x * blockDim.x;
+    const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int ncap = (int)((size_t)W * H);
+    int32_t* cnt = sc->counters;  // cnt[0..2] frontier sizes, triple-buffered
+    const int32_t rid0 = sc->round_id;  // marks of this launch are rid0 + round + 1
+    if (gtid == 0) {
+        cnt[0] = 0;
+        cnt[1] = 0;
+        cnt[2] = 0;
+    }
+    grid.sync();
+    // round 0: pull
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)n; base += gstride) {
+        const size_t i = base + threadIdx.x;
+        bool improved = false;
+        int32_t c = 0;
+        if (i < (size_t)n) {
+            c = cand[i];
+            const int x = c % W, y = c / W;
+            const unsigned long long kc = dkey(z[c]);
+            float best = kFar;
+            for (int d = 0; d < 8; ++d) {
+                const int nx = x + dir_dx(d), ny = y + dir_dy(d);
+                if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+                const size_t nb = (size_t)ny * W + nx;
+                if (dkey(z[nb]) != kc) continue;
+                const float dis = ld_sp(sp, nb) + ((d & 1) ? 1.41f : 1.0f);
+                if (best > dis) best = dis;
+            }
+            if (best < kFar) {
+                atomicMin(reinterpret_cast<int*>(sp + c), __float_as_int(best));
+                improved = true;
+            }
+        }
+        warp_append(improved, c, list_a, &cnt[0], ncap, &sc->err);
+    }
+    grid.sync();
+    int round = 0;
+    for (;; ++round) {
+        const int32_t* in = (round & 1) ? list_b : list_a;
+        int32_t* out = (round & 1) ? list_a : list_b;
+        const int nin = *((volatile int32_t*)&cnt[round % 3]);
+        if (nin == 0) break;
+        if (round >= kMaxRounds) {
+            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            break;
+        }
+        if (gtid == 0) cnt[(round + 2) % 3] = 0;
+        for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)nin; base += gstride) {
+            const size_t i = base + threadIdx.x;
+            // push the improvement of c to its equal-height neighbours
+            int32_t pushed[8];
+            int np = 0;
+            if (i < (size_t)nin) {
+                const int32_t c = in[i];
+                const int x = c % W, y = c / W;
+                const unsigned long long kc = dkey(z[c]);
+                const float v = ld_sp(sp, c);
+                for (int d = 0; d < 8; ++d) {
+                    const int nx = x + dir_dx(d), ny = y + dir_dy(d);
+                    if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+                    const size_t nb = (size_t)ny * W + nx;
+                    if (dkey(z[nb]) != kc) continue;
+                    const float nv = v + ((d & 1) ? 1.41f : 1.0f);
+                    const int old = atomicMin(reinterpret_cast<int*>(sp + nb), __float_as_int(nv));
+                    if (__int_as_float(old) > nv) {
+                        const int32_t id = rid0 + round + 1;
+                        if (atomicExch(mark + nb, id) != id) pushed[np++] = (int32_t)nb;
+                    }
+                }
+            }
+            for (int j = 0; j < 8; ++j)
+                warp_append(j < np, j < np ? pushed[j] : 0, out, &cnt[(round + 1) % 3], ncap, &sc->err);
+        }
+        grid.sync();
+    }
+    grid.sync();
+    if (gtid == 0) {
+        sc->plateau_sweeps += round + 1;
+        sc->round_id = rid0 + round + 2;
+    }
+}
+
+// Final direction of a routed plateau cell: the first direction whose
+// equal-height neighbour attains the cell's distance; pass 1 also stores the
+// 1e-4 slope on that direction (newflow.cu:339-346).
+__global__ void k_plateau_final(const double* __restrict__ z, const float* __restrict__ sp,
+                                const int32_t* __restrict__ cand, uint8_t* sfd, uint8_t* mfd, float* slopes,
+                                ModelConsts k, DevScalars* sc, int pass) {
+    if (pass == 2 && sc->sinkcount_pass1 == 0) return;
+    const int W = k.W, H = k.H;
+    const int n = sc->n_cand;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int32_t c = cand[i];
+        const float v = sp[c];
+        if (!(v < kFar)) continue;
+        const int x = c % W, y = c / W;
+        const unsigned long long kc = dkey(z[c]);
+        for (int d = 0; d < 8; ++d) {
+            const int nx = x + dir_dx(d), ny = y + dir_dy(d);
+            if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+            const size_t nb = (size_t)ny * W + nx;
+            if (dkey(z[nb]) != kc) continue;
+            if (sp[nb] + ((d & 1) ? 1.41f : 1.0f) == v) {
+                sfd[c] = (uint8_t)dir_bit(d);
+                mfd[c] = (uint8_t)dir_bit(d);
+                if (slopes) slopes[8 * (size_t)c + d] = 0.0001f;
+                break;
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// Sink flooding (floodingDriver, routeflow.cu:202-676).
+// init_watershedMFD (newflow.cu:352-420): sink cells get a unique id (cell+1),
+// other cells point at their SFD receiver, masked and edge cells are basin 0.
+__global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd, int32_t* ws,
+                             int32_t* sinks, unsigned long long* raise, ModelConsts k, DevScalars* sc) {
+    const int W = k.W, H = k.H;
+    const size_t N = (size_t)W * H;
+    int nsink = 0;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = base + threadIdx.x;
+        bool sink = false;
+        if (c < N) {
+            const int x = (int)(c % W), y = (int)(c / W);
+            int32_t v = 0;
+            if (mask[c]) {
+                const uint8_t s = sfd[c];
+                sink = (s == 0);
+                if (x == W - 1 || y == 0 || y == H - 1) {
+                    v = 0;
+                } else if (s == 0) {
+                    v = (int32_t)c + 1;
+                    raise[c + 1] = dkey(0.0);
+                } else {
+                    const int d = bit_dir(s);
+                    const int nx = x + dir_dx(d < 0 ? 0 : d), ny = y + dir_dy(d < 0 ? 0 : d);
+                    if (d >= 0 && nx >= 0 && nx < W && ny >= 0 && ny < H)
+                        v = -(int32_t)((size_t)ny * W + nx) - 1;
+                    else
+                        v = 0;
+                }
+            }
+            ws[c] = v;
+        }
+        nsink += warp_sum(sink ? 1 : 0) * ((threadIdx.x & 31) == 0);
+        warp_append(sink, (int32_t)c, sinks, &sc->n_sinks, (int)N, &sc->err);
+    }
+    if (nsink) atomicAdd(&sc->sinkcount_pass1, nsink);
+    if (blockIdx.x == 0 && threadIdx.x == 0) raise[0] = dkey(0.0);
+}
+
+// init_watershed_sinkMFD loop (newflow.cu:430-460): equal-height sink cells
+// adopt the largest neighbouring id until nothing changes.
+__global__ void k_flood_merge(const double* __restrict__ z, int32_t* ws, const int32_t* __restrict__ sinks,
+                              ModelConsts k, DevScalars* sc) {
+    if (sc->sinkcount_pass1 == 0) return;
+    cg::grid_group grid = cg::this_grid();
+    const int W = k.W, H = k.H;
+    const int n = sc->n_sinks;
+    const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gtid == 0) sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
+    grid.sync();
+    int round = 0;
+    for (;; ++round) {
+        if (gtid == 0) sc->flag[(round + 1) % 3] = 0;  // next round's flag; this round's is read after the sync
+        int changed = 0;
+        for (size_t i = gtid; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
+            const int32_t c = sinks[i];
+            const int x = c % W, y = c / W;
+            const unsigned long long kc = dkey(z[c]);
+            const int32_t mine = __ldcg(ws + c);
+            int32_t best = mine;
+            for (int d = 0; d < 8; ++d) {
+                const int nx = x + dir_dx(d), ny = y + dir_dy(d);
+                if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+                const size_t nb = (size_t)ny * W + nx;
+                if (dkey(z[nb]) != kc) continue;
+                const int32_t o = __ldcg(ws + nb);
+                if (o > best) best = o;
+            }
+            if (best > mine) {
+                atomicMax(ws + c, best);
+                changed = 1;
+            }
+        }
+        if (changed) sc->flag[round % 3] = 1;
+        grid.sync();
+        if (*((volatile int32_t*)&sc->flag[round % 3]) == 0) break;
+        if (round >= kMaxRounds) {
+            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            break;
+        }
+    }
+    if (gtid == 0) sc->flood_sweeps = round + 1;
+}
+
+// identify_watershedMFD loop (newflow.cu:469-487): pointer jumping until every
+// cell holds the label of the sink (or basin 0) its SFD path ends in.
+__global__ void k_flood_jump(int32_t* ws, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc) {
+    if (sc->sinkcount_pass1 == 0) return;
+    cg::grid_group grid = cg::this_grid();
+    const size_t N = (size_t)k.W * k.H;
+    const size_t gstride = (size_t)gridDim.x * blockDim.x;
+    const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t* cnt = sc->counters + 3;
+    if (gtid == 0) {
+        cnt[0] = 0;
+        cnt[1] = 0;
+        cnt[2] = 0;
+    }
+    grid.sync();
+    // round 0 over every cell
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += gstride) {
+        const size_t c = base + threadIdx.x;
+        bool keep = false;
+        if (c < N) {
+            int32_t v = __ldcg(ws + c);
+            if (v < 0) {
+                v = __ldcg(ws + (-(size_t)v - 1));
+                ws[c] = v;
+                keep = v < 0;
+            }
+        }
+        warp_append(keep, (int32_t)c, list_a, &cnt[0], (int)N, &sc->err);
+    }
+    grid.sync();
+    int round = 0;
+    for (;; ++round) {
+        const int32_t* in = (round & 1) ? list_b : list_a;
+        int32_t* out = (round & 1) ? list_a : list_b;
+        const int nin = *((volatile int32_t*)&cnt[round % 3]);
+        if (nin == 0) break;
+        if (round >= 64) {
+            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            break;
+        }
+        if (gtid == 0) cnt[(round + 2) % 3] = 0;
+        for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)nin; base += gstride) {
+            const size_t i = base + threadIdx.x;
+            bool keep = false;
+            int32_t c = 0;
+            if (i < (size_t)nin) {
+                c = in[i];
+                int32_t v = __ldcg(ws + c);
+                if (v < 0) {
+                    v = __ldcg(ws + (-(size_t)v - 1));
+                    ws[c] = v;
+                    keep = v < 0;
+                }
+            }
+            warp_append(keep, c, out, &cnt[(round + 1) % 3], (int)N, &sc->err);
+        }
+        grid.sync();
+    }
+    if (gtid == 0) sc->label_rounds = round + 1;
+}
+
+__device__ __forceinline__ uint64_t edge_hash(unsigned long long key, int logcap) {
+    return (key * 0x9E3779B97F4A7C15ull) >> (64 - logcap);
+}
+
+// identify_watershed_boundary_write_backMFD (newflow.cu:787-877): the minimum
+// boundary height per unordered basin pair, in an open-addressing table.
+__global__ void k_flood_edges(const double* __restrict__ z, const uint8_t* __restrict__ mask,
+                              const int32_t* __restrict__ ws, unsigned long long* ekey, unsigned long long* ewt,
+                              int logcap, ModelConsts k, DevScalars* sc) {
+    if (sc->sinkcount_pass1 == 0) return;
+    const int W = k.W, H = k.H;
+    const size_t N = (size_t)W * H;
+    const uint64_t capm = (1ull << logcap) - 1;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+        if (!mask[c]) continue;
+        const int x = (int)(c % W), y = (int)(c / W);
+        const int32_t a = ws[c];
+        const unsigned long long kz = dkey(z[c]);
+        for (int d = 0; d < 8; ++d) {
+            const int nx = x + dir_dx(d), ny = y + dir_dy(d);
+            if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+            const size_t nb = (size_t)ny * W + nx;
+            const int32_t b = ws[nb];
+            if (a == b) continue;
+            if (kz < dkey(z[nb])) continue;
+            const unsigned long long key = ((unsigned long long)(uint32_t)min(a, b) << 32) | (uint32_t)max(a, b);
+            uint64_t h = edge_hash(key, logcap);
+            int probes = 0;
+            for (;;) {
+                unsigned long long cur = ekey[h];
+                if (cur == ~0ull) cur = atomicCAS(ekey + h, ~0ull, key);
+                if (cur == ~0ull || cur == key) {
+                    if (kz < __ldcg(ewt + h)) atomicMin(ewt + h, kz);
+                    break;
+                }
+                h = (h + 1) & capm;
+                if (++probes > 4096) {
+                    atomicOr(&sc->err, ErrFlags::kCapacity);
+                    break;
+                }
+            }
+        }
+    }
+}
+
+// Compact the table into an edge list and count the labels on edges
+// (data->sinkcount, newflow.cu:1044-1045).  Labels on edges start unreached.
+__global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, const unsigned long long* __restrict__ ewt,
+                                int64_t cap, int32_t* ea, int32_t* eb, unsigned long long* ew,
+                                unsigned long long* raise, int32_t* seen, int32_t epoch, DevScalars* sc) {
+    if (sc->sinkcount_pass1 == 0) return;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)cap; base += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = base + threadIdx.x;
+        bool has = false;
+        int32_t a = 0, b = 0;
+        unsigned long long w = 0;
+        if (i < (size_t)cap) {
+            const unsigned long long key = ekey[i];
+            if (key != ~0ull) {
+                has = true;
+                a = (int32_t)(key >> 32);
+                b = (int32_t)(key & 0xffffffffu);
+                w = ewt[i];
+                int nd = 0;
+                if (atomicExch(seen + a, epoch) != epoch) ++nd;
+                if (atomicExch(seen + b, epoch) != epoch) ++nd;
+                if (nd) atomicAdd(&sc->sinkcount, nd);
+                if (a != 0) raise[a] = ~0ull;
+                if (b != 0) raise[b] = ~0ull;
+            }
+        }
+        unsigned ballot = __ballot_sync(0xffffffffu, has);
+        if (!ballot) continue;
+        const int lane = threadIdx.x & 31, leader = __ffs(ballot) - 1;
+        int pos = 0;
+        if (lane == leader) pos = atomicAdd(&sc->n_edges, __popc(ballot));
+        pos = __shfl_sync(0xffffffffu, pos, leader) + __popc(ballot & ((1u << lane) - 1));
+        if (has) {
+            ea[pos] = a;
+            eb[pos] = b;
+            ew[pos] = w;
+        }
+    }
+}
+
+// Spill heights.  The Kruskal pass of routeflow.cu:529-572 gives every basin
+// that can drain to basin 0 the smallest height h at which it connects to
+// basin 0 through boundaries no higher than h (the bottleneck distance); it is
+// computed here as the fixpoint raise[a] = min(raise[a], max(w_ab, raise[b])).
+__global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __restrict__ eb,
+                              const unsigned long long* __restrict__ ew, unsigned long long* raise, DevScalars* sc) {
+    if (sc->sinkcount_pass1 == 0) return;
+    cg::grid_group grid = cg::this_grid();
+    const int n = sc->n_edges;
+    const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gtid == 0) {
+        raise[0] = 0ull;  // basin 0 is done
+        sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
+    }
+    grid.sync();
+    int round = 0;
+    for (;; ++round) {
+        if (gtid == 0) sc->flag[(round + 1) % 3] = 0;  // next round's flag; this round's is read after the sync
+        int changed = 0;
+        for (size_t i = gtid; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
+            const int32_t a = ea[i], b = eb[i];
+            const unsigned long long w = ew[i];
+            const unsigned long long ra = __ldcg(raise + a), rb = __ldcg(raise + b);
+            const unsigned long long ca = w > rb ? w : rb;
+            const unsigned long long cb = w > ra ? w : ra;
+            if (a != 0 && ca < ra) {
+                atomicMin(raise + a, ca);
+                changed = 1;
+            }
+            if (b != 0 && cb < rb) {
+                atomicMin(raise + b, cb);
+                changed = 1;
+            }
+        }
+        if (changed) sc->flag[round % 3] = 1;
+        grid.sync();
+        if (*((volatile int32_t*)&sc->flag[round % 3]) == 0) break;
+        if (round >= kMaxRounds) {
+            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            break;
+        }
+    }
+    if (gtid == 0) {
+        sc->spill_rounds = round + 1;
+        raise[0] = dkey(0.0);
+    }
+    grid.sync();
+    // basins that never reach basin 0 keep height 0 (the reference leaves the
+    // last merge height there; such grids have no nodata and no open edge)
+    for (size_t i = gtid; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
+        const int32_t a = ea[i], b = eb[i];
+        if (raise[a] == ~0ull) { raise[a] = dkey(0.0); atomicOr(&sc->err, ErrFlags::kNoConverge); }
+        if (raise[b] == ~0ull) { raise[b] = dkey(0.0); atomicOr(&sc->err, ErrFlags::kNoConverge); }
+    }
+}
+
+// raise_watershedMFD (newflow.cu:879-894) into the scratch DEM of pass 2.
+__global__ void k_flood_raise(const double* __restrict__ z, const uint8_t* __restrict__ mask,
+                              const int32_t* __restrict__ ws, const unsigned long long* __restrict__ raise,
+                              double* __restrict__ zf, ModelConsts k, DevScalars* sc) {
+    if (sc->sinkcount_pass1 == 0) return;
+    const size_t N = (size_t)k.W * k.H;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+        double v = z[c];
+        if (mask[c]) {
+            const unsigned long long r = raise[ws[c]];
+            if (dkey(v) < r) v = dkey_inv(r);
+        }
+        zf[c] = v;
+    }
+}
+
+// Epilogue of cuFlowDirection (routeflow.cu:934-953) and the host outlet check
+// of routeflow.cu:738-741, which the reference applies after its device copy.
+__global__ void k_fd_epilogue(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
+                              const uint8_t* __restrict__ mfd, uint8_t* __restrict__ fd, double* z, ModelConsts k,
+                              DevScalars* sc) {
+    const size_t N = (size_t)k.W * k.H;
+    const int outlet = sc->outlet;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+        uint8_t v = sfd[c];
+        if (k.flow_type != 0 && mask[c] && mfd[c] != 0) v = mfd[c];
+        if ((int)c == outlet) v = 16;
+        fd[c] = v;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (sc->sinkcount_pass1 == 0) sc->sinkcount = 0;
+        const double zo = z[outlet];
+        sc->outlet_z_clim = zo;
+        unsigned long long low = sc->lowest_key;
+        const unsigned long long k1000 = dkey(1000.0);
+        if (low > k1000) low = k1000;
+        if (low < dkey(zo)) z[outlet] = dkey_inv(low) - 0.0001;
+    }
+}
+
+__global__ void k_fd_reset(DevScalars* sc) {
+    sc->lowest_key = ~0ull;
+    sc->sink_counter = sc->flat_counter = 0;
+    sc->sinkcount_pass1 = 0;
+    sc->sinkcount = 0;
+    sc->plateau_sweeps = 0;
+    sc->n_cand = 0;
+    sc->n_sinks = 0;
+    sc->n_edges = 0;
+}
+
+__global__ void k_cand_reset(DevScalars* sc) { sc->n_cand = 0; }
+
+}  // namespace
+
+int coop_blocks_for(const void* kernel, int threads, size_t smem) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
+    if (per < 1) per = 1;
+    return sms * per;
+}
+
+static lem_status coop(const void* fn, int blocks, int threads, void** args, cudaStream_t st, uint64_t* launches) {
+    LEM_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, 0, st));
+    ++*launches;
+    return LEM_OK;
+}
+
+static int flat_blocks(size_t n, int threads, int cap_blocks) {
+    size_t b = (n + threads - 1) / threads;
+    if (b > (size_t)cap_blocks) b = cap_blocks;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, cudaStream_t st, uint64_t* launches) {
+    const size_t N = (size_t)k.W * k.H;
+    const dim3 fdb(FD_BX, FD_BY), fdg((k.W + FD_BX - 1) / FD_BX, (k.H + FD_BY - 1) / FD_BY);
+    const int T = 256;
+    const int big = 152 * 32;
+    const int coopT = 256;
+    const int coopB = s.max_coop_blocks;
+    int pass;
+    k_fd_reset<<<1, 1, 0, st>>>(s.sc);
+    ++*launches;
+    // pass 1 on the DEM as uploaded at the start of the stage
+    pass = 1;
+    k_flowdirs<<<fdg, fdb, 0, st>>>(s.z, s.mask, s.slopes, s.sfd, s.mfd, k, s.sc, pass);
+    k_plateau_init<<<flat_blocks(N, T, big), T, 0, st>>>(s.mask, s.sfd, s.mfd, s.sp, s.list_a + 0, k, s.sc, pass);
+    *launches += 2;
+    {
+        // candidates live in the second half of `pending` (an int32 grid) during FD
+        const double* zz = s.z;
+        float* sp = s.sp;
+        const int32_t* cand = s.list_a;
+        int32_t* la = s.list_b;
+        int32_t* lb = s.pending;
+        int32_t* mark = s.mark;
+        ModelConsts kk = k;
+        DevScalars* sc = s.sc;
+        void* args[] = {(void*)&zz, (void*)&sp, (void*)&cand, (void*)&la, (void*)&lb, (void*)&mark, (void*)&kk,
+                        (void*)&sc, (void*)&pass};
+        lem_status r = coop((const void*)k_plateau_relax, coopB, coopT, args, st, launches);
+        if (r != LEM_OK) return r;
+    }
+    k_plateau_final<<<flat_blocks(N, T, big), T, 0, st>>>(s.z, s.sp, s.list_a, s.sfd, s.mfd, s.slopes, k, s.sc, pass);
+    ++*launches;
+    // sink flooding on the pass-1 codes
+    k_flood_init<<<flat_blocks(N, T, big), T, 0, st>>>(s.mask, s.sfd, s.ws, s.list_b, s.raise, k, s.sc);
+    ++*launches;
+    {
+        const double* zz = s.z;
+        int32_t* ws = s.ws;
+        const int32_t* sinks = s.list_b;
+        ModelConsts kk = k;
+        DevScalars* sc = s.sc;
+        void* args[] = {(void*)&zz, (void*)&ws, (void*)&sinks, (void*)&kk, (void*)&sc};
+        lem_status r = coop((const void*)k_flood_merge, coopB, coopT, args, st, launches);
+        if (r != LEM_OK) return r;
+    }
+    {
+        int32_t* ws = s.ws;
+        int32_t* la = s.list_a;
+        int32_t* lb = s.pending;
+        ModelConsts kk = k;
+        DevScalars* sc = s.sc;
+        void* args[] = {(void*)&ws, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc};
+        lem_status r = coop((const void*)k_flood_jump, coopB, coopT, args, st, launches);
+        if (r != LEM_OK) return r;
+    }
+    int logcap = 0;
+    while ((1ll << logcap) < s.ecap) ++logcap;
+    LEM_CUDA_TRY(cudaMemsetAsync(s.ekey, 0xff, sizeof(unsigned long long) * s.ecap, st));
+    LEM_CUDA_TRY(cudaMemsetAsync(s.ewt, 0xff, sizeof(unsigned long long) * s.ecap, st));
+    k_flood_edges<<<flat_blocks(N, T, big), T, 0, st>>>(s.z, s.mask, s.ws, s.ekey, s.ewt, logcap, k, s.sc);
+    ++*launches;
+    static int32_t epoch = 0;
+    ++epoch;
+    k_flood_compact<<<flat_blocks((size_t)s.ecap, T, big), T, 0, st>>>(s.ekey, s.ewt, s.ecap, s.edge_a, s.edge_b,
+                                                                         s.edge_w, s.raise, s.label_seen, epoch, s.sc);
+    ++*launches;
+    {
+        const int32_t* ea = s.edge_a;
+        const int32_t* eb = s.edge_b;
+        const unsigned long long* ew = s.edge_w;
+        unsigned long long* raise = s.raise;
+        DevScalars* sc = s.sc;
+        void* args[] = {(void*)&ea, (void*)&eb, (void*)&ew, (void*)&raise, (void*)&sc};
+        lem_status r = coop((const void*)k_flood_spill, coopB, coopT, args, st, launches);
+        if (r != LEM_OK) return r;
+    }
+    k_flood_raise<<<flat_blocks(N, T, big), T, 0, st>>>(s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc);
+    ++*launches;
+    // pass 2 on the raised DEM: codes only
+    pass = 2;
+    k_cand_reset<<<1, 1, 0, st>>>(s.sc);
+    k_flowdirs<<<fdg, fdb, 0, st>>>(s.zf, s.mask, nullptr, s.sfd, s.mfd, k, s.sc, pass);
+    k_plateau_init<<<flat_blocks(N, T, big), T, 0, st>>>(s.mask, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, pass);
+    *launches += 3;
+    {
+        const double* zz = s.zf;
+        float* sp = s.sp;
+        const int32_t* cand = s.list_a;
+        int32_t* la = s.list_b;
+        int32_t* lb = s.pending;
+        int32_t* mark = s.mark;
+        ModelConsts kk = k;
+        DevScalars* sc = s.sc;
+        void* args[] = {(void*)&zz, (void*)&sp, (void*)&cand, (void*)&la, (void*)&lb, (void*)&mark, (void*)&kk,
+                        (void*)&sc, (void*)&pass};
+        lem_status r = coop((const void*)k_plateau_relax, coopB, coopT, args, st, launches);
+        if (r != LEM_OK) return r;
+    }
+    k_plateau_final<<<flat_blocks(N, T, big), T, 0, st>>>(s.zf, s.sp, s.list_a, s.sfd, s.mfd, nullptr, k, s.sc, pass);
+    k_fd_epilogue<<<flat_blocks(N, T, big), T, 0, st>>>(s.mask, s.sfd, s.mfd, s.fd, s.z, k, s.sc);
+    *launches += 2;
+    LEM_CUDA_TRY(cudaGetLastError());
+    return LEM_OK;
+}
+
+// cooperative kernels of this file, for the co-residency query at handle creation
+const void* fd_coop_kernels[] = {(const void*)k_plateau_relax, (const void*)k_flood_merge,
+                                 (const void*)k_flood_jump, (const void*)k_flood_spill};
+extern const int fd_coop_kernel_count = 4;
+
+}  // namespace lem

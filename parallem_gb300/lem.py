@@ -1,0 +1,207 @@
+"""Python host mirror of the C ABI in include/lem_gb300.h (ctypes).
+
+The reference drives its path from C++ (lem.cpp) through cuFlowDirection,
+computeRunOffWeights/calcpropsSFD/correctmfdflow and erosionGPU on a host Data
+struct.  ``Model`` offers the same three stage calls and a whole ``step`` on a
+handle whose state stays resident on the GPU; fields are copied to or from
+numpy arrays only on request.  There is no CPU path: without the CUDA library
+every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "liblem_gb300.so")
+
+# lem_field
+FIELDS = {
+    "dem": 0, "mask": 1, "fd": 2, "sfd": 3, "slopes": 4, "slopeptr": 5, "fa": 6, "runoff": 7,
+    "stone": 8, "fines": 9, "soilT": 10, "soilM": 11, "soilB": 12, "nut": 13, "totB": 14,
+    "ero": 15, "inci": 16, "geli": 17, "depo": 18, "dz": 19, "wC": 20, "wP": 21,
+    "contrib": 22, "watershed": 23,
+}
+INT_FIELDS = {"mask", "fd", "sfd", "contrib", "watershed"}
+STATE_FIELDS = ("stone", "fines", "soilT", "soilM", "soilB", "nut", "totB")
+
+STEP_SET_OUTLET_FROM_FA = 0x1
+STEP_KEEP_DIAGNOSTICS = 0x2
+STEP_CONTRIB = 0x4
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "capacity exceeded", 3: "iteration cap reached",
+          4: "CUDA error", 5: "out of memory", 6: "call out of order"}
+
+
+class LemError(RuntimeError):
+    def __init__(self, code: int, what: str, detail: str = ""):
+        super().__init__(f"{what}: {STATUS.get(code, code)} {detail}".strip())
+        self.code = code
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("cellsize", C.c_double)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("flow_direction_type", C.c_int32), ("mfd_proportions", C.c_int32),
+        ("soil_struct", C.c_int32), ("profile_permeability", C.c_int32),
+        ("q_threshold", C.c_double), ("g_slope", C.c_double), ("kappa", C.c_double),
+        ("g_flowlim", C.c_double), ("flow_a", C.c_double), ("flow_b", C.c_double),
+        ("max_incision", C.c_double), ("ddk", C.c_double), ("dck", C.c_double), ("dgk", C.c_double),
+        ("temp_inflex", C.c_double), ("temp_sens", C.c_double),
+    ]
+
+
+class Climate(C.Structure):
+    _fields_ = [("rain", C.c_double), ("temp", C.c_double), ("recompute", C.c_int32)]
+
+
+class Totals(C.Structure):
+    _fields_ = [
+        ("tot_e", C.c_double), ("tot_i", C.c_double), ("tot_g", C.c_double), ("tot_d", C.c_double),
+        ("tot_weather_c", C.c_double), ("tot_weather_p", C.c_double), ("tot_bio", C.c_double),
+        ("fa_max", C.c_double), ("rain", C.c_double), ("temp", C.c_double),
+        ("sinkcount", C.c_int32), ("outlet", C.c_int32), ("initial_sinks", C.c_int32),
+        ("initial_flats", C.c_int32), ("plateau_sweeps", C.c_int32), ("flood_edges", C.c_int32),
+        ("fa_uncomputed", C.c_int32), ("sed_uncomputed", C.c_int32),
+    ]
+
+
+# every exported symbol of include/lem_gb300.h with its ctypes signature
+_H = C.c_void_p
+SIGNATURES = {
+    "lem_create": (C.c_int, [C.POINTER(GridDesc), C.POINTER(Params), C.c_double, C.c_double, C.POINTER(_H)]),
+    "lem_destroy": (C.c_int, [_H]),
+    "lem_set_field": (C.c_int, [_H, C.c_int, C.c_void_p]),
+    "lem_get_field": (C.c_int, [_H, C.c_int, C.c_void_p]),
+    "lem_set_outlet": (C.c_int, [_H, C.c_int32]),
+    "lem_flow_direction": (C.c_int, [_H]),
+    "lem_flow_accumulation": (C.c_int, [_H, C.c_uint32]),
+    "lem_erosion": (C.c_int, [_H, C.c_uint32]),
+    "lem_set_climate": (C.c_int, [_H, C.POINTER(Climate)]),
+    "lem_step": (C.c_int, [_H, C.POINTER(Climate), C.c_uint32]),
+    "lem_synchronize": (C.c_int, [_H]),
+    "lem_get_totals": (C.c_int, [_H, C.POINTER(Totals)]),
+    "lem_stream": (C.c_void_p, [_H]),
+    "lem_launch_count": (C.c_uint64, [_H]),
+    "lem_status_string": (C.c_char_p, [C.c_int]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build it with parallem_gb300.build.build()")
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(code: int, what: str):
+    if code != 0:
+        detail = load().lem_status_string(code).decode() if code == 4 else ""
+        raise LemError(code, what, detail)
+
+
+def make_params(**kw) -> Params:
+    from .scenario import DEFAULT_PAR
+    d = dict(DEFAULT_PAR, **kw)
+    return Params(**{k: d[k] for k, _ in Params._fields_})
+
+
+class Model:
+    """One DEM and its model state resident on the current CUDA device."""
+
+    def __init__(self, dem: np.ndarray, cellsize: float, init_rain: float, init_temp: float,
+                 params: Params | None = None):
+        L = load()
+        self.H, self.W = dem.shape
+        self.N = self.H * self.W
+        self.params = params if params is not None else make_params()
+        h = _H()
+        _check(L.lem_create(C.byref(GridDesc(self.W, self.H, float(cellsize))), C.byref(self.params),
+                            float(init_rain), float(init_temp), C.byref(h)), "lem_create")
+        self.h = h
+        self.set("dem", dem)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().lem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- fields ---------------------------------------------------------------
+    def set(self, name: str, arr: np.ndarray):
+        n = 8 * self.N if name == "slopes" else self.N
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        if a.size != n:
+            raise ValueError(f"{name}: expected {n} values, got {a.size}")
+        _check(load().lem_set_field(self.h, FIELDS[name], a.ctypes.data), f"lem_set_field({name})")
+
+    def get(self, name: str) -> np.ndarray:
+        if name in INT_FIELDS:
+            out = np.empty((self.H, self.W), np.int32)
+        elif name == "slopes":
+            out = np.empty((self.H, self.W, 8), np.float64)
+        else:
+            out = np.empty((self.H, self.W), np.float64)
+        _check(load().lem_get_field(self.h, FIELDS[name], out.ctypes.data), f"lem_get_field({name})")
+        return out
+
+    def set_state(self, state: dict):
+        for f in STATE_FIELDS:
+            if f in state:
+                self.set(f, state[f])
+        if "slopes" in state:
+            self.set("slopes", state["slopes"])
+        if "outlet" in state:
+            _check(load().lem_set_outlet(self.h, int(state["outlet"])), "lem_set_outlet")
+
+    # -- the path ---------------------------------------------------------------
+    def flow_direction(self):
+        _check(load().lem_flow_direction(self.h), "lem_flow_direction")
+
+    def flow_accumulation(self, flags: int = 0):
+        _check(load().lem_flow_accumulation(self.h, flags), "lem_flow_accumulation")
+
+    def erosion(self, flags: int = 0):
+        _check(load().lem_erosion(self.h, flags), "lem_erosion")
+
+    def set_climate(self, rain: float, temp: float, recompute: bool):
+        _check(load().lem_set_climate(self.h, C.byref(Climate(rain, temp, int(bool(recompute))))), "lem_set_climate")
+
+    def step(self, rain: float, temp: float, recompute: bool, flags: int = 0):
+        _check(load().lem_step(self.h, C.byref(Climate(rain, temp, int(bool(recompute)))), flags), "lem_step")
+
+    def synchronize(self):
+        _check(load().lem_synchronize(self.h), "lem_synchronize")
+
+    def totals(self) -> dict:
+        t = Totals()
+        _check(load().lem_get_totals(self.h, C.byref(t)), "lem_get_totals")
+        return {k: getattr(t, k) for k, _ in Totals._fields_}
+
+    @property
+    def stream(self) -> int:
+        return int(load().lem_stream(self.h) or 0)
+
+    @property
+    def launches(self) -> int:
+        return int(load().lem_launch_count(self.h))
