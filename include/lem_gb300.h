@@ -153,7 +153,9 @@ lem_status lem_destroy(lem_handle* h);
 
 /* Host <-> device copies of one field (synchronous).  The first LEM_F_DEM upload
  * also fixes the mask (dem != -9999, createmask in MEM_kernels/memory.cu:217-242)
- * and the DEM that the initial climate grids were built from. */
+ * and the DEM that the initial climate grids were built from.  LEM_F_FD and
+ * LEM_F_SFD may be set (int32 codes, -9999 outside the catchment) to run the
+ * later stages from given directions; MASK, CONTRIB and WATERSHED are read only. */
 lem_status lem_set_field(lem_handle* h, lem_field f, const void* host);
 lem_status lem_get_field(lem_handle* h, lem_field f, void* host);
 lem_status lem_set_outlet(lem_handle* h, int32_t cell);  /* init_setoutletcell result */
@@ -174,6 +176,29 @@ lem_status lem_get_totals(lem_handle* h, lem_totals* out);            /* synchro
 
 /* The handle's cudaStream_t, for callers that order their own work after it. */
 void* lem_stream(lem_handle* h);
+
+/* Makes `device` current for the calling host thread in this library (its CUDA
+ * runtime is linked statically, so the caller's own runtime state is not
+ * shared).  Handles are created on the device current at lem_create. */
+lem_status lem_select_device(int32_t device);
+
+/* Device timing on the handle's stream: lem_event_record places event `slot`
+ * (0..15) on the stream; lem_event_elapsed waits for event `to` and returns the
+ * milliseconds between the two records. */
+lem_status lem_event_record(lem_handle* h, int32_t slot);
+lem_status lem_event_elapsed(lem_handle* h, int32_t from, int32_t to, float* ms);
+
+/* Per-kernel timing: when enabled every kernel launch of the handle is
+ * bracketed by two events on its stream.  lem_profile_read synchronises,
+ * returns launches and summed device milliseconds per kernel name since the
+ * previous read (or since enabling) and starts a new interval. */
+typedef struct lem_kernel_stat {
+    char name[48];
+    uint32_t launches;
+    double total_ms;
+} lem_kernel_stat;
+lem_status lem_set_profiling(lem_handle* h, int32_t on);
+lem_status lem_profile_read(lem_handle* h, lem_kernel_stat* out, int32_t cap, int32_t* count);
 
 /* Kernel launches issued by this handle since creation (for launch accounting). */
 uint64_t lem_launch_count(lem_handle* h);

@@ -21,6 +21,43 @@ extern const int mod_coop_kernel_count;
 
 static thread_local std::string g_last_error;
 
+struct Profiler {
+    struct Rec {
+        const char* name;
+        int a, b;
+    };
+    std::vector<cudaEvent_t> pool;
+    std::vector<Rec> recs;
+    size_t used = 0;
+    int open_a = -1;
+    const char* open_name = nullptr;
+    int take() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return -1;
+            pool.push_back(e);
+        }
+        return (int)used++;
+    }
+};
+
+void profiler_begin(Profiler* p, const char* name, cudaStream_t st) {
+    const int a = p->take();
+    if (a < 0) return;
+    cudaEventRecord(p->pool[a], st);
+    p->open_a = a;
+    p->open_name = name;
+}
+
+void profiler_end(Profiler* p, cudaStream_t st) {
+    if (p->open_a < 0) return;
+    const int b = p->take();
+    if (b < 0) return;
+    cudaEventRecord(p->pool[b], st);
+    p->recs.push_back({p->open_name, p->open_a, b});
+    p->open_a = -1;
+}
+
 lem_status cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
     char buf[512];
     snprintf(buf, sizeof buf, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
@@ -46,6 +83,10 @@ struct lem_handle {
     void* staging = nullptr;  // pinned host buffer of 8*N floats / doubles
     size_t staging_bytes = 0;
     DevScalars* host_sc = nullptr;  // pinned mirror of the device scalars
+    Profiler prof;
+    bool profiling = false;
+    cudaEvent_t events[16] = {};
+    Launch launch() { return Launch{st, &launches, profiling ? &prof : nullptr}; }
 };
 
 namespace {
@@ -277,6 +318,9 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
 lem_status lem_destroy(lem_handle* h) {
     if (!h) return LEM_ERR_INVALID;
     if (h->st) cudaStreamSynchronize(h->st);
+    for (cudaEvent_t e : h->prof.pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : h->events)
+        if (e) cudaEventDestroy(e);
     for (void* q : h->allocs) cudaFree(q);
     if (h->staging) cudaFreeHost(h->staging);
     if (h->host_sc) cudaFreeHost(h->host_sc);
@@ -321,7 +365,16 @@ lem_status lem_set_field(lem_handle* h, lem_field f, const void* host) {
         LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
         return LEM_OK;
     }
-    if (field_is_int(f)) return LEM_ERR_INVALID;  // codes and the mask are computed, not set
+    if (f == LEM_F_FD || f == LEM_F_SFD) {
+        // int32 codes; -9999 (outside the catchment) keeps its low byte 0xF1
+        const int32_t* src = static_cast<const int32_t*>(host);
+        uint8_t* t = static_cast<uint8_t*>(h->staging);
+        for (size_t i = 0; i < N; ++i) t[i] = (uint8_t)(src[i] & 0xff);
+        LEM_CUDA_TRY(cudaMemcpyAsync(f == LEM_F_FD ? s.fd : s.sfd, t, N, cudaMemcpyHostToDevice, h->st));
+        LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+        return LEM_OK;
+    }
+    if (field_is_int(f)) return LEM_ERR_INVALID;  // the mask, counts and labels are computed, not set
     float* dst = float_field(h, f);
     if (!dst) return LEM_ERR_INVALID;
     const double* src = static_cast<const double*>(host);
@@ -419,19 +472,19 @@ lem_status lem_set_climate(lem_handle* h, const lem_climate* c) {
 lem_status lem_flow_direction(lem_handle* h) {
     if (!h) return LEM_ERR_INVALID;
     if (!h->dem_set) return LEM_ERR_STATE;
-    return launch_flow_direction(h->s, h->k, h->st, &h->launches);
+    return launch_flow_direction(h->s, h->k, h->launch());
 }
 
 lem_status lem_flow_accumulation(lem_handle* h, uint32_t flags) {
     if (!h) return LEM_ERR_INVALID;
     if (!h->dem_set) return LEM_ERR_STATE;
-    return launch_flow_accumulation(h->s, h->k, h->c, flags, h->st, &h->launches);
+    return launch_flow_accumulation(h->s, h->k, h->c, flags, h->launch());
 }
 
 lem_status lem_erosion(lem_handle* h, uint32_t flags) {
     if (!h) return LEM_ERR_INVALID;
     if (!h->dem_set) return LEM_ERR_STATE;
-    return launch_erosion(h->s, h->k, h->c, flags, h->st, &h->launches);
+    return launch_erosion(h->s, h->k, h->c, flags, h->launch());
 }
 
 lem_status lem_step(lem_handle* h, const lem_climate* c, uint32_t flags) {
@@ -495,6 +548,59 @@ lem_status lem_get_totals(lem_handle* h, lem_totals* o) {
 }
 
 void* lem_stream(lem_handle* h) { return h ? (void*)h->st : nullptr; }
+
+lem_status lem_select_device(int32_t device) {
+    LEM_CUDA_TRY(cudaSetDevice(device));
+    return LEM_OK;
+}
+
+lem_status lem_event_record(lem_handle* h, int32_t slot) {
+    if (!h || slot < 0 || slot >= 16) return LEM_ERR_INVALID;
+    if (!h->events[slot]) LEM_CUDA_TRY(cudaEventCreate(&h->events[slot]));
+    LEM_CUDA_TRY(cudaEventRecord(h->events[slot], h->st));
+    return LEM_OK;
+}
+
+lem_status lem_event_elapsed(lem_handle* h, int32_t from, int32_t to, float* ms) {
+    if (!h || !ms || from < 0 || from >= 16 || to < 0 || to >= 16 || !h->events[from] || !h->events[to])
+        return LEM_ERR_INVALID;
+    LEM_CUDA_TRY(cudaEventSynchronize(h->events[to]));
+    LEM_CUDA_TRY(cudaEventElapsedTime(ms, h->events[from], h->events[to]));
+    return LEM_OK;
+}
+
+lem_status lem_set_profiling(lem_handle* h, int32_t on) {
+    if (!h) return LEM_ERR_INVALID;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    h->profiling = on != 0;
+    h->prof.recs.clear();
+    h->prof.used = 0;
+    return LEM_OK;
+}
+
+lem_status lem_profile_read(lem_handle* h, lem_kernel_stat* out, int32_t cap, int32_t* count) {
+    if (!h || !count || (cap > 0 && !out)) return LEM_ERR_INVALID;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    std::vector<lem_kernel_stat> agg;
+    for (const Profiler::Rec& r : h->prof.recs) {
+        float ms = 0.f;
+        LEM_CUDA_TRY(cudaEventElapsedTime(&ms, h->prof.pool[r.a], h->prof.pool[r.b]));
+        size_t j = 0;
+        while (j < agg.size() && std::strncmp(agg[j].name, r.name, sizeof(agg[j].name)) != 0) ++j;
+        if (j == agg.size()) {
+            lem_kernel_stat z{};
+            std::strncpy(z.name, r.name, sizeof(z.name) - 1);
+            agg.push_back(z);
+        }
+        agg[j].launches += 1;
+        agg[j].total_ms += ms;
+    }
+    h->prof.recs.clear();
+    h->prof.used = 0;
+    *count = (int32_t)agg.size();
+    for (int32_t i = 0; i < cap && i < (int32_t)agg.size(); ++i) out[i] = agg[i];
+    return LEM_OK;
+}
 
 uint64_t lem_launch_count(lem_handle* h) { return h ? h->launches : 0; }
 

@@ -72,12 +72,39 @@ struct DevState {
     int32_t max_coop_blocks;    // co-resident blocks of the cooperative kernels
 };
 
+// Optional per-kernel timing with CUDA events on the handle's stream.
+struct Profiler;
+void profiler_begin(Profiler* p, const char* name, cudaStream_t st);
+void profiler_end(Profiler* p, cudaStream_t st);
+
+// Where and how a stage launches: the handle's stream, its launch counter and
+// (when enabled) the profiler that brackets every launch with events.
+struct Launch {
+    cudaStream_t st;
+    uint64_t* count;
+    Profiler* prof;
+    void pre(const char* name) const {
+        if (prof) profiler_begin(prof, name, st);
+    }
+    void post() const {
+        if (prof) profiler_end(prof, st);
+        ++*count;
+    }
+};
+
+#define LEM_LAUNCH(L, kern, grid, block, ...)                  \
+    do {                                                       \
+        (L).pre(#kern);                                        \
+        kern<<<(grid), (block), 0, (L).st>>>(__VA_ARGS__);     \
+        (L).post();                                            \
+    } while (0)
+
 // stage launchers (stream-ordered, no host synchronisation)
-lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, cudaStream_t st, uint64_t* launches);
+lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const Launch& L);
 lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
-                                    cudaStream_t st, uint64_t* launches);
+                                    const Launch& L);
 lem_status launch_erosion(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
-                          cudaStream_t st, uint64_t* launches);
+                          const Launch& L);
 int coop_blocks_for(const void* kernel, int threads, size_t smem);
 
 }  // namespace lem

@@ -216,23 +216,20 @@ __global__ void k_fa_reset(DevScalars* sc) {
 }  // namespace
 
 lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
-                                    cudaStream_t st, uint64_t* launches) {
+                                    const Launch& L) {
     const size_t N = (size_t)k.W * k.H;
     const int T = 256;
     size_t nb = (N + T - 1) / T;
     const int blocks = (int)(nb > 152 * 32 ? 152 * 32 : nb);
-    k_fa_reset<<<1, 1, 0, st>>>(s.sc);
-    ++*launches;
+    LEM_LAUNCH(L, k_fa_reset, 1, 1, s.sc);
     const float* prop = nullptr;
     if (k.flow_type != 0 && k.mfd_props) {
-        k_calcprops<<<blocks, T, 0, st>>>(s.mask, s.fd, s.slopes, s.prop, N);
-        ++*launches;
+        LEM_LAUNCH(L, k_calcprops, blocks, T, s.mask, s.fd, s.slopes, s.prop, N);
         prop = s.prop;
     }
     int32_t* contrib = (flags & LEM_STEP_CONTRIB) ? s.contrib : nullptr;
-    k_fa_prep<<<blocks, T, 0, st>>>(s.z, s.mask, s.fd, s.stone, s.totB, s.soilM, s.w, s.fa, s.pending, contrib,
-                                     s.list_a, k, c, s.sc);
-    ++*launches;
+    LEM_LAUNCH(L, k_fa_prep, blocks, T, s.z, s.mask, s.fd, s.stone, s.totB, s.soilM, s.w, s.fa, s.pending, contrib,
+               s.list_a, k, c, s.sc);
     {
         const uint8_t* mask = s.mask;
         const uint8_t* fd = s.fd;
@@ -245,15 +242,15 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, con
         DevScalars* sc = s.sc;
         void* args[] = {(void*)&mask, (void*)&fd, (void*)&w, (void*)&prop, (void*)&fa, (void*)&pending,
                         (void*)&contrib, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc};
+        L.pre("k_fa_walk");
         LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fa_walk, dim3(s.max_coop_blocks), dim3(256), args,
-                                                 0, st));
-        ++*launches;
+                                                 0, L.st));
+        L.post();
     }
     if (flags & LEM_STEP_SET_OUTLET_FROM_FA) {
-        k_fa_argmax<<<blocks, T, 0, st>>>(s.fa, N, s.sc, 0);
-        k_fa_argmax<<<blocks, T, 0, st>>>(s.fa, N, s.sc, 1);
-        k_fa_argmax_set<<<1, 1, 0, st>>>(s.sc);
-        *launches += 3;
+        LEM_LAUNCH(L, k_fa_argmax, blocks, T, s.fa, N, s.sc, 0);
+        LEM_LAUNCH(L, k_fa_argmax, blocks, T, s.fa, N, s.sc, 1);
+        LEM_LAUNCH(L, k_fa_argmax_set, 1, 1, s.sc);
     }
     LEM_CUDA_TRY(cudaGetLastError());
     return LEM_OK;

@@ -20,7 +20,7 @@ namespace {
 constexpr int FD_BX = 32;
 constexpr int FD_BY = 8;
 constexpr float kFar = 20000000.0f;  // shortest_paths_plateaus_initMFD (newflow.cu:252)
-constexpr int kMaxRounds = 1 << 20;
+constexpr int kMaxRounds = 1 << 16;
 
 __device__ __forceinline__ unsigned long long key_nodata() { return dkey(-9999.0); }
 
@@ -692,9 +692,10 @@ int coop_blocks_for(const void* kernel, int threads, size_t smem) {
     return sms * per;
 }
 
-static lem_status coop(const void* fn, int blocks, int threads, void** args, cudaStream_t st, uint64_t* launches) {
-    LEM_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, 0, st));
-    ++*launches;
+static lem_status coop(const char* name, const void* fn, int blocks, void** args, const Launch& L) {
+    L.pre(name);
+    LEM_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(256), args, 0, L.st));
+    L.post();
     return LEM_OK;
 }
 
@@ -705,24 +706,19 @@ static int flat_blocks(size_t n, int threads, int cap_blocks) {
     return (int)b;
 }
 
-lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, cudaStream_t st, uint64_t* launches) {
+// One pass of FlowDirs + plateau routing.  Pass 1 reads the stage's DEM and
+// updates the persistent slopes; pass 2 reads the raised DEM.
+static lem_status direction_pass(const DevState& s, const ModelConsts& k, const Launch& L, int pass) {
     const size_t N = (size_t)k.W * k.H;
+    const int T = 256, big = 152 * 32;
     const dim3 fdb(FD_BX, FD_BY), fdg((k.W + FD_BX - 1) / FD_BX, (k.H + FD_BY - 1) / FD_BY);
-    const int T = 256;
-    const int big = 152 * 32;
-    const int coopT = 256;
-    const int coopB = s.max_coop_blocks;
-    int pass;
-    k_fd_reset<<<1, 1, 0, st>>>(s.sc);
-    ++*launches;
-    // pass 1 on the DEM as uploaded at the start of the stage
-    pass = 1;
-    k_flowdirs<<<fdg, fdb, 0, st>>>(s.z, s.mask, s.slopes, s.sfd, s.mfd, k, s.sc, pass);
-    k_plateau_init<<<flat_blocks(N, T, big), T, 0, st>>>(s.mask, s.sfd, s.mfd, s.sp, s.list_a + 0, k, s.sc, pass);
-    *launches += 2;
+    const double* zz = pass == 1 ? s.z : s.zf;
+    float* slopes = pass == 1 ? s.slopes : nullptr;
+    if (pass == 2) LEM_LAUNCH(L, k_cand_reset, 1, 1, s.sc);
+    LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, k, s.sc, pass);
+    LEM_LAUNCH(L, k_plateau_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, pass);
     {
-        // candidates live in the second half of `pending` (an int32 grid) during FD
-        const double* zz = s.z;
+        // candidates in list_a; frontiers in list_b and `pending` (an int32 grid unused in this stage)
         float* sp = s.sp;
         const int32_t* cand = s.list_a;
         int32_t* la = s.list_b;
@@ -732,14 +728,22 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, cudaSt
         DevScalars* sc = s.sc;
         void* args[] = {(void*)&zz, (void*)&sp, (void*)&cand, (void*)&la, (void*)&lb, (void*)&mark, (void*)&kk,
                         (void*)&sc, (void*)&pass};
-        lem_status r = coop((const void*)k_plateau_relax, coopB, coopT, args, st, launches);
+        lem_status r = coop("k_plateau_relax", (const void*)k_plateau_relax, s.max_coop_blocks, args, L);
         if (r != LEM_OK) return r;
     }
-    k_plateau_final<<<flat_blocks(N, T, big), T, 0, st>>>(s.z, s.sp, s.list_a, s.sfd, s.mfd, s.slopes, k, s.sc, pass);
-    ++*launches;
+    LEM_LAUNCH(L, k_plateau_final, flat_blocks(N, T, big), T, zz, s.sp, s.list_a, s.sfd, s.mfd, slopes, k, s.sc,
+               pass);
+    return LEM_OK;
+}
+
+lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const Launch& L) {
+    const size_t N = (size_t)k.W * k.H;
+    const int T = 256, big = 152 * 32;
+    lem_status r;
+    LEM_LAUNCH(L, k_fd_reset, 1, 1, s.sc);
+    if ((r = direction_pass(s, k, L, 1)) != LEM_OK) return r;
     // sink flooding on the pass-1 codes
-    k_flood_init<<<flat_blocks(N, T, big), T, 0, st>>>(s.mask, s.sfd, s.ws, s.list_b, s.raise, k, s.sc);
-    ++*launches;
+    LEM_LAUNCH(L, k_flood_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.ws, s.list_b, s.raise, k, s.sc);
     {
         const double* zz = s.z;
         int32_t* ws = s.ws;
@@ -747,8 +751,7 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, cudaSt
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
         void* args[] = {(void*)&zz, (void*)&ws, (void*)&sinks, (void*)&kk, (void*)&sc};
-        lem_status r = coop((const void*)k_flood_merge, coopB, coopT, args, st, launches);
-        if (r != LEM_OK) return r;
+        if ((r = coop("k_flood_merge", (const void*)k_flood_merge, s.max_coop_blocks, args, L)) != LEM_OK) return r;
     }
     {
         int32_t* ws = s.ws;
@@ -757,20 +760,17 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, cudaSt
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
         void* args[] = {(void*)&ws, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc};
-        lem_status r = coop((const void*)k_flood_jump, coopB, coopT, args, st, launches);
-        if (r != LEM_OK) return r;
+        if ((r = coop("k_flood_jump", (const void*)k_flood_jump, s.max_coop_blocks, args, L)) != LEM_OK) return r;
     }
     int logcap = 0;
     while ((1ll << logcap) < s.ecap) ++logcap;
-    LEM_CUDA_TRY(cudaMemsetAsync(s.ekey, 0xff, sizeof(unsigned long long) * s.ecap, st));
-    LEM_CUDA_TRY(cudaMemsetAsync(s.ewt, 0xff, sizeof(unsigned long long) * s.ecap, st));
-    k_flood_edges<<<flat_blocks(N, T, big), T, 0, st>>>(s.z, s.mask, s.ws, s.ekey, s.ewt, logcap, k, s.sc);
-    ++*launches;
+    LEM_CUDA_TRY(cudaMemsetAsync(s.ekey, 0xff, sizeof(unsigned long long) * s.ecap, L.st));
+    LEM_CUDA_TRY(cudaMemsetAsync(s.ewt, 0xff, sizeof(unsigned long long) * s.ecap, L.st));
+    LEM_LAUNCH(L, k_flood_edges, flat_blocks(N, T, big), T, s.z, s.mask, s.ws, s.ekey, s.ewt, logcap, k, s.sc);
     static int32_t epoch = 0;
     ++epoch;
-    k_flood_compact<<<flat_blocks((size_t)s.ecap, T, big), T, 0, st>>>(s.ekey, s.ewt, s.ecap, s.edge_a, s.edge_b,
-                                                                         s.edge_w, s.raise, s.label_seen, epoch, s.sc);
-    ++*launches;
+    LEM_LAUNCH(L, k_flood_compact, flat_blocks((size_t)s.ecap, T, big), T, s.ekey, s.ewt, s.ecap, s.edge_a, s.edge_b,
+               s.edge_w, s.raise, s.label_seen, epoch, s.sc);
     {
         const int32_t* ea = s.edge_a;
         const int32_t* eb = s.edge_b;
@@ -778,34 +778,11 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, cudaSt
         unsigned long long* raise = s.raise;
         DevScalars* sc = s.sc;
         void* args[] = {(void*)&ea, (void*)&eb, (void*)&ew, (void*)&raise, (void*)&sc};
-        lem_status r = coop((const void*)k_flood_spill, coopB, coopT, args, st, launches);
-        if (r != LEM_OK) return r;
+        if ((r = coop("k_flood_spill", (const void*)k_flood_spill, s.max_coop_blocks, args, L)) != LEM_OK) return r;
     }
-    k_flood_raise<<<flat_blocks(N, T, big), T, 0, st>>>(s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc);
-    ++*launches;
-    // pass 2 on the raised DEM: codes only
-    pass = 2;
-    k_cand_reset<<<1, 1, 0, st>>>(s.sc);
-    k_flowdirs<<<fdg, fdb, 0, st>>>(s.zf, s.mask, nullptr, s.sfd, s.mfd, k, s.sc, pass);
-    k_plateau_init<<<flat_blocks(N, T, big), T, 0, st>>>(s.mask, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, pass);
-    *launches += 3;
-    {
-        const double* zz = s.zf;
-        float* sp = s.sp;
-        const int32_t* cand = s.list_a;
-        int32_t* la = s.list_b;
-        int32_t* lb = s.pending;
-        int32_t* mark = s.mark;
-        ModelConsts kk = k;
-        DevScalars* sc = s.sc;
-        void* args[] = {(void*)&zz, (void*)&sp, (void*)&cand, (void*)&la, (void*)&lb, (void*)&mark, (void*)&kk,
-                        (void*)&sc, (void*)&pass};
-        lem_status r = coop((const void*)k_plateau_relax, coopB, coopT, args, st, launches);
-        if (r != LEM_OK) return r;
-    }
-    k_plateau_final<<<flat_blocks(N, T, big), T, 0, st>>>(s.zf, s.sp, s.list_a, s.sfd, s.mfd, nullptr, k, s.sc, pass);
-    k_fd_epilogue<<<flat_blocks(N, T, big), T, 0, st>>>(s.mask, s.sfd, s.mfd, s.fd, s.z, k, s.sc);
-    *launches += 2;
+    LEM_LAUNCH(L, k_flood_raise, flat_blocks(N, T, big), T, s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc);
+    if ((r = direction_pass(s, k, L, 2)) != LEM_OK) return r;
+    LEM_LAUNCH(L, k_fd_epilogue, flat_blocks(N, T, big), T, s.mask, s.sfd, s.mfd, s.fd, s.z, k, s.sc);
     LEM_CUDA_TRY(cudaGetLastError());
     return LEM_OK;
 }

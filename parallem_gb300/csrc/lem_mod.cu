@@ -472,16 +472,15 @@ __global__ void k_mod_reset(DevScalars* sc) {
 }  // namespace
 
 lem_status launch_erosion(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
-                          cudaStream_t st, uint64_t* launches) {
+                          const Launch& L) {
     const size_t N = (size_t)k.W * k.H;
     const int T = 256;
     size_t nb = (N + T - 1) / T;
     const int blocks = (int)(nb > 152 * 32 ? 152 * 32 : nb);
-    k_mod_reset<<<1, 1, 0, st>>>(s.sc);
-    k_erosion<<<blocks, T, 0, st>>>(s.z, s.z_init, s.mask, s.slopes, s.fa, s.fines, s.nut, s.soilT, s.stone, s.totB,
-                                     s.slopeptr, s.ero, s.inci, s.geli, k, c, s.sc);
-    k_sed_prep<<<blocks, T, 0, st>>>(s.mask, s.fd, s.depo, s.pending, s.list_a, k, s.sc);
-    *launches += 3;
+    LEM_LAUNCH(L, k_mod_reset, 1, 1, s.sc);
+    LEM_LAUNCH(L, k_erosion, blocks, T, s.z, s.z_init, s.mask, s.slopes, s.fa, s.fines, s.nut, s.soilT, s.stone,
+               s.totB, s.slopeptr, s.ero, s.inci, s.geli, k, c, s.sc);
+    LEM_LAUNCH(L, k_sed_prep, blocks, T, s.mask, s.fd, s.depo, s.pending, s.list_a, k, s.sc);
     {
         const uint8_t* mask = s.mask;
         const uint8_t* fd = s.fd;
@@ -501,15 +500,15 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, const Climate
         void* args[] = {(void*)&mask, (void*)&fd,    (void*)&prop,  (void*)&ero,     (void*)&inci,
                         (void*)&geli, (void*)&depo,  (void*)&stone, (void*)&fines,   (void*)&soilT,
                         (void*)&pending, (void*)&la, (void*)&lb,    (void*)&kk,      (void*)&sc};
+        L.pre("k_sed_walk");
         LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sed_walk, dim3(s.max_coop_blocks), dim3(256), args,
-                                                 0, st));
-        ++*launches;
+                                                 0, L.st));
+        L.post();
     }
     const bool diag = (flags & LEM_STEP_KEEP_DIAGNOSTICS) != 0;
-    k_final<<<blocks, T, 0, st>>>(s.z, s.z_init, s.mask, s.fa, s.ero, s.inci, s.geli, s.depo, s.soilT, s.stone,
-                                   s.fines, s.soilM, s.soilB, s.nut, s.totB, diag ? s.dz : nullptr,
-                                   diag ? s.wc : nullptr, diag ? s.wp : nullptr, s.temp_tab, k, c, s.sc);
-    ++*launches;
+    LEM_LAUNCH(L, k_final, blocks, T, s.z, s.z_init, s.mask, s.fa, s.ero, s.inci, s.geli, s.depo, s.soilT, s.stone,
+               s.fines, s.soilM, s.soilB, s.nut, s.totB, diag ? s.dz : nullptr, diag ? s.wc : nullptr,
+               diag ? s.wp : nullptr, s.temp_tab, k, c, s.sc);
     LEM_CUDA_TRY(cudaGetLastError());
     return LEM_OK;
 }

@@ -71,6 +71,10 @@ class Totals(C.Structure):
     ]
 
 
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint32), ("total_ms", C.c_double)]
+
+
 # every exported symbol of include/lem_gb300.h with its ctypes signature
 _H = C.c_void_p
 SIGNATURES = {
@@ -89,6 +93,11 @@ SIGNATURES = {
     "lem_stream": (C.c_void_p, [_H]),
     "lem_launch_count": (C.c_uint64, [_H]),
     "lem_status_string": (C.c_char_p, [C.c_int]),
+    "lem_select_device": (C.c_int, [C.c_int32]),
+    "lem_event_record": (C.c_int, [_H, C.c_int32]),
+    "lem_event_elapsed": (C.c_int, [_H, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
+    "lem_set_profiling": (C.c_int, [_H, C.c_int32]),
+    "lem_profile_read": (C.c_int, [_H, C.POINTER(KernelStat), C.c_int32, C.POINTER(C.c_int32)]),
 }
 
 _lib = None
@@ -150,7 +159,7 @@ class Model:
     # -- fields ---------------------------------------------------------------
     def set(self, name: str, arr: np.ndarray):
         n = 8 * self.N if name == "slopes" else self.N
-        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        a = np.ascontiguousarray(arr, dtype=np.int32 if name in INT_FIELDS else np.float64).reshape(-1)
         if a.size != n:
             raise ValueError(f"{name}: expected {n} values, got {a.size}")
         _check(load().lem_set_field(self.h, FIELDS[name], a.ctypes.data), f"lem_set_field({name})")
@@ -205,3 +214,25 @@ class Model:
     @property
     def launches(self) -> int:
         return int(load().lem_launch_count(self.h))
+
+    def record(self, slot: int):
+        _check(load().lem_event_record(self.h, slot), "lem_event_record")
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        _check(load().lem_event_elapsed(self.h, a, b, C.byref(ms)), "lem_event_elapsed")
+        return float(ms.value)
+
+    def profiling(self, on: bool):
+        _check(load().lem_set_profiling(self.h, int(bool(on))), "lem_set_profiling")
+
+    def profile(self) -> dict:
+        """{kernel name: (launches, total device ms)} since the previous read."""
+        arr = (KernelStat * 64)()
+        n = C.c_int32()
+        _check(load().lem_profile_read(self.h, arr, 64, C.byref(n)), "lem_profile_read")
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(min(n.value, 64))}
+
+
+def select_device(device: int):
+    _check(load().lem_select_device(int(device)), "lem_select_device")
