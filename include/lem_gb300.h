@@ -132,7 +132,11 @@ typedef enum lem_field {
                                 (needs LEM_STEP_CONTRIB)                             */
     LEM_F_WATERSHED = 23, /* I  basin label of the last sink flooding (0 = drains
                                 off the grid or to nodata)                           */
-    LEM_F_COUNT = 24
+    LEM_F_DEM_ROUTED = 24,/* D  the DEM the final codes were computed on: the stage's
+                                DEM raised to the spill heights; read only           */
+    LEM_F_SFD_PASS1 = 25, /* I  SFD codes after the first plateau pass, the codes the
+                                basins of the sink flooding follow; read only        */
+    LEM_F_COUNT = 26
 } lem_field;
 
 /* Step flags. */

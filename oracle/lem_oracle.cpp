@@ -518,6 +518,8 @@ int oracle_flow_direction(oracle_state* s, const lem_params* p) {
     s->init_sinks = sinks;
     s->init_flats = flats;
     int sweeps = route_plateaus(g, s->mask, zd.data(), s->slopes, mfd.data(), sfd.data(), s->shortest_paths);
+    if (s->sfd_pass1)
+        for (long j = 0; j < N; ++j) s->sfd_pass1[j] = sfd[j];
     // routeflow.cu:893-909: sinks left after plateau routing
     int sinkcount = 0;
     for (long j = 0; j < N; ++j)

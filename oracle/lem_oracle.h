@@ -53,6 +53,7 @@ typedef struct oracle_state {
     int32_t* watershed;    /* N   optional: basin labels of the flooding (NULL ok) */
     int32_t* contrib;      /* N   optional: SFD contributing-cell counts (NULL ok) */
     double* dem_routed;    /* N   optional: the DEM the final codes were computed on (raised) */
+    int32_t* sfd_pass1;    /* N   optional: SFD codes after the first plateau pass */
     int32_t outlet;        /* Data.outletcellidx                            */
     double rain, temp;     /* Data.rain / Data.temp of the step             */
     double last_rain, last_temp;

@@ -37,8 +37,8 @@ class LemClimate(C.Structure):
 _FP_FIELDS = ["dem", "mask", "slopes", "prop", "fd", "sfd", "fa", "runoff", "slopeptr", "stone", "fines",
               "soilT", "soilM", "soilB", "nut", "totB", "ero", "inci", "geli", "depo", "dz", "wC", "wP",
               "rainmat", "tempmat", "last_rainmat", "last_tempmat", "shortest_paths", "watershed", "contrib",
-              "dem_routed"]
-_TYPES = {"mask": _I, "fd": _I, "sfd": _I, "shortest_paths": _F, "watershed": _I, "contrib": _I}
+              "dem_routed", "sfd_pass1"]
+_TYPES = {"mask": _I, "fd": _I, "sfd": _I, "shortest_paths": _F, "watershed": _I, "contrib": _I, "sfd_pass1": _I}
 
 
 class OracleStateC(C.Structure):
@@ -112,6 +112,7 @@ class OracleModel:
         a["watershed"] = np.zeros((h, w), np.int32) if diagnostics else None
         a["contrib"] = np.zeros((h, w), np.int32) if diagnostics else None
         a["dem_routed"] = np.zeros((h, w), np.float64) if diagnostics else None
+        a["sfd_pass1"] = np.zeros((h, w), np.int32) if diagnostics else None
         self.a = a
         self.s = OracleStateC()
         self.s.W, self.s.H, self.s.cellsize = w, h, self.cellsize

@@ -99,6 +99,7 @@ int ref_flow_direction(oracle_state* s, const lem_params* p) {
     int sweeps = 0;
     plateau_loop(g, mask, dem, slopes, fd, sfd, sp, low, csize, &sweeps);
     std::copy(slopes.begin(), slopes.begin() + 8 * g.N, s->slopes);  // routeflow.cu:883
+    if (s->sfd_pass1) std::copy(sfd.begin(), sfd.begin() + g.N, s->sfd_pass1);
     int sinkcount = 0;
     for (size_t j = 0; j < g.N; ++j)
         if (mask[j] == 1 && sfd[j] == 0) sinkcount++;

@@ -127,7 +127,8 @@ void dreybrodt_table(std::vector<float>& tab) {
 }
 
 bool field_is_int(lem_field f) {
-    return f == LEM_F_MASK || f == LEM_F_FD || f == LEM_F_SFD || f == LEM_F_CONTRIB || f == LEM_F_WATERSHED;
+    return f == LEM_F_MASK || f == LEM_F_FD || f == LEM_F_SFD || f == LEM_F_CONTRIB || f == LEM_F_WATERSHED ||
+           f == LEM_F_DEM_ROUTED || f == LEM_F_SFD_PASS1;
 }
 
 float* float_field(lem_handle* h, lem_field f) {
@@ -247,6 +248,7 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
     ALLOC(s.sfd, N);
     ALLOC(s.mfd, N);
     ALLOC(s.fd, N);
+    ALLOC(s.sfd1, N);
     ALLOC(s.sp, N);
     ALLOC(s.ws, N);
     ALLOC(s.pending, N);
@@ -394,6 +396,14 @@ lem_status lem_get_field(lem_handle* h, lem_field f, void* host) {
         case LEM_F_DEM:
             LEM_CUDA_TRY(cudaMemcpy(host, s.z, sizeof(double) * N, cudaMemcpyDeviceToHost));
             return LEM_OK;
+        case LEM_F_DEM_ROUTED: {
+            const lem_status rs = sync_scalars(h);
+            if (rs != LEM_OK) return rs;
+            // without sinks the second pass does not run and the stage's DEM is the routed one
+            LEM_CUDA_TRY(cudaMemcpy(host, h->host_sc->sinkcount_pass1 ? s.zf : s.z, sizeof(double) * N,
+                                    cudaMemcpyDeviceToHost));
+            return LEM_OK;
+        }
         case LEM_F_MASK: {
             uint8_t* m = static_cast<uint8_t*>(h->staging);
             LEM_CUDA_TRY(cudaMemcpy(m, s.mask, N, cudaMemcpyDeviceToHost));
@@ -402,9 +412,11 @@ lem_status lem_get_field(lem_handle* h, lem_field f, void* host) {
             return LEM_OK;
         }
         case LEM_F_FD:
-        case LEM_F_SFD: {
+        case LEM_F_SFD:
+        case LEM_F_SFD_PASS1: {
             uint8_t* buf = static_cast<uint8_t*>(h->staging);
-            LEM_CUDA_TRY(cudaMemcpy(buf, f == LEM_F_FD ? s.fd : s.sfd, N, cudaMemcpyDeviceToHost));
+            const uint8_t* src = f == LEM_F_FD ? s.fd : (f == LEM_F_SFD ? s.sfd : s.sfd1);
+            LEM_CUDA_TRY(cudaMemcpy(buf, src, N, cudaMemcpyDeviceToHost));
             LEM_CUDA_TRY(cudaMemcpy(buf + N, s.mask, N, cudaMemcpyDeviceToHost));
             const lem_status rs = sync_scalars(h);
             if (rs != LEM_OK) return rs;

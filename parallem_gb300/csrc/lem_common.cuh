@@ -15,7 +15,13 @@ __host__ __device__ constexpr int dir_dy(int d) { return (d == 0 || d == 1 || d 
 __host__ __device__ constexpr uint32_t dir_bit(int d) { return d == 0 ? 64u : d == 1 ? 128u : (1u << (d - 2)); }
 // direction index of a single-bit code (bit b of the byte maps to d = (b + 2) % 8)
 __host__ __device__ inline int bit_dir(uint32_t code) {
-    return (code == 0 || (code & (code - 1))) ? -1 : (int)((__builtin_ctz(code) + 2) & 7);
+    if (code == 0 || (code & (code - 1))) return -1;
+#ifdef __CUDA_ARCH__
+    const int b = __ffs((int)code) - 1;
+#else
+    const int b = __builtin_ctz(code);
+#endif
+    return (b + 2) & 7;
 }
 // Donor scan order of CalcMFD / MFDsedbud (mfd_simple.cu:95-165): neighbours E, SE,
 // S, SW, W, NW, N, NE; the neighbour in direction d donates when its code has the

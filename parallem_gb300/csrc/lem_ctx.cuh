@@ -46,6 +46,7 @@ struct DevState {
     uint8_t* sfd;       // SFD code (low byte; masked = 0xF1)
     uint8_t* mfd;       // MFD code
     uint8_t* fd;        // final code after the epilogue
+    uint8_t* sfd1;      // SFD code after the first plateau pass (the basis of the basin labels)
     float* sp;          // plateau distances
     int32_t* ws;        // basin labels / pointers
     int32_t* pending;   // wave in-degrees

@@ -344,8 +344,9 @@ __global__ void k_plateau_final(const double* __restrict__ z, const float* __res
 // Sink flooding (floodingDriver, routeflow.cu:202-676).
 // init_watershedMFD (newflow.cu:352-420): sink cells get a unique id (cell+1),
 // other cells point at their SFD receiver, masked and edge cells are basin 0.
-__global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd, int32_t* ws,
-                             int32_t* sinks, unsigned long long* raise, ModelConsts k, DevScalars* sc) {
+__global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
+                             uint8_t* __restrict__ sfd1, int32_t* ws, int32_t* sinks, unsigned long long* raise,
+                             ModelConsts k, DevScalars* sc) {
     const int W = k.W, H = k.H;
     const size_t N = (size_t)W * H;
     int nsink = 0;
@@ -355,6 +356,7 @@ __global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __
         if (c < N) {
             const int x = (int)(c % W), y = (int)(c / W);
             int32_t v = 0;
+            sfd1[c] = sfd[c];
             if (mask[c]) {
                 const uint8_t s = sfd[c];
                 sink = (s == 0);
@@ -743,7 +745,7 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
     LEM_LAUNCH(L, k_fd_reset, 1, 1, s.sc);
     if ((r = direction_pass(s, k, L, 1)) != LEM_OK) return r;
     // sink flooding on the pass-1 codes
-    LEM_LAUNCH(L, k_flood_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.ws, s.list_b, s.raise, k, s.sc);
+    LEM_LAUNCH(L, k_flood_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.sfd1, s.ws, s.list_b, s.raise, k, s.sc);
     {
         const double* zz = s.z;
         int32_t* ws = s.ws;

@@ -22,9 +22,9 @@ FIELDS = {
     "dem": 0, "mask": 1, "fd": 2, "sfd": 3, "slopes": 4, "slopeptr": 5, "fa": 6, "runoff": 7,
     "stone": 8, "fines": 9, "soilT": 10, "soilM": 11, "soilB": 12, "nut": 13, "totB": 14,
     "ero": 15, "inci": 16, "geli": 17, "depo": 18, "dz": 19, "wC": 20, "wP": 21,
-    "contrib": 22, "watershed": 23,
+    "contrib": 22, "watershed": 23, "dem_routed": 24, "sfd_pass1": 25,
 }
-INT_FIELDS = {"mask", "fd", "sfd", "contrib", "watershed"}
+INT_FIELDS = {"mask", "fd", "sfd", "contrib", "watershed", "sfd_pass1"}
 STATE_FIELDS = ("stone", "fines", "soilT", "soilM", "soilB", "nut", "totB")
 
 STEP_SET_OUTLET_FROM_FA = 0x1

@@ -3,7 +3,8 @@
 Every comparison starts both sides from the same state and runs one stage or
 one step.  Tolerances (stated per check):
 * direction codes, sink counts, contributing-cell counts: bit-exact;
-* slopes: 2e-6 relative (fp32 storage of the reference's fp64 quotient);
+* slopes: 2e-6 relative + 1e-12 absolute (fp32 storage of the reference's
+  fp64 quotient);
 * accumulation and elevation: 1e-5 relative (the north-star bound);
 * process grids: |gpu - oracle| <= 1e-5 |oracle| + 1e-8 max|oracle| (fp32
   arithmetic; the absolute floor covers sums that cancel, e.g. dz);
@@ -50,12 +51,12 @@ def resync(o, g):
     g.set_state({f: o[f] for f in STATE_FIELDS} | {"slopes": o["slopes"], "outlet": o.outlet})
 
 
-def close(name, gv, ov, mask, rtol=1e-5, afrac=1e-8):
+def close(name, gv, ov, mask, rtol=1e-5, afrac=1e-8, atol=0.0):
     gv, ov = np.asarray(gv)[mask], np.asarray(ov)[mask]
     both_nan = np.isnan(gv) & np.isnan(ov)
     scale = np.nanmax(np.abs(ov)) if ov.size else 0.0
     err = np.where(both_nan, 0.0, np.abs(gv - ov))
-    bad = ~(err <= rtol * np.abs(ov) + afrac * scale)
+    bad = ~(err <= rtol * np.abs(ov) + afrac * scale + atol)
     assert not bad.any(), (f"{name}: {int(bad.sum())} of {bad.size} outside tolerance, max err "
                            f"{np.nanmax(err):.3e} (scale {scale:.3e})")
 
@@ -68,7 +69,9 @@ def check_fd(o, g, mask):
     assert t["initial_sinks"] == o.s.init_sinks and t["initial_flats"] == o.s.init_flats
     gs, os_ = g.get("slopes"), o["slopes"]
     np.testing.assert_array_equal(gs != 0, os_ != 0)
-    close("slopes", gs, os_, np.broadcast_to(mask[..., None], gs.shape), rtol=2e-6, afrac=0.0)
+    # fp32 slopes: 2e-6 relative, plus 1e-12 absolute for near-flat drops whose
+    # fp32 estimate carries the 2^-44 |z| split error
+    close("slopes", gs, os_, np.broadcast_to(mask[..., None], gs.shape), rtol=2e-6, afrac=0.0, atol=1e-12)
     ws_g, ws_o = g.get("watershed"), o["watershed"]
     if o.s.sinkcount:
         pairs = set(zip(ws_g[mask].tolist(), ws_o[mask].tolist()))
