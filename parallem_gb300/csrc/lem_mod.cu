@@ -133,11 +133,23 @@ __global__ void __launch_bounds__(256)
             in = st + bed;
             if (in > k.max_incision) in = k.max_incision;
         }
-        // gelifluction (eroincidep.cu:154-198)
-        const float T = clim_temp(c, z, z_init, i, outlet, outlet_z);
+        // gelifluction (eroincidep.cu:154-198).  The quartic kappa(T) cancels near
+        // its roots (T ~ -16.8 and 8.6 C) and the range test has edges at -20 and 8.87 C:
+        // there the temperature and kappa take the reference's fp64 arithmetic.
+        float T = clim_temp(c, z, z_init, i, outlet, outlet_z);
         float kappa = k.kappa;
         if (T >= -20.f && T <= 8.87f)
             kappa = 0.15711f - 0.011835f * T - 0.001195f * T * T + 0.000038f * T * T * T + 0.000002f * T * T * T * T;
+        if (fabsf(T - 8.87f) < 1e-3f || fabsf(T + 20.0f) < 1e-3f || fabsf(kappa) < 4e-3f) {
+            const double zc = c.from_current_dem ? (((int)i == outlet) ? outlet_z : z[i]) : z_init[i];
+            const double Td = c.temp - ((zc - kMinHeight) * 0.0065);
+            double kd = (double)k.kappa;
+            if (Td >= -20. && Td <= 8.87)
+                kd = 0.15711 - 0.011835 * Td - 0.001195 * Td * Td + 0.000038 * Td * Td * Td +
+                     0.000002 * Td * Td * Td * Td;
+            kappa = (float)kd;
+            T = (float)Td;
+        }
         float scaler = 1.0f - (fav / k.g_flowlim);
         if (fav > k.g_flowlim) scaler = 0.0f;
         float sthr = sp;

@@ -7,7 +7,7 @@ one step.  Tolerances (stated per check):
   fp64 quotient);
 * accumulation and elevation: 1e-5 relative (the north-star bound);
 * process grids: |gpu - oracle| <= 1e-5 |oracle| + 1e-8 max|oracle| (fp32
-  arithmetic; the absolute floor covers sums that cancel, e.g. dz);
+  arithmetic); dz, a difference of sums that cancel, gets 1e-6 max|oracle|;
 * budget totals: 1e-5 relative.
 At sizes the oracle cannot finish quickly the checks are size-independent
 invariants of the outputs (local accumulation balance, donor deposition,
@@ -56,7 +56,7 @@ def close(name, gv, ov, mask, rtol=1e-5, afrac=1e-8, atol=0.0):
     both_nan = np.isnan(gv) & np.isnan(ov)
     scale = np.nanmax(np.abs(ov)) if ov.size else 0.0
     err = np.where(both_nan, 0.0, np.abs(gv - ov))
-    bad = ~(err <= rtol * np.abs(ov) + afrac * scale + atol)
+    bad = ~(err <= rtol * np.abs(ov) + afrac * scale + atol) & ~both_nan
     assert not bad.any(), (f"{name}: {int(bad.sum())} of {bad.size} outside tolerance, max err "
                            f"{np.nanmax(err):.3e} (scale {scale:.3e})")
 
@@ -92,7 +92,10 @@ def check_mod(o, g, mask, diag=False):
     for f in MOD_FIELDS:
         close(f, g.get(f), o[f], mask)
     if diag:
-        for f in ("dz", "wC", "wP"):
+        # dz = depo - ero - inci - geli cancels: its error is bounded by the
+        # fp32 rounding of its terms, 1e-6 of the field's largest magnitude
+        close("dz", g.get("dz"), o["dz"], mask, afrac=1e-6)
+        for f in ("wC", "wP"):
             close(f, g.get(f), o[f], mask)
     close("dem", g.get("dem"), o["dem"], mask, rtol=1e-9, afrac=0.0)
     t = g.totals()
