@@ -224,6 +224,9 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
     k.temp_inflex = (float)h->p.temp_inflex;
     k.temp_sens = (float)h->p.temp_sens;
     k.rescale_conc = (float)(1 / (10000 / (cs * cs)));
+    k.rescale_conc_lo = (float)((1 / (10000 / (cs * cs))) - (double)k.rescale_conc);
+    k.q_threshold_lo = (float)(h->p.q_threshold - (double)k.q_threshold);
+    k.g_flowlim_lo = (float)(h->p.g_flowlim - (double)k.g_flowlim);
     k.rescale_weather = (float)(10000 * (10000 / (cs * cs)));
     k.rescale_veg = (float)(10000 / (cs * cs));
     k.erod_const = (float)((0.043 * (params->soil_struct - 2.)) + (0.033 * (params->profile_permeability - 3.)));

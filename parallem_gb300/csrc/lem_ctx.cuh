@@ -22,6 +22,9 @@ struct ModelConsts {  // per-handle constants derived on the host in double
     float q_threshold, g_slope, kappa, g_flowlim, flow_a, flow_b, max_incision;
     float ddk, dck, dgk, temp_inflex, temp_sens;
     float rescale_conc;     // 1 / (10000 / cs^2)          eroincidep.cu:310
+    float rescale_conc_lo;  //   its fp32 tail (rescale_conc + rescale_conc_lo = the fp64 value)
+    float q_threshold_lo;   //   fp32 tail of Qthreshold
+    float g_flowlim_lo;     //   fp32 tail of Gflowlim
     float rescale_weather;  // 10000 * (10000 / cs^2)      eroincidep.cu:628
     float rescale_veg;      // 10000 / cs^2                Data.cpp:124
     float erod_const;       // 0.043*(struct-2) + 0.033*(perm-3)

@@ -119,7 +119,10 @@ __global__ void __launch_bounds__(256)
         // conc_erosion (eroincidep.cu:89-152)
         float cslope = sp;
         if (cslope > 0.5f) cslope = 0.5f;
-        float f_temp = fav * k.rescale_conc - k.q_threshold;
+        // fa * cs^2/1e4 - Qthreshold cancels near the threshold: evaluate it on the
+        // (hi, lo) accumulation and the split constants
+        float f_temp = fmaf(f2.x, k.rescale_conc, -k.q_threshold) +
+                       (fmaf(f2.x, k.rescale_conc_lo, f2.y * k.rescale_conc) - k.q_threshold_lo);
         float in;
         if (f_temp < 0.0f) {
             f_temp = 0.0f;
@@ -150,8 +153,10 @@ __global__ void __launch_bounds__(256)
             kappa = (float)kd;
             T = (float)Td;
         }
-        float scaler = 1.0f - (fav / k.g_flowlim);
-        if (fav > k.g_flowlim) scaler = 0.0f;
+        // 1 - fa/Gflowlim cancels where fa approaches Gflowlim
+        const float gap = ((k.g_flowlim - f2.x) + k.g_flowlim_lo) - f2.y;
+        float scaler = gap / (k.g_flowlim + k.g_flowlim_lo);
+        if (gap < 0.0f) scaler = 0.0f;
         float sthr = sp;
         if (sthr > k.g_slope) sthr = k.g_slope;
         float g = kappa * sthr * scaler;

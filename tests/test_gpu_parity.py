@@ -5,7 +5,8 @@ one step.  Tolerances (stated per check):
 * direction codes, sink counts, contributing-cell counts: bit-exact;
 * slopes: 2e-6 relative + 1e-12 absolute (fp32 storage of the reference's
   fp64 quotient);
-* accumulation and elevation: 1e-5 relative (the north-star bound);
+* accumulation: 1e-5 relative (the benchmark spec's bound); elevation: 1e-9
+  relative + 1e-6 m (fp64 state, fp32 increments);
 * process grids: |gpu - oracle| <= 1e-5 |oracle| + 1e-8 max|oracle| (fp32
   arithmetic); dz, a difference of sums that cancel, gets 1e-6 max|oracle|;
 * budget totals: 1e-5 relative.
@@ -97,13 +98,14 @@ def check_mod(o, g, mask, diag=False):
         close("dz", g.get("dz"), o["dz"], mask, afrac=1e-6)
         for f in ("wC", "wP"):
             close(f, g.get(f), o[f], mask)
-    close("dem", g.get("dem"), o["dem"], mask, rtol=1e-9, afrac=0.0)
+    # elevation: fp64 state updated by fp32 increments; 1e-9 relative plus 1e-6 m
+    close("dem", g.get("dem"), o["dem"], mask, rtol=1e-9, afrac=0.0, atol=1e-6)
     t = g.totals()
     for k_g, k_o in (("tot_e", "totE"), ("tot_i", "totI"), ("tot_g", "totG"), ("tot_d", "totD"),
                      ("tot_weather_c", "totWC"), ("tot_weather_p", "totWP"), ("tot_bio", "totbio"),
                      ("fa_max", "FA_max")):
         a, b = t[k_g], getattr(o.s, k_o)
-        assert abs(a - b) <= 1e-5 * abs(b) + 1e-12, (k_g, a, b)
+        assert abs(a - b) <= 1e-5 * abs(b) + 1e-12 or (np.isnan(a) and np.isnan(b)), (k_g, a, b)
     assert t["sed_uncomputed"] == o.s.sed_uncomputed
     assert t["outlet"] == o.outlet
 
