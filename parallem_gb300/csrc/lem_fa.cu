@@ -192,7 +192,9 @@ __global__ void k_fa_walk(const uint8_t* __restrict__ mask, const uint8_t* __res
 // becomes the first cell holding the largest accumulation.
 __global__ void k_fa_argmax(const float2* __restrict__ fa, size_t N, DevScalars* sc, int phase) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
-        const unsigned long long kk = ffkey(fa[i]);
+        const float2 v = fa[i];
+        if (v.x != v.x) continue;  // NaN never wins the host scan (mfd_simple.cu:341)
+        const unsigned long long kk = ffkey(v);
         if (phase == 0)
             atomicMax(&sc->fa_max_key, kk);
         else if (kk == sc->fa_max_key)

@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(256)
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
         const float2 f2 = fa[i];
         const unsigned long long fk = ffkey(f2);
-        famax = fk > famax ? fk : famax;
+        if (f2.x == f2.x) famax = fk > famax ? fk : famax;  // the reduction skips NaN (thrust::maximum order)
         if (!mask[i]) {
             ero[i] = inci[i] = geli[i] = 0.0f;
             slopeptr[i] = 0.0f;
