@@ -33,9 +33,12 @@ __host__ __device__ constexpr int scan_dir(int k) { return (k + 2) & 7; }
 constexpr uint8_t kMaskedCode = 0xF1;
 constexpr double kNoData = -9999.0;
 
-// Order-preserving map of a double to uint64 (exact comparisons without the FP64 pipe).
+// Order-preserving map of a double to uint64 (exact comparisons without the FP64
+// pipe).  NaN maps to 0, which callers treat as "unordered": every comparison of
+// the reference involving a NaN elevation is false.
 __device__ __forceinline__ uint64_t dkey(double z) {
     uint64_t b = (uint64_t)__double_as_longlong(z);
+    if ((b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return 0;  // NaN
     if (b == 0x8000000000000000ull) b = 0;  // -0.0 == +0.0
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }

@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     for (int t = tid; t < (FD_BX + 2) * (FD_BY + 2); t += FD_BX * FD_BY) {
         int ly = t / (FD_BX + 2), lx = t % (FD_BX + 2);
         int gx = x0 + lx - 1, gy = y0 + ly - 1;
-        unsigned long long key = 0;  // 0 = outside the grid
+        unsigned long long key = 0;  // 0 = outside the grid or NaN: never compared
         float hi = 0.f, lo = 0.f;
         if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
             double v = z[(size_t)gy * W + gx];
@@ -92,6 +92,9 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
         const size_t self = (size_t)y * W + x;
         uint8_t cs = kMaskedCode, cm = kMaskedCode;
         if (mask[self]) {
+            cs = cm = 0;  // a NaN elevation compares false with every neighbour: no direction
+        }
+        if (mask[self] && skey[ly][lx] != 0) {
             const unsigned long long ks = skey[ly][lx];
             const unsigned long long knd = key_nodata();
             const float hs = shi[ly][lx], ls = slo[ly][lx];
@@ -253,7 +256,7 @@ __global__ void k_plateau_relax(const double* __restrict__ z, float* sp, const i
             const int x = c % W, y = c / W;
             const unsigned long long kc = dkey(z[c]);
             float best = kFar;
-            for (int d = 0; d < 8; ++d) {
+            for (int d = 0; kc != 0 && d < 8; ++d) {  // a NaN cell (key 0) equals no neighbour
                 const int nx = x + dir_dx(d), ny = y + dir_dy(d);
                 if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
                 const size_t nb = (size_t)ny * W + nx;
@@ -290,7 +293,7 @@ __global__ void k_plateau_relax(const double* __restrict__ z, float* sp, const i
                 const int x = c % W, y = c / W;
                 const unsigned long long kc = dkey(z[c]);
                 const float v = ld_sp(sp, c);
-                for (int d = 0; d < 8; ++d) {
+                for (int d = 0; kc != 0 && d < 8; ++d) {
                     const int nx = x + dir_dx(d), ny = y + dir_dy(d);
                     if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
                     const size_t nb = (size_t)ny * W + nx;
@@ -331,7 +334,7 @@ __global__ void k_plateau_final(const double* __restrict__ z, const float* __res
         if (!(v < kFar)) continue;
         const int x = c % W, y = c / W;
         const unsigned long long kc = dkey(z[c]);
-        for (int d = 0; d < 8; ++d) {
+        for (int d = 0; kc != 0 && d < 8; ++d) {
             const int nx = x + dir_dx(d), ny = y + dir_dy(d);
             if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
             const size_t nb = (size_t)ny * W + nx;
@@ -410,7 +413,7 @@ __global__ void k_flood_merge(const double* __restrict__ z, int32_t* ws, const i
             const unsigned long long kc = dkey(z[c]);
             const int32_t mine = __ldcg(ws + c);
             int32_t best = mine;
-            for (int d = 0; d < 8; ++d) {
+            for (int d = 0; kc != 0 && d < 8; ++d) {
                 const int nx = x + dir_dx(d), ny = y + dir_dy(d);
                 if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
                 const size_t nb = (size_t)ny * W + nx;
@@ -519,7 +522,8 @@ __global__ void k_flood_edges(const double* __restrict__ z, const uint8_t* __res
             const size_t nb = (size_t)ny * W + nx;
             const int32_t b = ws[nb];
             if (a == b) continue;
-            if (kz < dkey(z[nb])) continue;
+            const unsigned long long kn = dkey(z[nb]);
+            if (kz == 0 || kn == 0 || kz < kn) continue;  // zs[this] >= zs[idx] is false for NaN
             const unsigned long long key = ((unsigned long long)(uint32_t)min(a, b) << 32) | (uint32_t)max(a, b);
             uint64_t h = edge_hash(key, logcap);
             int probes = 0;
@@ -646,7 +650,8 @@ __global__ void k_flood_raise(const double* __restrict__ z, const uint8_t* __res
         double v = z[c];
         if (mask[c]) {
             const unsigned long long r = raise[ws[c]];
-            if (dkey(v) < r) v = dkey_inv(r);
+            const unsigned long long kv = dkey(v);
+            if (kv != 0 && kv < r) v = dkey_inv(r);  // zs < raise is false for NaN
         }
         zf[c] = v;
     }
