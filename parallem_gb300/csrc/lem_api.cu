@@ -289,6 +289,9 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
     ALLOC(s.edge_w, (size_t)cap);
     ALLOC(s.raise, N + 1);
     ALLOC(s.label_seen, N + 1);
+    ALLOC(s.comp, N + 1);
+    ALLOC(s.cdist, N + 1);
+    ALLOC(s.cmaxw, N + 1);
     ALLOC(s.sc, 1);
     ALLOC(s.temp_tab, (size_t)kTabN);
 #undef ALLOC

@@ -71,6 +71,9 @@ struct DevState {
     int32_t* edge_a; int32_t* edge_b; unsigned long long* edge_w;
     unsigned long long* raise;  // per label (label = cell + 1), ordered keys
     int32_t* label_seen;
+    int32_t* comp;              // component label of basins that never reach basin 0
+    unsigned long long* cdist;  //   their minimax distance to the component's label basin
+    unsigned long long* cmaxw;  //   the component's largest spanning-tree edge
     DevScalars* sc;
     float* temp_tab;
     int32_t max_coop_blocks;    // co-resident blocks of the cooperative kernels

@@ -589,11 +589,13 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
 // basin 0 through boundaries no higher than h (the bottleneck distance); it is
 // computed here as the fixpoint raise[a] = min(raise[a], max(w_ab, raise[b])).
 __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __restrict__ eb,
-                              const unsigned long long* __restrict__ ew, unsigned long long* raise, DevScalars* sc) {
+                              const unsigned long long* __restrict__ ew, unsigned long long* raise, int32_t* comp,
+                              unsigned long long* cdist, unsigned long long* cmaxw, DevScalars* sc) {
     if (sc->sinkcount_pass1 == 0) return;
     cg::grid_group grid = cg::this_grid();
     const int n = sc->n_edges;
     const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t gstride = (size_t)gridDim.x * blockDim.x;
     if (gtid == 0) {
         raise[0] = 0ull;  // basin 0 is done
         sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
@@ -628,16 +630,84 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
     }
     if (gtid == 0) {
         sc->spill_rounds = round + 1;
-        raise[0] = dkey(0.0);
+        sc->flag[3] = 0;
     }
     grid.sync();
-    // basins that never reach basin 0 keep height 0 (the reference leaves the
-    // last merge height there; such grids have no nodata and no open edge)
-    for (size_t i = gtid; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
-        const int32_t a = ea[i], b = eb[i];
-        if (raise[a] == ~0ull) { raise[a] = dkey(0.0); atomicOr(&sc->err, ErrFlags::kNoConverge); }
-        if (raise[b] == ~0ull) { raise[b] = dkey(0.0); atomicOr(&sc->err, ErrFlags::kNoConverge); }
+    // Basins that never reach basin 0 (walled in by NaN elevations, or a grid
+    // with no nodata and no open edge): the Kruskal pass leaves every basin of
+    // such a component the weight of the component's last merge, i.e. its
+    // largest spanning-tree edge (routeflow.cu:562-572).  It equals the largest
+    // minimax distance from any one basin of the component to the others.
+    for (size_t i = gtid; i < (size_t)n; i += gstride)
+        if (raise[ea[i]] == ~0ull || raise[eb[i]] == ~0ull) sc->flag[3] = 1;
+    grid.sync();
+    if (*((volatile int32_t*)&sc->flag[3])) {
+        // (a) component label = smallest basin label, by min-propagation over edges
+        for (size_t i = gtid; i < (size_t)n; i += gstride) {
+            if (raise[ea[i]] == ~0ull) comp[ea[i]] = ea[i];
+            if (raise[eb[i]] == ~0ull) comp[eb[i]] = eb[i];
+        }
+        if (gtid == 0) sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
+        grid.sync();
+        for (int r = 0;; ++r) {
+            if (gtid == 0) sc->flag[(r + 1) % 3] = 0;
+            int ch = 0;
+            for (size_t i = gtid; i < (size_t)n; i += gstride) {
+                const int32_t a = ea[i], b = eb[i];
+                if (raise[a] != ~0ull || raise[b] != ~0ull) continue;
+                const int32_t ca = __ldcg(comp + a), cb = __ldcg(comp + b);
+                if (ca < cb) { atomicMin(comp + b, ca); ch = 1; }
+                if (cb < ca) { atomicMin(comp + a, cb); ch = 1; }
+            }
+            if (ch) sc->flag[r % 3] = 1;
+            grid.sync();
+            if (*((volatile int32_t*)&sc->flag[r % 3]) == 0 || r >= kMaxRounds) break;
+        }
+        // (b) minimax distance to the component's label basin, in cdist
+        for (size_t i = gtid; i < (size_t)n; i += gstride) {
+            const int32_t a = ea[i], b = eb[i];
+            if (raise[a] == ~0ull) cdist[a] = (comp[a] == a) ? 0ull : ~0ull;
+            if (raise[b] == ~0ull) cdist[b] = (comp[b] == b) ? 0ull : ~0ull;
+        }
+        if (gtid == 0) sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
+        grid.sync();
+        for (int r = 0;; ++r) {
+            if (gtid == 0) sc->flag[(r + 1) % 3] = 0;
+            int ch = 0;
+            for (size_t i = gtid; i < (size_t)n; i += gstride) {
+                const int32_t a = ea[i], b = eb[i];
+                if (raise[a] != ~0ull || raise[b] != ~0ull) continue;
+                const unsigned long long w = ew[i];
+                const unsigned long long da = __ldcg(cdist + a), db = __ldcg(cdist + b);
+                const unsigned long long ca = w > db ? w : db, cb = w > da ? w : da;
+                if (ca < da) { atomicMin(cdist + a, ca); ch = 1; }
+                if (cb < db) { atomicMin(cdist + b, cb); ch = 1; }
+            }
+            if (ch) sc->flag[r % 3] = 1;
+            grid.sync();
+            if (*((volatile int32_t*)&sc->flag[r % 3]) == 0 || r >= kMaxRounds) break;
+        }
+        // (c) the component's largest distance, gathered at its label basin
+        for (size_t i = gtid; i < (size_t)n; i += gstride) {
+            const int32_t a = ea[i], b = eb[i];
+            if (raise[a] == ~0ull && comp[a] != a) atomicMax(cdist + comp[a], cdist[a]);
+            if (raise[b] == ~0ull && comp[b] != b) atomicMax(cdist + comp[b], cdist[b]);
+        }
+        grid.sync();
+        for (size_t i = gtid; i < (size_t)n; i += gstride) {
+            const int32_t a = ea[i], b = eb[i];
+            if (raise[a] == ~0ull) cmaxw[a] = cdist[comp[a]];
+            if (raise[b] == ~0ull) cmaxw[b] = cdist[comp[b]];
+        }
+        grid.sync();
+        for (size_t i = gtid; i < (size_t)n; i += gstride) {
+            const int32_t a = ea[i], b = eb[i];
+            if (raise[a] == ~0ull) raise[a] = cmaxw[a];
+            if (raise[b] == ~0ull) raise[b] = cmaxw[b];
+        }
     }
+    grid.sync();
+    if (gtid == 0) raise[0] = dkey(0.0);
 }
 
 // raise_watershedMFD (newflow.cu:879-894) into the scratch DEM of pass 2.
@@ -789,8 +859,12 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
         const int32_t* eb = s.edge_b;
         const unsigned long long* ew = s.edge_w;
         unsigned long long* raise = s.raise;
+        int32_t* comp = s.comp;
+        unsigned long long* cdist = s.cdist;
+        unsigned long long* cmaxw = s.cmaxw;
         DevScalars* sc = s.sc;
-        void* args[] = {(void*)&ea, (void*)&eb, (void*)&ew, (void*)&raise, (void*)&sc};
+        void* args[] = {(void*)&ea, (void*)&eb, (void*)&ew, (void*)&raise, (void*)&comp, (void*)&cdist,
+                        (void*)&cmaxw, (void*)&sc};
         if ((r = coop("k_flood_spill", (const void*)k_flood_spill, s.max_coop_blocks, args, L)) != LEM_OK) return r;
     }
     LEM_LAUNCH(L, k_flood_raise, flat_blocks(N, T, big), T, s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc);
