@@ -209,6 +209,29 @@ uint64_t lem_launch_count(lem_handle* h);
 
 const char* lem_status_string(lem_status s);
 
+/* Flow accumulation that allocates nothing.  No counterpart in the reference:
+ * it serves callers that must not allocate device memory themselves or through
+ * this library -- e.g. a host program that hands the path only buffers from its
+ * own device arena, or a memory-budgeted service that may not call cudaMalloc
+ * (a device-wide synchronisation that can also fail under fragmentation) on
+ * its request path.  Inputs and the output are the caller's device arrays:
+ * d_fd the int32 direction codes (-9999 outside the catchment, as Data.fd),
+ * d_weight the runoff weights, d_dem the DEM (cells equal to -9999 are outside
+ * and complete with zero flow, like correctmfdflow's okgrid); d_fa receives the
+ * accumulation of correctmfdflow with calcpropsSFD proportions (every donor
+ * passes its whole flow).  Intermediate data lives in one statically allocated
+ * device array sized for LEM_NOALLOC_MAX_CELLS cells (about 27 MB, held by
+ * every GPU that loads the library until the process exits); larger grids are
+ * rejected with LEM_ERR_CAPACITY before any work.  The first call on a device
+ * looks up that array's device address and should come before any stream
+ * capture on that device.  All calls share the array: calls whose work
+ * overlaps on the GPU (other threads or streams) race, so serialise them.  The
+ * call is stream-ordered on `stream` (NULL: the default stream) and returns
+ * after its work has finished. */
+#define LEM_NOALLOC_MAX_CELLS (1 << 20)
+lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const double* d_weight, const double* d_dem,
+                                       double* d_fa, int32_t width, int32_t height, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,8 @@
 
 #include <cooperative_groups.h>
 
+#include <mutex>
+
 #include "lem_wave.cuh"
 
 namespace cg = cooperative_groups;
@@ -255,6 +257,139 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, con
         LEM_LAUNCH(L, k_fa_argmax_set, 1, 1, s.sc);
     }
     LEM_CUDA_TRY(cudaGetLastError());
+    return LEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// lem_accumulate_flow_noalloc: the accumulation wave on caller-owned buffers,
+// with its intermediate data in one file-scope device array.
+namespace {
+
+constexpr size_t kNaCells = LEM_NOALLOC_MAX_CELLS;
+constexpr size_t kNaHead = 1024;  // DevScalars, rounded up
+static_assert(sizeof(DevScalars) <= kNaHead, "scalar block");
+constexpr size_t kNaOffCode = kNaHead;
+constexpr size_t kNaOffMask = kNaOffCode + kNaCells;
+constexpr size_t kNaOffPend = kNaOffMask + kNaCells;          // int32
+constexpr size_t kNaOffListA = kNaOffPend + 4 * kNaCells;     // int32
+constexpr size_t kNaOffListB = kNaOffListA + 4 * kNaCells;    // int32
+constexpr size_t kNaOffW = kNaOffListB + 4 * kNaCells;        // float
+constexpr size_t kNaOffFa = kNaOffW + 4 * kNaCells;           // float2
+constexpr size_t kNaBytes = kNaOffFa + 8 * kNaCells;
+
+// Scratch of the no-allocation entry point (every call shares it).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+struct NaDevice {
+    unsigned char* base = nullptr;  // device address of g_noalloc_scratch
+    int blocks = 0;                 // co-resident blocks of k_fa_walk
+};
+std::mutex g_na_mutex;
+NaDevice g_na[64];
+
+__global__ void k_na_reset(DevScalars* sc) {
+    sc->counters[0] = sc->counters[1] = sc->counters[2] = 0;
+    sc->fa_done = 0;
+    sc->err = 0;
+}
+
+// Codes, mask, weights, initial accumulation and in-degrees from the caller's
+// int32 codes and DEM (cells at -9999 are outside and complete with zero flow).
+__global__ void k_na_prep(const int32_t* __restrict__ fd_in, const double* __restrict__ w_in,
+                          const double* __restrict__ dem, uint8_t* __restrict__ code, uint8_t* __restrict__ mask,
+                          float* __restrict__ w, float2* __restrict__ fa, int32_t* __restrict__ pending,
+                          int32_t* ready, int W, int H, DevScalars* sc) {
+    const size_t N = (size_t)W * H;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = base + threadIdx.x;
+        bool src = false;
+        if (i < N) {
+            const int x = (int)(i % W), y = (int)(i / W);
+            const bool in = dem[i] != kNoData;
+            code[i] = (uint8_t)(fd_in[i] & 0xff);
+            mask[i] = in ? 1 : 0;
+            const float wi = (float)w_in[i];
+            w[i] = wi;
+            fa[i] = make_float2(in ? wi : 0.0f, 0.0f);
+            int32_t pend = in ? 0 : kBlocked;
+            for (int d = 0; in && d < 8; ++d) {
+                const int nx = x + dir_dx(d), ny = y + dir_dy(d);
+                if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+                const size_t n = (size_t)ny * W + nx;
+                if (donates((uint8_t)(fd_in[n] & 0xff), d) && dem[n] != kNoData) ++pend;
+            }
+            pending[i] = pend;
+            src = in && pend == 0;
+        }
+        wave_append(src, (int32_t)i, ready, &sc->counters[0], (int)N, &sc->err);
+    }
+}
+
+__global__ void k_na_out(const float2* __restrict__ fa, double* __restrict__ out, size_t N) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (double)fa[i].x + (double)fa[i].y;
+}
+
+}  // namespace
+
+extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const double* d_weight,
+                                                  const double* d_dem, double* d_fa, int32_t width,
+                                                  int32_t height, void* stream) {
+    if (!d_fd || !d_weight || !d_dem || !d_fa || width < 1 || height < 1) return LEM_ERR_INVALID;
+    const size_t N = (size_t)width * height;
+    if (N > kNaCells) return LEM_ERR_CAPACITY;  // the static scratch holds LEM_NOALLOC_MAX_CELLS cells
+    int dev = 0;
+    LEM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return LEM_ERR_INVALID;
+    NaDevice nd;
+    {
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        if (!g_na[dev].base) {
+            // once per device, with that device current: the device address of the array
+            void* ptr = nullptr;
+            LEM_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+            int per = 0, sms = 0;
+            LEM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fa_walk, 256, 0));
+            LEM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            g_na[dev].base = static_cast<unsigned char*>(ptr);
+            g_na[dev].blocks = (per < 1 ? 1 : per) * sms;
+        }
+        nd = g_na[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    DevScalars* sc = reinterpret_cast<DevScalars*>(nd.base);
+    uint8_t* code = nd.base + kNaOffCode;
+    uint8_t* mask = nd.base + kNaOffMask;
+    int32_t* pending = reinterpret_cast<int32_t*>(nd.base + kNaOffPend);
+    int32_t* la = reinterpret_cast<int32_t*>(nd.base + kNaOffListA);
+    int32_t* lb = reinterpret_cast<int32_t*>(nd.base + kNaOffListB);
+    float* w = reinterpret_cast<float*>(nd.base + kNaOffW);
+    float2* fa = reinterpret_cast<float2*>(nd.base + kNaOffFa);
+    const int T = 256;
+    const int blocks = (int)std::min<size_t>((N + T - 1) / T, 152 * 32);
+    k_na_reset<<<1, 1, 0, st>>>(sc);  // the array keeps the previous call's contents
+    k_na_prep<<<blocks, T, 0, st>>>(d_fd, d_weight, d_dem, code, mask, w, fa, pending, la, width, height, sc);
+    LEM_CUDA_TRY(cudaGetLastError());
+    {
+        const uint8_t* m = mask;
+        const uint8_t* c = code;
+        const float* ww = w;
+        const float* prop = nullptr;
+        int32_t* contrib = nullptr;
+        ModelConsts k{};
+        k.W = width;
+        k.H = height;
+        void* args[] = {(void*)&m, (void*)&c, (void*)&ww, (void*)&prop, (void*)&fa, (void*)&pending,
+                        (void*)&contrib, (void*)&la, (void*)&lb, (void*)&k, (void*)&sc};
+        LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fa_walk, dim3(nd.blocks), dim3(256), args, 0, st));
+    }
+    k_na_out<<<blocks, T, 0, st>>>(fa, d_fa, N);
+    LEM_CUDA_TRY(cudaGetLastError());
+    uint32_t err = 0;
+    LEM_CUDA_TRY(cudaMemcpyAsync(&err, &sc->err, sizeof err, cudaMemcpyDeviceToHost, st));
+    LEM_CUDA_TRY(cudaStreamSynchronize(st));
+    if (err & ErrFlags::kCapacity) return LEM_ERR_CAPACITY;
+    if (err) return LEM_ERR_NOCONVERGE;
     return LEM_OK;
 }
 

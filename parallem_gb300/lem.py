@@ -98,6 +98,8 @@ SIGNATURES = {
     "lem_event_elapsed": (C.c_int, [_H, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
     "lem_set_profiling": (C.c_int, [_H, C.c_int32]),
     "lem_profile_read": (C.c_int, [_H, C.POINTER(KernelStat), C.c_int32, C.POINTER(C.c_int32)]),
+    "lem_accumulate_flow_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                              C.c_int32, C.c_void_p]),
 }
 
 _lib = None
