@@ -111,81 +111,45 @@ __device__ __forceinline__ float prop_of(const float* prop, const uint8_t* mask,
     return prop ? prop[8 * n + slot] : (mask[n] ? 1.0f : 0.0f);
 }
 
-// The accumulation wave.  Round 0 starts at every source; MFD cells that
-// release more than one receiver queue the extra ones for the next round.
+// One cell of correctmfdflow's CalcMFD (mfd_simple.cu:31-171): the weight plus
+// the donors' accumulation in the order E, SE, S, SW, W, NW, N, NE, a negative
+// donor sum clamped to zero.
+struct FaCell {
+    const uint8_t* mask;
+    const uint8_t* fd;
+    const float* w;
+    const float* prop;
+    float2* fa;
+    int32_t* contrib;
+    int W, H;
+    __device__ __forceinline__ void cell(int32_t cur, int x, int y) const {
+        float2 acc = make_float2(0.f, 0.f);
+        int32_t cacc = 1;
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+            const int d = scan_dir(kk);
+            const int nx = x + dir_dx(d), ny = y + dir_dy(d);
+            if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+            const int32_t n = ny * W + nx;
+            if (!donates(__ldg(fd + n), d)) continue;
+            const float2 v = __ldcg(fa + n);
+            const float p = prop_of(prop, mask, n, (d + 4) & 7);
+            acc = ff_add(acc, p == 1.0f ? v : ff_scale(v, p));
+            if (contrib && __ldg(mask + n)) cacc += __ldcg(contrib + n);
+        }
+        if (acc.x < 0.0f) acc = make_float2(0.f, 0.f);
+        __stcg(fa + cur, ff_add(make_float2(__ldg(w + cur), 0.f), acc));
+        if (contrib) __stcg(contrib + cur, cacc);
+    }
+};
+
+// The accumulation wave: every source starts it; cells follow as their last
+// donor finishes.
 __global__ void k_fa_walk(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                           const float* __restrict__ w, const float* __restrict__ prop, float2* fa, int32_t* pending,
                           int32_t* contrib, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc) {
-    cg::grid_group grid = cg::this_grid();
-    const int W = k.W, H = k.H;
-    const size_t N = (size_t)W * H;
-    const size_t gstride = (size_t)gridDim.x * blockDim.x;
-    const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int32_t* cnt = sc->counters;  // cnt[0] holds the sources written by k_fa_prep
-    if (gtid == 0) cnt[1] = cnt[2] = 0;
-    grid.sync();
-    int done = 0;
-    int round = 0;
-    for (;; ++round) {
-        const int32_t* in = (round & 1) ? list_b : list_a;
-        int32_t* out = (round & 1) ? list_a : list_b;
-        const int nin = *((volatile int32_t*)&cnt[round % 3]);
-        if (nin == 0) break;
-        if (round > (1 << 24)) {
-            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
-            break;
-        }
-        if (gtid == 0) cnt[(round + 2) % 3] = 0;
-        for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)nin; base += gstride) {
-            const size_t it = base + threadIdx.x;
-            int32_t cur = it < (size_t)nin ? in[it] : -1;
-            int32_t extra[8];
-            int nextra = 0;
-            for (size_t steps = 0; cur >= 0 && steps < N; ++steps) {
-                const int x = cur % W, y = cur / W;
-                float2 acc = make_float2(0.f, 0.f);
-                int32_t cacc = 1;
-#pragma unroll
-                for (int kk = 0; kk < 8; ++kk) {
-                    const int d = scan_dir(kk);
-                    const int nx = x + dir_dx(d), ny = y + dir_dy(d);
-                    if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
-                    const size_t n = (size_t)ny * W + nx;
-                    if (!donates(fd[n], d)) continue;
-                    const float2 v = __ldcg(fa + n);
-                    const float p = prop_of(prop, mask, n, (d + 4) & 7);
-                    acc = ff_add(acc, p == 1.0f ? v : ff_scale(v, p));
-                    if (contrib && mask[n]) cacc += __ldcg(contrib + n);
-                }
-                if (acc.x < 0.0f) acc = make_float2(0.f, 0.f);
-                __stcg(fa + cur, ff_add(make_float2(w[cur], 0.f), acc));
-                if (contrib) __stcg(contrib + cur, cacc);
-                ++done;
-                __threadfence();
-                // release the receivers
-                const uint8_t code = fd[cur];
-                int32_t next = -1;
-                for (int d = 0; d < 8; ++d) {
-                    if (!(code & dir_bit(d))) continue;
-                    const int rx = x + dir_dx(d), ry = y + dir_dy(d);
-                    if (rx < 0 || rx >= W || ry < 0 || ry >= H) continue;
-                    const size_t r = (size_t)ry * W + rx;
-                    if (!mask[r]) continue;
-                    if (atomicSub(pending + r, 1) == 1) {
-                        if (next < 0)
-                            next = (int32_t)r;
-                        else if (nextra < 8)
-                            extra[nextra++] = (int32_t)r;
-                    }
-                }
-                __threadfence();
-                cur = next;
-            }
-            for (int j = 0; j < 8; ++j)
-                wave_append(j < nextra, j < nextra ? extra[j] : 0, out, &cnt[(round + 1) % 3], (int)N, &sc->err);
-        }
-        grid.sync();
-    }
+    const FaCell op{mask, fd, w, prop, fa, contrib, k.W, k.H};
+    int done = wave_walk(op, fd, mask, pending, list_a, list_b, k.W, k.H, sc);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&sc->fa_done, done);
 }

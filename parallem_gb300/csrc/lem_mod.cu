@@ -219,101 +219,69 @@ __global__ void k_sed_prep(const uint8_t* __restrict__ mask, const uint8_t* __re
     }
 }
 
-// MFDsedbud (mfd_accum.cu:32-254) as a wave: deposition from the donors'
+// One cell of MFDsedbud (mfd_accum.cu:32-254): deposition from the donors'
 // erosion, stone mixing with the donors' updated stone, new soil thickness.
+struct SedCell {
+    const uint8_t* fd;
+    const float* prop;
+    const float* ero;
+    const float* inci;
+    const float* geli;
+    float* depo;
+    float* stone;
+    float* fines;
+    float* soilT;
+    int W, H;
+    float ddk, dck, dgk;
+    __device__ __forceinline__ void cell(int32_t cur, int x, int y) const {
+        const float omd = 1.0f - ddk, omc = 1.0f - dck, omg = 1.0f - dgk;
+        float ad = 0.f, ac = 0.f, ag = 0.f, from = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+            const int d = scan_dir(kk);
+            const int nx = x + dir_dx(d), ny = y + dir_dy(d);
+            if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+            const int32_t n = ny * W + nx;
+            if (!donates(__ldg(fd + n), d)) continue;
+            const float p = prop ? __ldg(prop + 8 * (size_t)n + ((d + 4) & 7)) : 1.0f;
+            ad += p * (__ldg(ero + n) * omd);
+            ac += p * (__ldg(inci + n) * omc);
+            ag += p * (__ldg(geli + n) * omg);
+            from += p * __ldcg(stone + n);
+        }
+        const float e = __ldg(ero + cur), ic = __ldg(inci + cur), g = __ldg(geli + cur);
+        const float dep = ((ad + e) * ddk) + ((ac + ic) * dck) + ((ag + g) * dgk);
+        depo[cur] = dep;
+        const float st0 = soilT[cur];
+        const float sedthick = st0 + dep;
+        if (sedthick != 0.0f) {
+            const float old = st0 / sedthick;
+            const float input = 1.0f - old;
+            float sn = (old * __ldcg(stone + cur)) + (input * from);
+            if (sn < 0.01f)
+                sn = 0.01f;
+            else if (sn > 99.9f)
+                sn = 99.9f;
+            __stcg(stone + cur, sn);
+            fines[cur] = 100.0f - sn;
+        }
+        const float toterosion = e + ic + g;
+        float stn = st0;
+        if (toterosion >= sedthick) stn = 0.0f;
+        if (sedthick > toterosion) stn = sedthick - toterosion;
+        soilT[cur] = stn;
+    }
+};
+
+// The sediment wave: every source starts it; cells follow as their last donor
+// finishes.
 __global__ void k_sed_walk(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                            const float* __restrict__ prop, const float* __restrict__ ero,
                            const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
                            float* fines, float* soilT, int32_t* pending, int32_t* list_a, int32_t* list_b,
                            ModelConsts k, DevScalars* sc) {
-    cg::grid_group grid = cg::this_grid();
-    const int W = k.W, H = k.H;
-    const size_t N = (size_t)W * H;
-    const size_t gstride = (size_t)gridDim.x * blockDim.x;
-    const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const float omd = 1.0f - k.ddk, omc = 1.0f - k.dck, omg = 1.0f - k.dgk;
-    int32_t* cnt = sc->counters;
-    if (gtid == 0) cnt[1] = cnt[2] = 0;
-    grid.sync();
-    int done = 0;
-    int round = 0;
-    for (;; ++round) {
-        const int32_t* in = (round & 1) ? list_b : list_a;
-        int32_t* out = (round & 1) ? list_a : list_b;
-        const int nin = *((volatile int32_t*)&cnt[round % 3]);
-        if (nin == 0) break;
-        if (round > (1 << 24)) {
-            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
-            break;
-        }
-        if (gtid == 0) cnt[(round + 2) % 3] = 0;
-        for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)nin; base += gstride) {
-            const size_t it = base + threadIdx.x;
-            int32_t cur = it < (size_t)nin ? in[it] : -1;
-            int32_t extra[8];
-            int nextra = 0;
-            for (size_t steps = 0; cur >= 0 && steps < N; ++steps) {
-                const int x = cur % W, y = cur / W;
-                float ad = 0.f, ac = 0.f, ag = 0.f, from = 0.f;
-#pragma unroll
-                for (int kk = 0; kk < 8; ++kk) {
-                    const int d = scan_dir(kk);
-                    const int nx = x + dir_dx(d), ny = y + dir_dy(d);
-                    if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
-                    const size_t n = (size_t)ny * W + nx;
-                    if (!donates(fd[n], d)) continue;
-                    const float p = prop ? prop[8 * n + ((d + 4) & 7)] : 1.0f;
-                    ad += p * (ero[n] * omd);
-                    ac += p * (inci[n] * omc);
-                    ag += p * (geli[n] * omg);
-                    from += p * __ldcg(stone + n);
-                }
-                const float e = ero[cur], ic = inci[cur], g = geli[cur];
-                const float dep = ((ad + e) * k.ddk) + ((ac + ic) * k.dck) + ((ag + g) * k.dgk);
-                depo[cur] = dep;
-                const float st0 = soilT[cur];
-                const float sedthick = st0 + dep;
-                if (sedthick != 0.0f) {
-                    const float old = st0 / sedthick;
-                    const float input = 1.0f - old;
-                    float sn = (old * stone[cur]) + (input * from);
-                    if (sn < 0.01f)
-                        sn = 0.01f;
-                    else if (sn > 99.9f)
-                        sn = 99.9f;
-                    __stcg(stone + cur, sn);
-                    fines[cur] = 100.0f - sn;
-                }
-                const float toterosion = e + ic + g;
-                float stn = st0;
-                if (toterosion >= sedthick) stn = 0.0f;
-                if (sedthick > toterosion) stn = sedthick - toterosion;
-                soilT[cur] = stn;
-                ++done;
-                __threadfence();
-                const uint8_t code = fd[cur];
-                int32_t next = -1;
-                for (int d = 0; d < 8; ++d) {
-                    if (!(code & dir_bit(d))) continue;
-                    const int rx = x + dir_dx(d), ry = y + dir_dy(d);
-                    if (rx < 0 || rx >= W || ry < 0 || ry >= H) continue;
-                    const size_t r = (size_t)ry * W + rx;
-                    if (!mask[r]) continue;
-                    if (atomicSub(pending + r, 1) == 1) {
-                        if (next < 0)
-                            next = (int32_t)r;
-                        else if (nextra < 8)
-                            extra[nextra++] = (int32_t)r;
-                    }
-                }
-                __threadfence();
-                cur = next;
-            }
-            for (int j = 0; j < 8; ++j)
-                wave_append(j < nextra, j < nextra ? extra[j] : 0, out, &cnt[(round + 1) % 3], (int)N, &sc->err);
-        }
-        grid.sync();
-    }
+    const SedCell op{fd, prop, ero, inci, geli, depo, stone, fines, soilT, k.W, k.H, k.ddk, k.dck, k.dgk};
+    int done = wave_walk(op, fd, mask, pending, list_a, list_b, k.W, k.H, sc);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&sc->sed_done, done);
 }

@@ -2,6 +2,8 @@
 // sediment routing): float-float arithmetic, warp lists, donor tests.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "lem_ctx.cuh"
 
 namespace lem {
@@ -57,5 +59,116 @@ __device__ __forceinline__ void wave_append(bool pred, int32_t value, int32_t* l
 __device__ __forceinline__ bool donates(uint8_t code_n, int d) { return (code_n & dir_bit((d + 4) & 7)) != 0; }
 
 constexpr int32_t kBlocked = 0x40000000;  // pending flag of a cell with a donor that never completes
+
+// Decrement with acquire-release semantics: the release publishes this
+// thread's earlier stores (the finished cell) to whichever thread sees the
+// count reach zero, and the acquire lets that thread read every donor.
+__device__ __forceinline__ int32_t dec_acq_rel(int32_t* p) {
+    int32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], -1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
+constexpr int kWaveStack = 8;      // receivers a lane keeps for itself before spilling to the next round
+constexpr int kWaveMaxRounds = 1 << 16;
+
+// The dependency wave shared by flow accumulation and sediment routing, run by
+// every thread of a cooperative launch.  A cell is ready once all its donors
+// are finished (pending[c] counts them; kBlocked marks a donor that never
+// finishes).  Lanes take ready cells from the round's list through one atomic
+// head per warp request, so no lane idles while work is left.  A lane that
+// finishes a cell decrements its receivers and carries on with the first one
+// it made ready (it was that cell's last donor); further receivers made ready
+// at the same time (MFD) go on the lane's own stack, and only when that is full
+// to the next round's list.  Op::cell(c, x, y) computes and stores cell c,
+// reading finished donors with ld.global.cg.  Returns the cells this thread
+// finished.
+template <class Op>
+__device__ int wave_walk(const Op& op, const uint8_t* __restrict__ fd, const uint8_t* __restrict__ mask,
+                         int32_t* pending, int32_t* list_a, int32_t* list_b, int W, int H, DevScalars* sc) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    const size_t N = (size_t)W * H;
+    const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    int32_t* cnt = sc->counters;  // [0..2] list sizes by round % 3, [3..5] take heads by round % 3
+    if (gtid == 0) {
+        cnt[1] = cnt[2] = 0;
+        cnt[3] = cnt[4] = cnt[5] = 0;
+    }
+    grid.sync();
+    int done = 0;
+    for (int round = 0;; ++round) {
+        const int32_t* in = (round & 1) ? list_b : list_a;
+        int32_t* out = (round & 1) ? list_a : list_b;
+        const int nin = *((volatile int32_t*)&cnt[round % 3]);
+        if (nin == 0) break;
+        if (round >= kWaveMaxRounds) {
+            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            break;
+        }
+        if (gtid == 0) {
+            cnt[(round + 2) % 3] = 0;      // size of the list after next (read before the last sync)
+            cnt[3 + (round + 1) % 3] = 0;  // head of the next round
+        }
+        int32_t* head = &cnt[3 + round % 3];
+        int32_t stack[kWaveStack];
+        int sp = 0;
+        int32_t cur = -1;
+        bool more = true;  // warp-uniform: the round's list may still hold cells
+        for (size_t guard = 0;; ++guard) {
+            if (cur < 0 && sp > 0) cur = stack[--sp];
+            const bool need = cur < 0;
+            const unsigned m = __ballot_sync(0xffffffffu, need && more);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(head, __popc(m));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (need) {
+                    const int it = base + __popc(m & below);
+                    if (it < nin) cur = __ldcg(in + it);
+                }
+                if (base + __popc(m) >= nin) more = false;
+            }
+            if (!__any_sync(0xffffffffu, cur >= 0)) break;
+            if (guard > 2 * N + 64) {  // every cell is finished at most once
+                if (lane == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+                break;
+            }
+            int32_t spill[8];
+            int nspill = 0;
+            if (cur >= 0) {
+                const int x = cur % W, y = cur / W;
+                op.cell(cur, x, y);
+                ++done;
+                const uint8_t code = fd[cur];
+                int32_t next = -1;
+                for (int d = 0; d < 8; ++d) {
+                    if (!(code & dir_bit(d))) continue;
+                    const int rx = x + dir_dx(d), ry = y + dir_dy(d);
+                    if (rx < 0 || rx >= W || ry < 0 || ry >= H) continue;
+                    const int32_t r = ry * W + rx;
+                    if (!mask[r]) continue;
+                    if (dec_acq_rel(pending + r) == 1) {
+                        if (next < 0)
+                            next = r;
+                        else if (sp < kWaveStack)
+                            stack[sp++] = r;
+                        else
+                            spill[nspill++] = r;
+                    }
+                }
+                cur = next;
+            }
+            if (__any_sync(0xffffffffu, nspill > 0))
+                for (int j = 0; j < 8; ++j)
+                    wave_append(j < nspill, j < nspill ? spill[j] : 0, out, &cnt[(round + 1) % 3], (int)N, &sc->err);
+        }
+        grid.sync();
+    }
+    return done;
+}
 
 }  // namespace lem
