@@ -223,55 +223,56 @@ __global__ void k_plateau_init(const uint8_t* __restrict__ mask, const uint8_t* 
     }
 }
 
-__device__ __forceinline__ float ld_sp(const float* sp, size_t i) { return __ldcg(sp + i); }
+constexpr int kPT = 32;            // plateau tile edge (cells)
+constexpr int kPH = kPT + 2;       // tile with its one-cell halo
+constexpr int kTileSweeps = 2048;  // sweeps of one tile visit before it is re-queued
 
 // Least fixpoint of sp = min(sp, sp[n] + dc) over equal-height in-grid
-// neighbours (the route_plateausMFD loop, routeflow.cu:854-872), by a pull sweep
-// over all candidates followed by push rounds from the cells that improved.
-__global__ void k_plateau_relax(const double* __restrict__ z, float* sp, const int32_t* __restrict__ cand,
-                                int32_t* list_a, int32_t* list_b, int32_t* mark, ModelConsts k, DevScalars* sc,
-                                int pass) {
+// neighbours (the route_plateausMFD loop, routeflow.cu:854-872), dc = 1 along
+// the axes and 1.41 on the diagonals.  The grid is cut into 32x32 tiles; a
+// round relaxes every queued tile to its local fixpoint in shared memory
+// (Gauss-Seidel sweeps with the halo read at the start of the visit), writes
+// back the cells that improved and queues the neighbouring tiles across every
+// border an improved cell lies on.  Round 0 queues every tile that holds a
+// candidate.  The fixpoint is unique, so the visiting order does not change the
+// result.  Only candidates (sp > 0) ever change: every other cell is a source
+// at 0.
+__global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict__ z, float* sp,
+                                                       const int32_t* __restrict__ cand, int32_t* list_a,
+                                                       int32_t* list_b, int32_t* mark, ModelConsts k,
+                                                       DevScalars* sc, int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
     cg::grid_group grid = cg::this_grid();
+    __shared__ unsigned long long s_key[kPH * kPH];
+    __shared__ float s_v[kPH * kPH];
+    __shared__ int s_act[9];
     const int W = k.W, H = k.H;
+    const int TW = (W + kPT - 1) / kPT, TH = (H + kPT - 1) / kPT;
     const int n = sc->n_cand;
     const size_t gstride = (size_t)gridDim.x * blockDim.x;
     const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int ncap = (int)((size_t)W * H);
-    int32_t* cnt = sc->counters;  // cnt[0..2] frontier sizes, triple-buffered
-    const int32_t rid0 = sc->round_id;  // marks of this launch are rid0 + round + 1
+    int32_t* cnt = sc->counters;  // cnt[0..2] queued tiles, triple-buffered
+    const int32_t rid0 = sc->round_id;  // marks of round r are rid0 + r + 1
     if (gtid == 0) {
         cnt[0] = 0;
         cnt[1] = 0;
         cnt[2] = 0;
     }
     grid.sync();
-    // round 0: pull
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)n; base += gstride) {
         const size_t i = base + threadIdx.x;
-        bool improved = false;
-        int32_t c = 0;
+        bool fresh = false;
+        int32_t t = 0;
         if (i < (size_t)n) {
-            c = cand[i];
-            const int x = c % W, y = c / W;
-            const unsigned long long kc = dkey(z[c]);
-            float best = kFar;
-            for (int d = 0; kc != 0 && d < 8; ++d) {  // a NaN cell (key 0) equals no neighbour
-                const int nx = x + dir_dx(d), ny = y + dir_dy(d);
-                if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
-                const size_t nb = (size_t)ny * W + nx;
-                if (dkey(z[nb]) != kc) continue;
-                const float dis = ld_sp(sp, nb) + ((d & 1) ? 1.41f : 1.0f);
-                if (best > dis) best = dis;
-            }
-            if (best < kFar) {
-                atomicMin(reinterpret_cast<int*>(sp + c), __float_as_int(best));
-                improved = true;
-            }
+            const int32_t c = cand[i];
+            t = (c / W / kPT) * TW + (c % W) / kPT;
+            fresh = atomicExch(mark + t, rid0 + 1) != rid0 + 1;
         }
-        warp_append(improved, c, list_a, &cnt[0], ncap, &sc->err);
+        warp_append(fresh, t, list_a, &cnt[0], ncap, &sc->err);
     }
     grid.sync();
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;  // rows ly0 + 8q of the tile
     int round = 0;
     for (;; ++round) {
         const int32_t* in = (round & 1) ? list_b : list_a;
@@ -283,31 +284,82 @@ __global__ void k_plateau_relax(const double* __restrict__ z, float* sp, const i
             break;
         }
         if (gtid == 0) cnt[(round + 2) % 3] = 0;
-        for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)nin; base += gstride) {
-            const size_t i = base + threadIdx.x;
-            // push the improvement of c to its equal-height neighbours
-            int32_t pushed[8];
-            int np = 0;
-            if (i < (size_t)nin) {
-                const int32_t c = in[i];
-                const int x = c % W, y = c / W;
-                const unsigned long long kc = dkey(z[c]);
-                const float v = ld_sp(sp, c);
-                for (int d = 0; kc != 0 && d < 8; ++d) {
-                    const int nx = x + dir_dx(d), ny = y + dir_dy(d);
-                    if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
-                    const size_t nb = (size_t)ny * W + nx;
-                    if (dkey(z[nb]) != kc) continue;
-                    const float nv = v + ((d & 1) ? 1.41f : 1.0f);
-                    const int old = atomicMin(reinterpret_cast<int*>(sp + nb), __float_as_int(nv));
-                    if (__int_as_float(old) > nv) {
-                        const int32_t id = rid0 + round + 1;
-                        if (atomicExch(mark + nb, id) != id) pushed[np++] = (int32_t)nb;
+        const int32_t id_next = rid0 + round + 2;
+        for (int ti = blockIdx.x; ti < nin; ti += gridDim.x) {
+            const int32_t t = __ldcg(in + ti);
+            const int tx0 = (t % TW) * kPT, ty0 = (t / TW) * kPT;
+            for (int j = threadIdx.x; j < kPH * kPH; j += blockDim.x) {
+                const int gx = tx0 - 1 + j % kPH, gy = ty0 - 1 + j / kPH;
+                unsigned long long kk = 0;  // outside the grid: equal to no cell
+                float v = 0.f;
+                if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+                    const size_t g = (size_t)gy * W + gx;
+                    kk = dkey(z[g]);
+                    v = __ldcg(sp + g);
+                }
+                s_key[j] = kk;
+                s_v[j] = v;
+            }
+            if (threadIdx.x < 9) s_act[threadIdx.x] = 0;
+            __syncthreads();
+            float v0[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v0[q] = s_v[(ly0 + 8 * q + 1) * kPH + lx + 1];
+            int sweep = 0;
+            for (; sweep < kTileSweeps; ++sweep) {
+                bool ch = false;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int sidx = (ly0 + 8 * q + 1) * kPH + lx + 1;
+                    const float cv = s_v[sidx];
+                    const unsigned long long kc = s_key[sidx];
+                    if (cv > 0.f && kc != 0) {  // a NaN cell (key 0) equals no neighbour
+                        float best = cv;
+#pragma unroll
+                        for (int d = 0; d < 8; ++d) {
+                            const int sn = sidx + dir_dy(d) * kPH + dir_dx(d);
+                            if (s_key[sn] != kc) continue;
+                            const float nv = s_v[sn] + ((d & 1) ? 1.41f : 1.0f);
+                            if (nv < best) best = nv;
+                        }
+                        if (best < cv) {
+                            s_v[sidx] = best;
+                            ch = true;
+                        }
+                    }
+                }
+                if (!__syncthreads_or(ch)) break;
+            }
+            if (sweep == kTileSweeps && threadIdx.x == 0) s_act[4] = 1;  // not settled: visit again
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int ly = ly0 + 8 * q;
+                const int gx = tx0 + lx, gy = ty0 + ly;
+                const float v = s_v[(ly + 1) * kPH + lx + 1];
+                if (gx < W && gy < H && v < v0[q]) {
+                    __stcg(sp + (size_t)gy * W + gx, v);
+                    const int ex = lx == 0 ? 0 : (lx == kPT - 1 ? 2 : 1);
+                    const int ey = ly == 0 ? 0 : (ly == kPT - 1 ? 2 : 1);
+                    if (ex != 1) s_act[3 + ex] = 1;
+                    if (ey != 1) s_act[3 * ey + 1] = 1;
+                    if (ex != 1 && ey != 1) s_act[3 * ey + ex] = 1;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x < 9 && s_act[threadIdx.x]) {
+                const int ntx = t % TW + (int)(threadIdx.x % 3) - 1, nty = t / TW + (int)(threadIdx.x / 3) - 1;
+                if (ntx >= 0 && ntx < TW && nty >= 0 && nty < TH) {
+                    const int32_t nt = nty * TW + ntx;
+                    if (atomicExch(mark + nt, id_next) != id_next) {
+                        const int pos = atomicAdd(&cnt[(round + 1) % 3], 1);
+                        if (pos < ncap)
+                            out[pos] = nt;
+                        else
+                            atomicOr(&sc->err, ErrFlags::kCapacity);
                     }
                 }
             }
-            for (int j = 0; j < 8; ++j)
-                warp_append(j < np, j < np ? pushed[j] : 0, out, &cnt[(round + 1) % 3], ncap, &sc->err);
+            __syncthreads();
         }
         grid.sync();
     }
