@@ -276,6 +276,14 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
     ALLOC(s.wc, N);
     ALLOC(s.wp, N);
     ALLOC(s.contrib, N);
+    ALLOC(s.t_dst, N);
+    ALLOC(s.t_pend, N);
+    ALLOC(s.t_orng, N);
+    ALLOC(s.t_la, N);
+    {
+        const size_t tiles = (size_t)((grid->width + kTile - 1) / kTile) * ((grid->height + kTile - 1) / kTile);
+        ALLOC(s.t_ent, tiles * kTileEnt);
+    }
     if (params->flow_direction_type != 0 && params->mfd_proportions) {
         ALLOC(s.prop, 8 * N);
     }

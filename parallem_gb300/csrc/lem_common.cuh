@@ -95,6 +95,8 @@ struct DevScalars {
     double tot_e, tot_i, tot_g, tot_d, tot_wc, tot_wp, tot_bio;
     int32_t flag[4];                 // convergence flags of the cooperative loops
     int32_t counters[8];
+    int32_t tiled_ok;                // 1: this step's accumulation may take the tiled path
+    int32_t tile_src;                // tile outlets with no pending inflow (coarse sources)
 };
 
 }  // namespace lem

@@ -5,6 +5,9 @@
 
 namespace lem {
 
+constexpr int kTile = 32;     // edge of the accumulation tiles
+constexpr int kTileEnt = 136; // inflow slots per tile (inflows come from the 132 halo ring cells)
+
 // Dreybrodt temperature response table (see lem_mod.cu): log10 of
 // K1*KC*KH / (4*K2*gammaCa*gammaHCO3^2) sampled every kTabStep degrees.
 constexpr int kTabN = 3841;
@@ -64,6 +67,12 @@ struct DevState {
     float* dz; float* wc; float* wp;  // diagnostics
     float* prop;        // 8 per cell, MFD proportions (calcprops mode only)
     int32_t* contrib;
+    // tiled accumulation (32x32 tiles): per cell, used at tile entries / outlets
+    int32_t* t_dst;     // entry cell: the outlet of its tile its path reaches, or -1
+    int32_t* t_pend;    // outlet: inflows still to arrive (kBlocked: never completes)
+    int32_t* t_orng;    // outlet: (first << 16) | count of its inflows in t_ent
+    float2* t_la;       // outlet: accumulation from inside its tile only
+    int32_t* t_ent;     // per tile, kTileEnt inflow cells (outlets of neighbours) grouped by outlet
     // flooding tables
     unsigned long long* ekey;   // hash keys (label pair)
     unsigned long long* ewt;    // min boundary height key

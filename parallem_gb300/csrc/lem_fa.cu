@@ -50,6 +50,8 @@ __global__ void k_fa_prep(const double* __restrict__ z, const uint8_t* __restric
                 soilM[i] = sm;
                 w[i] = wi;
                 fa[i] = make_float2(wi, 0.0f);
+                const uint8_t code = fd[i];
+                if (wi < 0.0f || (code & (code - 1))) sc->tiled_ok = 0;
                 if (contrib) contrib[i] = 1;
                 int32_t pend = 0;
 #pragma unroll
@@ -141,17 +143,444 @@ struct FaCell {
         __stcg(fa + cur, ff_add(make_float2(__ldg(w + cur), 0.f), acc));
         if (contrib) __stcg(contrib + cur, cacc);
     }
+    __device__ __forceinline__ int receivers(int32_t cur, int x, int y, int32_t* r) const {
+        return code_receivers(fd, mask, cur, x, y, W, H, r);
+    }
 };
 
 // The accumulation wave: every source starts it; cells follow as their last
-// donor finishes.
+// donor finishes.  With gate set it runs only when the tiled path is off.
 __global__ void k_fa_walk(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                           const float* __restrict__ w, const float* __restrict__ prop, float2* fa, int32_t* pending,
-                          int32_t* contrib, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc) {
+                          int32_t* contrib, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc,
+                          int gate) {
+    if (gate && sc->tiled_ok) return;  // the tiled kernels did this step
     const FaCell op{mask, fd, w, prop, fa, contrib, k.W, k.H};
-    int done = wave_walk(op, fd, mask, pending, list_a, list_b, k.W, k.H, sc);
+    int done = wave_walk(op, pending, list_a, list_b, k.W, k.H, sc);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&sc->fa_done, done);
+}
+
+// ---------------------------------------------------------------------------
+// Tiled accumulation for single-receiver codes (SFD).  A chain walk through
+// global memory pays an L2 round trip per cell on the longest flow path; here
+// the grid is cut into 32x32 tiles and most of the path runs in shared memory.
+//   local : per tile, the accumulation from inside the tile (la), the outlet
+//           each entry cell drains to, and per outlet its entries and the
+//           number of inflows from other tiles it waits for;
+//   coarse: a wave over the outlets only: F(o) = la(o) + the final values of
+//           the outlets of neighbouring tiles that flow into o's entries;
+//   final : per tile, every other cell by the reference formula, with the
+//           donors in other tiles taken at their final values.
+// All sums are pulled in a fixed order, so results do not depend on timing.
+// The decomposition is exact while no donor sum can be negative (CalcMFD
+// clamps those to zero); k_fa_prep disables the path for a step with a
+// negative weight or a multi-direction code, and the walk then runs instead.
+
+constexpr int kTH = kTile + 2;  // tile with its one-cell halo
+constexpr uint8_t kKindIn = 0, kKindOutlet = 1, kKindEnd = 2;
+constexpr uint8_t kCellOff = 0;    // outside the grid, or outside the catchment with a nodata DEM
+constexpr uint8_t kCellIn = 1;     // in the catchment
+constexpr uint8_t kCellBlock = 2;  // outside the catchment with a DEM value: a donor that never completes
+
+__device__ __forceinline__ void tile_load(const double* __restrict__ z, const uint8_t* __restrict__ mask,
+                                          const uint8_t* __restrict__ fd, int W, int H, int tx0, int ty0,
+                                          uint8_t* s_code, uint8_t* s_cls) {
+    for (int j = threadIdx.x; j < kTH * kTH; j += blockDim.x) {
+        const int gx = tx0 - 1 + j % kTH, gy = ty0 - 1 + j / kTH;
+        uint8_t c = 0, cl = kCellOff;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            const size_t g = (size_t)gy * W + gx;
+            c = fd[g];
+            if (mask[g])
+                cl = kCellIn;
+            else if (z[g] != kNoData)
+                cl = kCellBlock;
+        }
+        s_code[j] = c;
+        s_cls[j] = cl;
+    }
+}
+
+__device__ __forceinline__ bool in_tile(int lx, int ly) { return lx >= 0 && lx < kTile && ly >= 0 && ly < kTile; }
+
+// The halo ring in a fixed order: top row, bottom row, left column, right column.
+constexpr int kRing = 4 * kTH - 4;
+constexpr int kRingChunks = (kRing + 31) / 32;
+__device__ __forceinline__ int ring_halo(int i) {
+    if (i < kTH) return i;
+    if (i < 2 * kTH) return (kTH - 1) * kTH + (i - kTH);
+    if (i < 2 * kTH + kTile) return (i - 2 * kTH + 1) * kTH;
+    return (i - 2 * kTH - kTile + 1) * kTH + kTH - 1;
+}
+
+__global__ void __launch_bounds__(256)
+    k_fat_local(const double* __restrict__ z, const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
+                const float* __restrict__ w, float2* __restrict__ t_la, int32_t* __restrict__ t_dst,
+                int32_t* __restrict__ t_pend, int32_t* __restrict__ t_orng, int32_t* __restrict__ t_ent,
+                int32_t* srcs, ModelConsts k, DevScalars* sc) {
+    if (!sc->tiled_ok) return;
+    __shared__ uint8_t s_code[kTH * kTH];
+    __shared__ uint8_t s_cls[kTH * kTH];
+    __shared__ int32_t s_pend[kTile * kTile];
+    __shared__ float2 s_la[kTile * kTile];
+    __shared__ int16_t s_ptr[kTile * kTile];
+    __shared__ uint8_t s_kind[kTile * kTile];
+    __shared__ uint8_t s_ext[kTile * kTile];
+    __shared__ uint8_t s_done[kTile * kTile];
+    __shared__ int16_t s_oslot[kTile * kTile];
+    __shared__ int16_t s_olist[kTileEnt];
+    __shared__ int32_t s_ocnt[kTileEnt];
+    __shared__ int16_t s_ostart[kTileEnt];
+    __shared__ int16_t s_ofill[kTileEnt];
+    __shared__ int s_no;
+    const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
+    const int t = blockIdx.x;
+    const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
+    tile_load(z, mask, fd, W, H, tx0, ty0, s_code, s_cls);
+    __syncthreads();
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
+    bool src[4];  // chain starts, fixed before any chain runs (a chain may enter them later)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
+        int32_t pend = kBlocked;
+        uint8_t kind = kKindEnd, ext = 0;
+        int16_t ptr = (int16_t)l;
+        float wl = 0.f;
+        if (s_cls[hc] == kCellIn) {
+            pend = 0;
+#pragma unroll
+            for (int d = 0; d < 8; ++d) {
+                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+                if (!donates(s_code[nh], d)) continue;
+                const uint8_t cl = s_cls[nh];
+                if (cl == kCellBlock)
+                    pend |= kBlocked;
+                else if (cl == kCellIn) {
+                    if (in_tile(lx + dir_dx(d), ly + dir_dy(d)))
+                        ++pend;
+                    else
+                        ++ext;
+                }
+            }
+            const int d = bit_dir(s_code[hc]);
+            if (d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn) {
+                const int rlx = lx + dir_dx(d), rly = ly + dir_dy(d);
+                if (in_tile(rlx, rly)) {
+                    kind = kKindIn;
+                    ptr = (int16_t)(rly * kTile + rlx);
+                } else {
+                    kind = kKindOutlet;
+                }
+            }
+            wl = w[(size_t)(ty0 + ly) * W + tx0 + lx];
+        }
+        s_pend[l] = pend;
+        src[q] = pend == 0;
+        s_kind[l] = kind;
+        s_ext[l] = ext;
+        s_ptr[l] = ptr;
+        s_la[l] = make_float2(wl, 0.f);
+        s_done[l] = 0;
+    }
+    __syncthreads();
+    // accumulation from inside the tile: chains of last-arriving donors
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        int cur = src[q] ? (ly0 + 8 * q) * kTile + lx : -1;
+        for (int guard = 0; cur >= 0 && guard < kTile * kTile; ++guard) {
+            const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const int d = scan_dir(kk);
+                const int nlx = cx + dir_dx(d), nly = cy + dir_dy(d);
+                if (!in_tile(nlx, nly)) continue;
+                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+                if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
+                acc = ff_add(acc, s_la[nly * kTile + nlx]);
+            }
+            if (acc.x < 0.0f) acc = make_float2(0.f, 0.f);
+            s_la[cur] = ff_add(s_la[cur], acc);
+            s_done[cur] = 1;
+            __threadfence_block();
+            int nxt = -1;
+            if (s_kind[cur] == kKindIn) {
+                const int r = s_ptr[cur];
+                if (atomicSub(&s_pend[r], 1) == 1) {
+                    __threadfence_block();
+                    nxt = r;
+                }
+            }
+            cur = nxt;
+        }
+    }
+    __syncthreads();
+    // the end of every in-tile path: pointer jumping (paths are shorter than 2^10 cells)
+    for (int it = 0; it < 10; ++it) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int l = (ly0 + 8 * q) * kTile + lx;
+            s_ptr[l] = s_ptr[s_ptr[l]];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx;
+        if (s_ext[l]) {
+            const int e = s_ptr[l];
+            t_dst[(size_t)(ty0 + ly) * W + tx0 + lx] =
+                s_kind[e] == kKindOutlet ? (int32_t)((ty0 + e / kTile) * W + tx0 + (e & (kTile - 1))) : -1;
+        }
+    }
+    // outlets in cell order (they lie on the border: at most 124)
+    if (threadIdx.x < 32) {
+        const unsigned below = (1u << lx) - 1u;
+        int no = 0;
+        for (int base = 0; base < kTile * kTile; base += 32) {
+            const int l = base + lx;
+            const bool io = s_kind[l] == kKindOutlet;
+            const unsigned mo = __ballot_sync(0xffffffffu, io);
+            if (io) {
+                s_olist[no + __popc(mo & below)] = (int16_t)l;
+                s_oslot[l] = (int16_t)(no + __popc(mo & below));
+            }
+            no += __popc(mo);
+        }
+        if (lx == 0) s_no = no;
+    }
+    if (threadIdx.x < kTileEnt) s_ocnt[threadIdx.x] = 0;
+    __syncthreads();
+    // inflows: ring cells of the halo that flow into the tile, grouped by the
+    // outlet their entry drains to, in ring order
+    int key[kRingChunks];
+    int32_t donor[kRingChunks];
+#pragma unroll
+    for (int c = 0; c < kRingChunks; ++c) {
+        const int i = c * 32 + lx;
+        key[c] = -1;
+        donor[c] = 0;
+        if (threadIdx.x < 32 && i < kRing) {
+            const int h = ring_halo(i);
+            const int d = s_cls[h] == kCellIn ? bit_dir(s_code[h]) : -1;
+            if (d >= 0) {
+                const int hx = h % kTH + dir_dx(d), hy = h / kTH + dir_dy(d);
+                if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile && s_cls[hy * kTH + hx] == kCellIn) {
+                    const int e = (hy - 1) * kTile + hx - 1;
+                    const int o = s_ptr[e];
+                    if (s_kind[o] == kKindOutlet) {
+                        key[c] = s_oslot[o];
+                        donor[c] = (ty0 - 1 + h / kTH) * W + tx0 - 1 + h % kTH;
+                        atomicAdd(&s_ocnt[key[c]], 1);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const int no = s_no;
+    if (threadIdx.x == 0) {
+        int a = 0;
+        for (int i = 0; i < no; ++i) {
+            s_ostart[i] = (int16_t)a;
+            s_ofill[i] = (int16_t)a;
+            a += s_ocnt[i];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const unsigned below = (1u << lx) - 1u;
+#pragma unroll
+        for (int c = 0; c < kRingChunks; ++c) {
+            const unsigned peers = __match_any_sync(0xffffffffu, key[c]);
+            const int base = key[c] >= 0 ? s_ofill[key[c]] : 0;
+            __syncwarp();
+            if (key[c] >= 0) {
+                t_ent[(size_t)t * kTileEnt + base + __popc(peers & below)] = donor[c];
+                if ((peers & below) == 0) s_ofill[key[c]] = (int16_t)(base + __popc(peers));
+            }
+            __syncwarp();
+        }
+    }
+    const int j = threadIdx.x;
+    bool ready = false;
+    int32_t og = 0;
+    if (j < no) {
+        const int o = s_olist[j];
+        const int32_t opend = (s_done[o] ? 0 : kBlocked) + s_ocnt[j];
+        og = (ty0 + o / kTile) * W + tx0 + (o & (kTile - 1));
+        t_orng[og] = ((int)s_ostart[j] << 16) | s_ocnt[j];
+        t_pend[og] = opend;
+        t_la[og] = s_la[o];
+        ready = (opend == 0);
+    }
+    wave_append(ready, og, srcs, &sc->tile_src, W * H, &sc->err);
+}
+
+// One outlet of the coarse wave.
+struct CoarseCell {
+    const uint8_t* mask;
+    const uint8_t* fd;
+    const float2* t_la;
+    const int32_t* t_orng;
+    const int32_t* t_ent;
+    const int32_t* t_dst;
+    float2* fa;
+    int W, H, TW;
+    __device__ __forceinline__ void cell(int32_t o, int x, int y) const {
+        const int t = (y / kTile) * TW + x / kTile;
+        const int rng = __ldg(t_orng + o);
+        const int start = rng >> 16, cnt = rng & 0xffff;
+        const int32_t* list = t_ent + (size_t)t * kTileEnt + start;
+        float2 acc = __ldg(t_la + o);
+        for (int i = 0; i < cnt; i += 8) {
+            float2 v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v[j] = (i + j < cnt) ? __ldcg(fa + __ldg(list + i + j)) : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (i + j < cnt) acc = ff_add(acc, v[j]);
+        }
+        __stcg(fa + o, acc);
+    }
+    __device__ __forceinline__ int receivers(int32_t o, int x, int y, int32_t* r) const {
+        const int d = bit_dir(__ldg(fd + o));
+        const int32_t rc = (y + dir_dy(d)) * W + x + dir_dx(d);
+        const int32_t dst = __ldg(t_dst + rc);
+        r[0] = dst;
+        return dst >= 0 ? 1 : 0;
+    }
+};
+
+__global__ void k_fat_coarse(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
+                             const float2* __restrict__ t_la, const int32_t* __restrict__ t_orng,
+                             const int32_t* __restrict__ t_ent, const int32_t* __restrict__ t_dst, float2* fa,
+                             int32_t* t_pend, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc) {
+    if (!sc->tiled_ok) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->counters[0] = sc->tile_src;
+    const CoarseCell op{mask, fd, t_la, t_orng, t_ent, t_dst, fa, k.W, k.H, (k.W + kTile - 1) / kTile};
+    wave_walk(op, t_pend, list_a, list_b, k.W, k.H, sc);
+}
+
+__global__ void __launch_bounds__(256)
+    k_fat_final(const double* __restrict__ z, const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
+                const float* __restrict__ w, const int32_t* __restrict__ t_pend, float2* fa, ModelConsts k,
+                DevScalars* sc) {
+    if (!sc->tiled_ok) return;
+    __shared__ uint8_t s_code[kTH * kTH];
+    __shared__ uint8_t s_cls[kTH * kTH];
+    __shared__ uint8_t s_hok[kTH * kTH];
+    __shared__ float2 s_hval[kTH * kTH];
+    __shared__ int32_t s_pend[kTile * kTile];
+    __shared__ float2 s_val[kTile * kTile];
+    __shared__ int s_done;
+    const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
+    const int t = blockIdx.x;
+    const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
+    tile_load(z, mask, fd, W, H, tx0, ty0, s_code, s_cls);
+    // donors in other tiles: outlets of their tiles, final after the coarse wave
+    for (int j = threadIdx.x; j < kTH * kTH; j += blockDim.x) {
+        const int hx = j % kTH, hy = j / kTH;
+        if (hx != 0 && hx != kTH - 1 && hy != 0 && hy != kTH - 1) continue;
+        const int gx = tx0 - 1 + hx, gy = ty0 - 1 + hy;
+        uint8_t ok = 0;
+        float2 v = make_float2(0.f, 0.f);
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H && mask[(size_t)gy * W + gx]) {
+            const size_t g = (size_t)gy * W + gx;
+            ok = t_pend[g] == 0;
+            v = fa[g];
+        }
+        s_hok[j] = ok;
+        s_hval[j] = v;
+    }
+    if (threadIdx.x == 0) s_done = 0;
+    __syncthreads();
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
+    int done = 0;
+    bool outlet[4], src[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
+        int32_t pend = kBlocked;
+        float wl = 0.f;
+        outlet[q] = false;
+        if (s_cls[hc] == kCellIn) {
+            pend = 0;
+#pragma unroll
+            for (int d = 0; d < 8; ++d) {
+                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+                if (!donates(s_code[nh], d)) continue;
+                const uint8_t cl = s_cls[nh];
+                if (cl == kCellBlock)
+                    pend |= kBlocked;
+                else if (cl == kCellIn) {
+                    if (in_tile(lx + dir_dx(d), ly + dir_dy(d)))
+                        ++pend;
+                    else if (!s_hok[nh])
+                        pend |= kBlocked;
+                }
+            }
+            const int d = bit_dir(s_code[hc]);
+            if (d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn &&
+                !in_tile(lx + dir_dx(d), ly + dir_dy(d))) {
+                outlet[q] = true;
+                if (t_pend[(size_t)(ty0 + ly) * W + tx0 + lx] == 0) ++done;
+            }
+            wl = w[(size_t)(ty0 + ly) * W + tx0 + lx];
+        }
+        s_pend[l] = pend;
+        src[q] = pend == 0 && !outlet[q];
+        s_val[l] = make_float2(wl, 0.f);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        int cur = src[q] ? (ly0 + 8 * q) * kTile + lx : -1;
+        for (int guard = 0; cur >= 0 && guard < kTile * kTile; ++guard) {
+            const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const int d = scan_dir(kk);
+                const int nlx = cx + dir_dx(d), nly = cy + dir_dy(d);
+                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+                if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
+                acc = ff_add(acc, in_tile(nlx, nly) ? s_val[nly * kTile + nlx] : s_hval[nh]);
+            }
+            if (acc.x < 0.0f) acc = make_float2(0.f, 0.f);
+            const float2 v = ff_add(s_val[cur], acc);
+            s_val[cur] = v;
+            fa[(size_t)(ty0 + cy) * W + tx0 + cx] = v;
+            ++done;
+            __threadfence_block();
+            int nxt = -1;
+            const int d = bit_dir(s_code[hc]);
+            if (d >= 0) {
+                const int rlx = cx + dir_dx(d), rly = cy + dir_dy(d);
+                const int rh = hc + dir_dy(d) * kTH + dir_dx(d);
+                if (in_tile(rlx, rly) && s_cls[rh] == kCellIn) {
+                    const int r = rly * kTile + rlx;
+                    if (atomicSub(&s_pend[r], 1) == 1) {
+                        __threadfence_block();
+                        // an outlet keeps the coarse wave's value
+                        const bool r_out = [&] {
+                            const int dr = bit_dir(s_code[rh]);
+                            return dr >= 0 && s_cls[rh + dir_dy(dr) * kTH + dir_dx(dr)] == kCellIn &&
+                                   !in_tile(rlx + dir_dx(dr), rly + dir_dy(dr));
+                        }();
+                        if (!r_out) nxt = r;
+                    }
+                }
+            }
+            cur = nxt;
+        }
+    }
+    done = wsum(done);
+    if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_done) atomicAdd(&sc->fa_done, s_done);
 }
 
 // correctmfdflow's first-iteration branch (mfd_simple.cu:336-349): the outlet
@@ -173,8 +602,10 @@ __global__ void k_fa_argmax_set(DevScalars* sc) {
     sc->outlet = (sc->fa_max_key > zero) ? sc->counters[7] : 0;
 }
 
-__global__ void k_fa_reset(DevScalars* sc) {
+__global__ void k_fa_reset(DevScalars* sc, int tiled) {
     sc->counters[0] = 0;
+    sc->tiled_ok = tiled;
+    sc->tile_src = 0;
     sc->fa_done = 0;
     sc->n_active = 0;
     sc->fa_max_key = 0ull;
@@ -189,15 +620,40 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, con
     const int T = 256;
     size_t nb = (N + T - 1) / T;
     const int blocks = (int)(nb > 152 * 32 ? 152 * 32 : nb);
-    LEM_LAUNCH(L, k_fa_reset, 1, 1, s.sc);
+    int32_t* contrib = (flags & LEM_STEP_CONTRIB) ? s.contrib : nullptr;
+    const int tiled = (k.flow_type == 0 && !contrib) ? 1 : 0;
+    LEM_LAUNCH(L, k_fa_reset, 1, 1, s.sc, tiled);
     const float* prop = nullptr;
     if (k.flow_type != 0 && k.mfd_props) {
         LEM_LAUNCH(L, k_calcprops, blocks, T, s.mask, s.fd, s.slopes, s.prop, N);
         prop = s.prop;
     }
-    int32_t* contrib = (flags & LEM_STEP_CONTRIB) ? s.contrib : nullptr;
     LEM_LAUNCH(L, k_fa_prep, blocks, T, s.z, s.mask, s.fd, s.stone, s.totB, s.soilM, s.w, s.fa, s.pending, contrib,
                s.list_a, k, c, s.sc);
+    if (tiled) {
+        const int tiles = ((k.W + kTile - 1) / kTile) * ((k.H + kTile - 1) / kTile);
+        LEM_LAUNCH(L, k_fat_local, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_la, s.t_dst, s.t_pend, s.t_orng, s.t_ent,
+                   s.list_b, k, s.sc);
+        const uint8_t* mask = s.mask;
+        const uint8_t* fd = s.fd;
+        const float2* tla = s.t_la;
+        const int32_t* torng = s.t_orng;
+        const int32_t* tent = s.t_ent;
+        const int32_t* tdst = s.t_dst;
+        float2* fa = s.fa;
+        int32_t* tpend = s.t_pend;
+        int32_t* la = s.list_b;  // the outlets k_fat_local found ready
+        int32_t* lb = s.list_a;
+        ModelConsts kk = k;
+        DevScalars* sc = s.sc;
+        void* args[] = {(void*)&mask, (void*)&fd, (void*)&tla, (void*)&torng, (void*)&tent, (void*)&tdst,
+                        (void*)&fa, (void*)&tpend, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc};
+        L.pre("k_fat_coarse");
+        LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fat_coarse, dim3(s.max_coop_blocks), dim3(256),
+                                                 args, 0, L.st));
+        L.post();
+        LEM_LAUNCH(L, k_fat_final, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_pend, s.fa, k, s.sc);
+    }
     {
         const uint8_t* mask = s.mask;
         const uint8_t* fd = s.fd;
@@ -208,8 +664,9 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, con
         int32_t* lb = s.list_b;
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
+        int gate = tiled;
         void* args[] = {(void*)&mask, (void*)&fd, (void*)&w, (void*)&prop, (void*)&fa, (void*)&pending,
-                        (void*)&contrib, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc};
+                        (void*)&contrib, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc, (void*)&gate};
         L.pre("k_fa_walk");
         LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fa_walk, dim3(s.max_coop_blocks), dim3(256), args,
                                                  0, L.st));
@@ -343,8 +800,9 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
         ModelConsts k{};
         k.W = width;
         k.H = height;
+        int gate = 0;
         void* args[] = {(void*)&m, (void*)&c, (void*)&ww, (void*)&prop, (void*)&fa, (void*)&pending,
-                        (void*)&contrib, (void*)&la, (void*)&lb, (void*)&k, (void*)&sc};
+                        (void*)&contrib, (void*)&la, (void*)&lb, (void*)&k, (void*)&sc, (void*)&gate};
         LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fa_walk, dim3(nd.blocks), dim3(256), args, 0, st));
     }
     k_na_out<<<blocks, T, 0, st>>>(fa, d_fa, N);
@@ -357,7 +815,7 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
     return LEM_OK;
 }
 
-const void* fa_coop_kernels[] = {(const void*)k_fa_walk};
-extern const int fa_coop_kernel_count = 1;
+const void* fa_coop_kernels[] = {(const void*)k_fa_walk, (const void*)k_fat_coarse};
+extern const int fa_coop_kernel_count = 2;
 
 }  // namespace lem

@@ -222,6 +222,7 @@ __global__ void k_sed_prep(const uint8_t* __restrict__ mask, const uint8_t* __re
 // One cell of MFDsedbud (mfd_accum.cu:32-254): deposition from the donors'
 // erosion, stone mixing with the donors' updated stone, new soil thickness.
 struct SedCell {
+    const uint8_t* mask;
     const uint8_t* fd;
     const float* prop;
     const float* ero;
@@ -271,6 +272,9 @@ struct SedCell {
         if (sedthick > toterosion) stn = sedthick - toterosion;
         soilT[cur] = stn;
     }
+    __device__ __forceinline__ int receivers(int32_t cur, int x, int y, int32_t* r) const {
+        return code_receivers(fd, mask, cur, x, y, W, H, r);
+    }
 };
 
 // The sediment wave: every source starts it; cells follow as their last donor
@@ -280,8 +284,8 @@ __global__ void k_sed_walk(const uint8_t* __restrict__ mask, const uint8_t* __re
                            const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
                            float* fines, float* soilT, int32_t* pending, int32_t* list_a, int32_t* list_b,
                            ModelConsts k, DevScalars* sc) {
-    const SedCell op{fd, prop, ero, inci, geli, depo, stone, fines, soilT, k.W, k.H, k.ddk, k.dck, k.dgk};
-    int done = wave_walk(op, fd, mask, pending, list_a, list_b, k.W, k.H, sc);
+    const SedCell op{mask, fd, prop, ero, inci, geli, depo, stone, fines, soilT, k.W, k.H, k.ddk, k.dck, k.dgk};
+    int done = wave_walk(op, pending, list_a, list_b, k.W, k.H, sc);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&sc->sed_done, done);
 }

@@ -81,11 +81,12 @@ constexpr int kWaveMaxRounds = 1 << 16;
 // it made ready (it was that cell's last donor); further receivers made ready
 // at the same time (MFD) go on the lane's own stack, and only when that is full
 // to the next round's list.  Op::cell(c, x, y) computes and stores cell c,
-// reading finished donors with ld.global.cg.  Returns the cells this thread
-// finished.
+// reading finished donors with ld.global.cg; Op::receivers(c, x, y, r) lists
+// the nodes whose pending count c's completion decrements.  Returns the nodes
+// this thread finished.
 template <class Op>
-__device__ int wave_walk(const Op& op, const uint8_t* __restrict__ fd, const uint8_t* __restrict__ mask,
-                         int32_t* pending, int32_t* list_a, int32_t* list_b, int W, int H, DevScalars* sc) {
+__device__ int wave_walk(const Op& op, int32_t* pending, int32_t* list_a, int32_t* list_b, int W, int H,
+                         DevScalars* sc) {
     namespace cg = cooperative_groups;
     cg::grid_group grid = cg::this_grid();
     const size_t N = (size_t)W * H;
@@ -143,14 +144,11 @@ __device__ int wave_walk(const Op& op, const uint8_t* __restrict__ fd, const uin
                 const int x = cur % W, y = cur / W;
                 op.cell(cur, x, y);
                 ++done;
-                const uint8_t code = fd[cur];
+                int32_t rcv[8];
+                const int nr = op.receivers(cur, x, y, rcv);
                 int32_t next = -1;
-                for (int d = 0; d < 8; ++d) {
-                    if (!(code & dir_bit(d))) continue;
-                    const int rx = x + dir_dx(d), ry = y + dir_dy(d);
-                    if (rx < 0 || rx >= W || ry < 0 || ry >= H) continue;
-                    const int32_t r = ry * W + rx;
-                    if (!mask[r]) continue;
+                for (int j = 0; j < nr; ++j) {
+                    const int32_t r = rcv[j];
                     if (dec_acq_rel(pending + r) == 1) {
                         if (next < 0)
                             next = r;
@@ -169,6 +167,21 @@ __device__ int wave_walk(const Op& op, const uint8_t* __restrict__ fd, const uin
         grid.sync();
     }
     return done;
+}
+
+// Receivers of cell (x, y) by its direction code: in-grid, in-catchment cells.
+__device__ __forceinline__ int code_receivers(const uint8_t* __restrict__ fd, const uint8_t* __restrict__ mask,
+                                              int32_t cur, int x, int y, int W, int H, int32_t* r) {
+    const uint8_t code = __ldg(fd + cur);
+    int nr = 0;
+    for (int d = 0; d < 8; ++d) {
+        if (!(code & dir_bit(d))) continue;
+        const int rx = x + dir_dx(d), ry = y + dir_dy(d);
+        if (rx < 0 || rx >= W || ry < 0 || ry >= H) continue;
+        const int32_t n = ry * W + rx;
+        if (__ldg(mask + n)) r[nr++] = n;
+    }
+    return nr;
 }
 
 }  // namespace lem
