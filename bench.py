@@ -42,13 +42,16 @@ STAGE_BYTES = {
     "flow_direction": 38, "routing": 12, "runoff": 20, "accumulation": 11,
     "erosion": 72, "sediment": 37, "surface": 84,
 }
-KERNEL_STAGE = {
-    "k_flowdirs": "flow_direction", "k_plateau_init": "routing", "k_plateau_relax": "routing",
-    "k_plateau_final": "routing", "k_flood_init": "routing", "k_flood_merge": "routing",
-    "k_flood_jump": "routing", "k_flood_edges": "routing", "k_flood_compact": "routing",
-    "k_flood_spill": "routing", "k_flood_raise": "routing", "k_fd_epilogue": "routing",
-    "k_fa_prep": "runoff", "k_fa_walk": "accumulation", "k_erosion": "erosion",
-    "k_sed_prep": "sediment", "k_sed_walk": "sediment", "k_final": "surface",
+# Per launch and per cell, the fields a kernel must read or write at least once
+# (its share of its stage).  Routing (plateaus, flooding) and the coarse waves
+# touch a data-dependent subset of cells and have no per-cell figure.
+KERNEL_BYTES = {
+    "k_flowdirs": 19,                 # FlowDirs, two launches per step: 38 / 2
+    "k_fa_prep": 20,                  # runoff
+    "k_fa_walk": 11, "k_fat_final": 9, "k_fat_local": 5,  # accumulation: R code, w (+ W fa)
+    "k_erosion": 72,
+    "k_sed_walk": 37, "k_sedt_final": 37, "k_sedt_local": 21,  # sediment: R code, ero/inci/geli, stone, soilT (+ W)
+    "k_final": 84,
 }
 B_ALG = sum(STAGE_BYTES.values())
 
@@ -300,9 +303,7 @@ def main():
     hbm, peak_kind = peaks()
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 1.0))
     kname, (klaunches, kms) = dom
-    stage = KERNEL_STAGE.get(kname)
-    kbytes_per_launch = (STAGE_BYTES.get(stage, 0) * cells * args.steps / max(klaunches, 1)) if stage else 0
-    achieved = kbytes_per_launch / (kms / klaunches / 1e3) / 1e9 if kms > 0 else 0.0
+    kbytes_per_launch = KERNEL_BYTES.get(kname, 0) * cells
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
     if os.path.exists(tfile):
@@ -310,6 +311,12 @@ def main():
             traffic = json.load(open(tfile)).get(kname)
         except Exception:
             traffic = None
+    bytes_source = "algorithmic"
+    if kbytes_per_launch == 0 and traffic:
+        # data-dependent kernel: its measured DRAM bytes per launch stand in
+        kbytes_per_launch = traffic
+        bytes_source = "ncu dram bytes per launch (data-dependent kernel)"
+    achieved = kbytes_per_launch / (kms / klaunches / 1e3) / 1e9 if kms > 0 else 0.0
     cpu = None if args.no_cpu else cpu_sample(S)
     step_ms = ms_max / args.steps
     line = {
@@ -327,7 +334,8 @@ def main():
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_kind": f"{peak_kind} hbm_gbs",
-                     "algorithmic_bytes_per_launch": kbytes_per_launch, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": kbytes_per_launch, "bytes_source": bytes_source,
+                     "traffic": traffic,
                      "step_level": {"bytes_per_cell_timestep": B_ALG,
                                     "achieved": B_ALG * cells / (step_ms / 1e3) / 1e9,
                                     "frac": B_ALG * cells / (step_ms / 1e3) / 1e9 / hbm}},

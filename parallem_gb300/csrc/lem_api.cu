@@ -283,7 +283,12 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
     {
         const size_t tiles = (size_t)((grid->width + kTile - 1) / kTile) * ((grid->height + kTile - 1) / kTile);
         ALLOC(s.t_ent, tiles * kTileEnt);
+        ALLOC(s.p_abc, tiles * kTile * kTile);
+        ALLOC(s.p_ref, tiles * kTilePool);
+        ALLOC(s.p_map, tiles * kTilePool);
+        ALLOC(s.p_val, tiles * kTile * kTile);
     }
+    ALLOC(s.t_stat, N);
     if (params->flow_direction_type != 0 && params->mfd_proportions) {
         ALLOC(s.prop, 8 * N);
     }

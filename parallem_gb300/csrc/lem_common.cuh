@@ -97,6 +97,7 @@ struct DevScalars {
     int32_t counters[8];
     int32_t tiled_ok;                // 1: this step's accumulation may take the tiled path
     int32_t tile_src;                // tile outlets with no pending inflow (coarse sources)
+    int32_t sed_tiled_ok;            // 1: this step's sediment routing may take the tiled path
 };
 
 }  // namespace lem

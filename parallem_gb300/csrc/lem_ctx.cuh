@@ -7,6 +7,7 @@ namespace lem {
 
 constexpr int kTile = 32;     // edge of the accumulation tiles
 constexpr int kTileEnt = 136; // inflow slots per tile (inflows come from the 132 halo ring cells)
+constexpr int kTilePool = 1280; // sediment node inputs per tile: one per waiting in-tile edge (< 1024) or inflow (< 132)
 
 // Dreybrodt temperature response table (see lem_mod.cu): log10 of
 // K1*KC*KH / (4*K2*gammaCa*gammaHCO3^2) sampled every kTabStep degrees.
@@ -73,6 +74,13 @@ struct DevState {
     int32_t* t_orng;    // outlet: (first << 16) | count of its inflows in t_ent
     float2* t_la;       // outlet: accumulation from inside its tile only
     int32_t* t_ent;     // per tile, kTileEnt inflow cells (outlets of neighbours) grouped by outlet
+    // tiled sediment routing: per tile, the cells that wait on other tiles as
+    // programs (one per outlet, kTile*kTile slots per tile)
+    float4* p_abc;      // node: stone mix coefficients A, B, the settled donors' sum C, inputs and flags
+    int32_t* p_ref;     // per tile, kPool node inputs: the feeding node (program slot) or cell
+    float4* p_map;      // per tile, kPool node inputs: the map through the cells in between
+    float* p_val;       // slot: values of programs longer than the evaluator's local buffer
+    uint8_t* t_stat;    // cell: 1 settled inside its tile, 2 waits on another tile, 0 neither
     // flooding tables
     unsigned long long* ekey;   // hash keys (label pair)
     unsigned long long* ewt;    // min boundary height key

@@ -177,11 +177,6 @@ __global__ void k_fa_walk(const uint8_t* __restrict__ mask, const uint8_t* __res
 // clamps those to zero); k_fa_prep disables the path for a step with a
 // negative weight or a multi-direction code, and the walk then runs instead.
 
-constexpr int kTH = kTile + 2;  // tile with its one-cell halo
-constexpr uint8_t kKindIn = 0, kKindOutlet = 1, kKindEnd = 2;
-constexpr uint8_t kCellOff = 0;    // outside the grid, or outside the catchment with a nodata DEM
-constexpr uint8_t kCellIn = 1;     // in the catchment
-constexpr uint8_t kCellBlock = 2;  // outside the catchment with a DEM value: a donor that never completes
 
 __device__ __forceinline__ void tile_load(const double* __restrict__ z, const uint8_t* __restrict__ mask,
                                           const uint8_t* __restrict__ fd, int W, int H, int tx0, int ty0,
@@ -200,18 +195,6 @@ __device__ __forceinline__ void tile_load(const double* __restrict__ z, const ui
         s_code[j] = c;
         s_cls[j] = cl;
     }
-}
-
-__device__ __forceinline__ bool in_tile(int lx, int ly) { return lx >= 0 && lx < kTile && ly >= 0 && ly < kTile; }
-
-// The halo ring in a fixed order: top row, bottom row, left column, right column.
-constexpr int kRing = 4 * kTH - 4;
-constexpr int kRingChunks = (kRing + 31) / 32;
-__device__ __forceinline__ int ring_halo(int i) {
-    if (i < kTH) return i;
-    if (i < 2 * kTH) return (kTH - 1) * kTH + (i - kTH);
-    if (i < 2 * kTH + kTile) return (i - 2 * kTH + 1) * kTH;
-    return (i - 2 * kTH - kTile + 1) * kTH + kTH - 1;
 }
 
 __global__ void __launch_bounds__(256)

@@ -183,7 +183,9 @@ __global__ void __launch_bounds__(256)
 
 // sedmfdaccum set-up (mfd_accum.cu:389-396): depo = 1e-5 in the catchment;
 // cells in row 0 or column 0 are never processed (:42) and masked cells never
-// complete, so a donor of either kind blocks its receiver for good.
+// complete, so a donor of either kind blocks its receiver for good.  A step
+// with a multi-direction code among these cells takes the walk instead of the
+// tiled path.
 __global__ void k_sed_prep(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                            float* __restrict__ depo, int32_t* __restrict__ pending, int32_t* ready, ModelConsts k,
                            DevScalars* sc) {
@@ -198,6 +200,8 @@ __global__ void k_sed_prep(const uint8_t* __restrict__ mask, const uint8_t* __re
             if (mask[i]) {
                 depo[i] = 0.00001f;
                 if (x != 0 && y != 0) {
+                    const uint8_t code = fd[i];
+                    if (code & (code - 1)) sc->sed_tiled_ok = 0;
                     pend = 0;
 #pragma unroll
                     for (int d = 0; d < 8; ++d) {
@@ -217,6 +221,49 @@ __global__ void k_sed_prep(const uint8_t* __restrict__ mask, const uint8_t* __re
         }
         wave_append(src, (int32_t)i, ready, &sc->counters[0], (int)N, &sc->err);
     }
+}
+
+// The per-cell arithmetic of MFDsedbud (mfd_accum.cu:222-249), rounded the same
+// way wherever it is evaluated (no contraction): deposition, the stone mix
+// coefficients (stone = A + B * from, clamped, when the sediment column is not
+// empty; stone kept otherwise) and the new soil thickness.
+struct SedLocal {
+    float dep, A, B, stn;
+    bool nz;
+};
+__device__ __forceinline__ SedLocal sed_local(float ad, float ac, float ag, float e, float ic, float g, float st0,
+                                              float stone0, float ddk, float dck, float dgk) {
+    SedLocal r;
+    r.dep = __fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(ad, e), ddk), __fmul_rn(__fadd_rn(ac, ic), dck)),
+                      __fmul_rn(__fadd_rn(ag, g), dgk));
+    const float sedthick = __fadd_rn(st0, r.dep);
+    r.nz = sedthick != 0.0f;
+    const float old = r.nz ? __fdiv_rn(st0, sedthick) : 0.0f;
+    r.B = __fsub_rn(1.0f, old);
+    r.A = r.nz ? __fmul_rn(old, stone0) : stone0;
+    const float toterosion = __fadd_rn(__fadd_rn(e, ic), g);
+    float stn = st0;
+    if (toterosion >= sedthick) stn = 0.0f;
+    if (sedthick > toterosion) stn = __fsub_rn(sedthick, toterosion);
+    r.stn = stn;
+    return r;
+}
+__device__ __forceinline__ float sed_mix(float A, float B, float from) {
+    float sn = __fadd_rn(A, __fmul_rn(B, from));
+    if (sn < 0.01f)
+        sn = 0.01f;
+    else if (sn > 99.9f)
+        sn = 99.9f;
+    return sn;
+}
+__device__ __forceinline__ void sed_store(size_t g, const SedLocal& L, float sn, float* depo, float* stone,
+                                          float* fines, float* soilT) {
+    depo[g] = L.dep;
+    if (L.nz) {
+        __stcg(stone + g, sn);
+        fines[g] = __fsub_rn(100.0f, sn);
+    }
+    soilT[g] = L.stn;
 }
 
 // One cell of MFDsedbud (mfd_accum.cu:32-254): deposition from the donors'
@@ -245,32 +292,14 @@ struct SedCell {
             const int32_t n = ny * W + nx;
             if (!donates(__ldg(fd + n), d)) continue;
             const float p = prop ? __ldg(prop + 8 * (size_t)n + ((d + 4) & 7)) : 1.0f;
-            ad += p * (__ldg(ero + n) * omd);
-            ac += p * (__ldg(inci + n) * omc);
-            ag += p * (__ldg(geli + n) * omg);
-            from += p * __ldcg(stone + n);
+            ad = __fadd_rn(ad, __fmul_rn(p, __fmul_rn(__ldg(ero + n), omd)));
+            ac = __fadd_rn(ac, __fmul_rn(p, __fmul_rn(__ldg(inci + n), omc)));
+            ag = __fadd_rn(ag, __fmul_rn(p, __fmul_rn(__ldg(geli + n), omg)));
+            from = __fadd_rn(from, __fmul_rn(p, __ldcg(stone + n)));
         }
-        const float e = __ldg(ero + cur), ic = __ldg(inci + cur), g = __ldg(geli + cur);
-        const float dep = ((ad + e) * ddk) + ((ac + ic) * dck) + ((ag + g) * dgk);
-        depo[cur] = dep;
-        const float st0 = soilT[cur];
-        const float sedthick = st0 + dep;
-        if (sedthick != 0.0f) {
-            const float old = st0 / sedthick;
-            const float input = 1.0f - old;
-            float sn = (old * __ldcg(stone + cur)) + (input * from);
-            if (sn < 0.01f)
-                sn = 0.01f;
-            else if (sn > 99.9f)
-                sn = 99.9f;
-            __stcg(stone + cur, sn);
-            fines[cur] = 100.0f - sn;
-        }
-        const float toterosion = e + ic + g;
-        float stn = st0;
-        if (toterosion >= sedthick) stn = 0.0f;
-        if (sedthick > toterosion) stn = sedthick - toterosion;
-        soilT[cur] = stn;
+        const SedLocal L = sed_local(ad, ac, ag, __ldg(ero + cur), __ldg(inci + cur), __ldg(geli + cur), soilT[cur],
+                                     __ldcg(stone + cur), ddk, dck, dgk);
+        sed_store(cur, L, L.nz ? sed_mix(L.A, L.B, from) : 0.0f, depo, stone, fines, soilT);
     }
     __device__ __forceinline__ int receivers(int32_t cur, int x, int y, int32_t* r) const {
         return code_receivers(fd, mask, cur, x, y, W, H, r);
@@ -278,16 +307,654 @@ struct SedCell {
 };
 
 // The sediment wave: every source starts it; cells follow as their last donor
-// finishes.
+// finishes.  With gate set it runs only when the tiled path is off.
 __global__ void k_sed_walk(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                            const float* __restrict__ prop, const float* __restrict__ ero,
                            const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
                            float* fines, float* soilT, int32_t* pending, int32_t* list_a, int32_t* list_b,
-                           ModelConsts k, DevScalars* sc) {
+                           ModelConsts k, DevScalars* sc, int gate) {
+    if (gate && sc->sed_tiled_ok) return;
     const SedCell op{mask, fd, prop, ero, inci, geli, depo, stone, fines, soilT, k.W, k.H, k.ddk, k.dck, k.dgk};
     int done = wave_walk(op, pending, list_a, list_b, k.W, k.H, sc);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&sc->sed_done, done);
+}
+
+// ---------------------------------------------------------------------------
+// Tiled sediment routing for single-receiver codes, on the tiles of the tiled
+// accumulation.  Deposition and soil thickness are local; only the stone mix
+// carries the donors' new values downstream, through a clamp, so the coarse
+// level cannot add partial sums.  Instead:
+//   local : per tile, cells with no donor outside the tile upstream are
+//           settled and stored; the others ("waiting" cells) are written as a
+//           program per outlet, in dependency order: A, B, the sum C of the
+//           settled donors and references to the waiting donors (earlier
+//           slots of the same program, or cells of other tiles);
+//   coarse: a wave over the outlets: an outlet whose inflows are all final
+//           runs its program and stores its own new values;
+//   final : per tile, the remaining waiting cells by the per-cell formula.
+// Cell classes follow MFDsedbud: in-catchment cells off row 0 and column 0 are
+// computed; every other in-grid donor blocks its receiver.
+
+constexpr int kProgLocal = 256;  // program nodes the coarse evaluator keeps in local memory
+constexpr int kPool = kTilePool;
+constexpr uint8_t kFDone = 1, kFTaint = 2;
+
+// Maps of a value through a run of single-input cells: v -> clamp(a*v + b, lo, hi)
+// as float4(a, b, lo, hi); lo > hi encodes the constant b (a cell whose
+// sediment column is empty keeps its stone whatever its donors carry).
+__device__ __forceinline__ float4 map_identity() { return make_float4(1.0f, 0.0f, -INFINITY, INFINITY); }
+__device__ __forceinline__ float4 map_const(float c) { return make_float4(0.0f, c, INFINITY, -INFINITY); }
+__device__ __forceinline__ float map_apply(const float4 m, float v) {
+    if (m.z > m.w) return m.y;
+    const float y = __fadd_rn(__fmul_rn(m.x, v), m.y);
+    return y < m.z ? m.z : (y > m.w ? m.w : y);
+}
+// a single-input cell: from = C + v, stone = clamp(A + B * from) (or its old stone S)
+__device__ __forceinline__ float4 map_cell(float A, float B, float C, bool nz, float S) {
+    if (!nz) return map_const(S);
+    return make_float4(B, __fadd_rn(A, __fmul_rn(B, C)), 0.01f, 99.9f);
+}
+// outer after inner
+__device__ __forceinline__ float4 map_compose(const float4 outer, const float4 inner) {
+    if (outer.z > outer.w) return outer;
+    if (inner.z > inner.w) return map_const(map_apply(outer, inner.y));
+    const float a1 = outer.x, b1 = outer.y;
+    if (a1 == 0.0f) return map_const(map_apply(outer, 0.0f));
+    const float L = __fadd_rn(__fmul_rn(a1, a1 > 0.0f ? inner.z : inner.w), b1);
+    const float U = __fadd_rn(__fmul_rn(a1, a1 > 0.0f ? inner.w : inner.z), b1);
+    const float lo = fmaxf(L, outer.z), hi = fminf(U, outer.w);
+    if (lo > hi) return map_const(U < outer.z ? outer.z : outer.w);
+    return make_float4(__fmul_rn(a1, inner.x), __fadd_rn(__fmul_rn(a1, inner.y), b1), lo, hi);
+}
+
+__device__ __forceinline__ void sed_tile_load(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd, int W,
+                                              int H, int tx0, int ty0, uint8_t* s_code, uint8_t* s_cls) {
+    for (int j = threadIdx.x; j < kTH * kTH; j += blockDim.x) {
+        const int gx = tx0 - 1 + j % kTH, gy = ty0 - 1 + j / kTH;
+        uint8_t c = 0, cl = kCellOff;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            const size_t g = (size_t)gy * W + gx;
+            c = fd[g];
+            cl = (mask[g] && gx != 0 && gy != 0) ? kCellIn : kCellBlock;
+        }
+        s_code[j] = c;
+        s_cls[j] = cl;
+    }
+}
+
+// Static part of a cell: deposition from all donors (in scan order), the mix
+// coefficients and the new soil thickness; pend counts donors inside the tile,
+// ext those outside, kBlocked marks a blocked donor.
+struct SedInit {
+    SedLocal L;
+    int32_t pend;
+    int ext;
+};
+__device__ __forceinline__ SedInit sed_init(const uint8_t* s_code, const uint8_t* s_cls, int lx, int ly, int tx0,
+                                            int ty0, int W, const float* __restrict__ ero,
+                                            const float* __restrict__ inci, const float* __restrict__ geli,
+                                            const float* __restrict__ soilT, const float* stone, const ModelConsts& k) {
+    const float omd = 1.0f - k.ddk, omc = 1.0f - k.dck, omg = 1.0f - k.dgk;
+    const int hc = (ly + 1) * kTH + lx + 1;
+    SedInit r;
+    r.pend = 0;
+    r.ext = 0;
+    float ad = 0.f, ac = 0.f, ag = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+        const int d = scan_dir(kk);
+        const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+        if (!donates(s_code[nh], d)) continue;
+        const uint8_t cl = s_cls[nh];
+        if (cl == kCellBlock) {
+            r.pend |= kBlocked;
+            continue;
+        }
+        if (cl != kCellIn) continue;
+        const size_t n = (size_t)(ty0 + ly + dir_dy(d)) * W + tx0 + lx + dir_dx(d);
+        ad = __fadd_rn(ad, __fmul_rn(1.0f, __fmul_rn(__ldg(ero + n), omd)));
+        ac = __fadd_rn(ac, __fmul_rn(1.0f, __fmul_rn(__ldg(inci + n), omc)));
+        ag = __fadd_rn(ag, __fmul_rn(1.0f, __fmul_rn(__ldg(geli + n), omg)));
+        if (in_tile(lx + dir_dx(d), ly + dir_dy(d)))
+            ++r.pend;
+        else
+            ++r.ext;
+    }
+    const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
+    r.L = sed_local(ad, ac, ag, __ldg(ero + g), __ldg(inci + g), __ldg(geli + g), soilT[g], __ldcg(stone + g), k.ddk,
+                    k.dck, k.dgk);
+    return r;
+}
+
+__global__ void __launch_bounds__(256)
+    k_sedt_local(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd, const float* __restrict__ ero,
+                 const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
+                 float* fines, float* soilT, int32_t* __restrict__ t_dst, int32_t* __restrict__ t_pend,
+                 int32_t* __restrict__ t_orng, float2* __restrict__ t_out, float4* __restrict__ p_abc,
+                 int32_t* __restrict__ p_ref, float4* __restrict__ p_map, uint8_t* __restrict__ t_stat,
+                 int32_t* srcs, ModelConsts k, DevScalars* sc) {
+    if (!sc->sed_tiled_ok) return;
+    __shared__ uint8_t s_code[kTH * kTH];
+    __shared__ uint8_t s_cls[kTH * kTH];
+    __shared__ int32_t s_pend[kTile * kTile];
+    __shared__ float s_new[kTile * kTile];  // settled stone (the old stone until then)
+    __shared__ float s_A[kTile * kTile];
+    __shared__ float s_B[kTile * kTile];
+    __shared__ float s_dep[kTile * kTile];
+    __shared__ float s_stn[kTile * kTile];
+    __shared__ int16_t s_ptr[kTile * kTile];
+    __shared__ int16_t s_topo[kTile * kTile];
+    __shared__ int16_t s_pos[kTile * kTile];
+    __shared__ int16_t s_oslot[kTile * kTile];
+    __shared__ uint8_t s_kind[kTile * kTile];
+    __shared__ uint8_t s_ext[kTile * kTile];
+    __shared__ uint8_t s_flag[kTile * kTile];
+    __shared__ uint8_t s_nz[kTile * kTile];
+    __shared__ int16_t s_olist[kTileEnt];
+    __shared__ int32_t s_ocnt[kTileEnt];
+    __shared__ int32_t s_pcnt[kTileEnt];
+    __shared__ int16_t s_pstart[kTileEnt];
+    __shared__ int16_t s_pfill[kTileEnt];
+    __shared__ int s_no, s_nt, s_done, s_pool;
+    const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
+    const int t = blockIdx.x;
+    const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
+    sed_tile_load(mask, fd, W, H, tx0, ty0, s_code, s_cls);
+    if (threadIdx.x < kTileEnt) {
+        s_ocnt[threadIdx.x] = 0;
+        s_pcnt[threadIdx.x] = 0;
+    }
+    if (threadIdx.x == 0) s_nt = s_done = 0;
+    __syncthreads();
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
+    bool src[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
+        int32_t pend = kBlocked;
+        uint8_t kind = kKindEnd, ext = 0, nz = 0;
+        int16_t ptr = (int16_t)l;
+        float A = 0.f, B = 0.f, dep = 0.f, stn = 0.f, snew = 0.f;
+        if (s_cls[hc] == kCellIn) {
+            const SedInit in = sed_init(s_code, s_cls, lx, ly, tx0, ty0, W, ero, inci, geli, soilT, stone, k);
+            pend = in.pend;
+            ext = (uint8_t)in.ext;
+            A = in.L.A;
+            B = in.L.B;
+            dep = in.L.dep;
+            stn = in.L.stn;
+            nz = in.L.nz;
+            snew = __ldcg(stone + (size_t)(ty0 + ly) * W + tx0 + lx);
+            const int d = bit_dir(s_code[hc]);
+            if (d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn) {
+                const int rlx = lx + dir_dx(d), rly = ly + dir_dy(d);
+                if (in_tile(rlx, rly)) {
+                    kind = kKindIn;
+                    ptr = (int16_t)(rly * kTile + rlx);
+                } else {
+                    kind = kKindOutlet;
+                }
+            }
+        }
+        s_pend[l] = pend;
+        src[q] = pend == 0;
+        s_kind[l] = kind;
+        s_ext[l] = ext;
+        s_ptr[l] = ptr;
+        s_new[l] = snew;
+        s_A[l] = A;
+        s_B[l] = B;
+        s_dep[l] = dep;
+        s_stn[l] = stn;
+        s_nz[l] = nz;
+        s_flag[l] = 0;
+        s_pos[l] = -1;
+    }
+    __syncthreads();
+    // settle what depends on this tile only; order the waiting cells
+    int done = 0;
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        int cur = src[q] ? (ly0 + 8 * q) * kTile + lx : -1;
+        for (int guard = 0; cur >= 0 && guard < kTile * kTile; ++guard) {
+            const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
+            bool taint = s_ext[cur] != 0;
+            float from = 0.f;
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const int d = scan_dir(kk);
+                const int nlx = cx + dir_dx(d), nly = cy + dir_dy(d);
+                if (!in_tile(nlx, nly)) continue;
+                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+                if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
+                const int n = nly * kTile + nlx;
+                if (s_flag[n] & kFTaint)
+                    taint = true;
+                else
+                    from = __fadd_rn(from, __fmul_rn(1.0f, s_new[n]));
+            }
+            if (!taint) {
+                SedLocal L;
+                L.dep = s_dep[cur];
+                L.A = s_A[cur];
+                L.B = s_B[cur];
+                L.stn = s_stn[cur];
+                L.nz = s_nz[cur] != 0;
+                const float sn = L.nz ? sed_mix(L.A, L.B, from) : s_new[cur];
+                s_new[cur] = sn;
+                sed_store((size_t)(ty0 + cy) * W + tx0 + cx, L, sn, depo, stone, fines, soilT);
+                s_flag[cur] = kFDone;
+                ++done;
+            } else {
+                s_flag[cur] = kFDone | kFTaint;
+                s_topo[atomicAdd(&s_nt, 1)] = (int16_t)cur;
+            }
+            __threadfence_block();
+            int nxt = -1;
+            if (s_kind[cur] == kKindIn) {
+                const int r = s_ptr[cur];
+                if (atomicSub(&s_pend[r], 1) == 1) {
+                    __threadfence_block();
+                    nxt = r;
+                }
+            }
+            cur = nxt;
+        }
+    }
+    __syncthreads();
+    for (int it = 0; it < 10; ++it) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int l = (ly0 + 8 * q) * kTile + lx;
+            s_ptr[l] = s_ptr[s_ptr[l]];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx;
+        const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
+        if (s_ext[l]) {
+            const int e = s_ptr[l];
+            t_dst[g] = s_kind[e] == kKindOutlet ? (int32_t)((ty0 + e / kTile) * W + tx0 + (e & (kTile - 1))) : -1;
+        }
+        if (tx0 + lx < W && ty0 + ly < H) t_stat[g] = (s_flag[l] & kFDone) ? ((s_flag[l] & kFTaint) ? 2 : 1) : 0;
+    }
+    if (threadIdx.x < 32) {
+        const unsigned below = (1u << lx) - 1u;
+        int no = 0;
+        for (int base = 0; base < kTile * kTile; base += 32) {
+            const int l = base + lx;
+            const bool io = s_kind[l] == kKindOutlet;
+            const unsigned mo = __ballot_sync(0xffffffffu, io);
+            if (io) {
+                s_olist[no + __popc(mo & below)] = (int16_t)l;
+                s_oslot[l] = (int16_t)(no + __popc(mo & below));
+            }
+            no += __popc(mo);
+        }
+        if (lx == 0) s_no = no;
+    }
+    __syncthreads();
+    // inflows per outlet (ring cells flowing into the tile)
+    if (threadIdx.x < kRing) {
+        const int h = ring_halo(threadIdx.x);
+        const int d = s_cls[h] == kCellIn ? bit_dir(s_code[h]) : -1;
+        if (d >= 0) {
+            const int hx = h % kTH + dir_dx(d), hy = h / kTH + dir_dy(d);
+            if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile && s_cls[hy * kTH + hx] == kCellIn) {
+                const int o = s_ptr[(hy - 1) * kTile + hx - 1];
+                if (s_kind[o] == kKindOutlet) atomicAdd(&s_ocnt[s_oslot[o]], 1);
+            }
+        }
+    }
+    // program nodes: waiting cells draining to an outlet that take an inflow
+    // from another tile, join two waiting branches, or are the outlet.  The
+    // waiting cells between nodes pass one value on; they become the maps of
+    // the nodes' inputs.
+    int32_t* s_node = s_pend;  // the in-degrees are spent
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
+        bool node = false;
+        if (s_flag[l] == (kFDone | kFTaint) && s_kind[s_ptr[l]] == kKindOutlet) {
+            int ntd = 0;
+#pragma unroll
+            for (int d = 0; d < 8; ++d) {
+                const int nlx = lx + dir_dx(d), nly = ly + dir_dy(d);
+                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+                if (in_tile(nlx, nly) && donates(s_code[nh], d) && s_cls[nh] == kCellIn &&
+                    (s_flag[nly * kTile + nlx] & kFTaint))
+                    ++ntd;
+            }
+            node = s_ext[l] != 0 || ntd >= 2 || s_kind[l] == kKindOutlet;
+        }
+        s_node[l] = node;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int l = (ly0 + 8 * q) * kTile + lx;
+        if (s_node[l]) atomicAdd(&s_pcnt[s_oslot[s_ptr[l]]], 1);
+    }
+    __syncthreads();
+    const int no = s_no, nt = s_nt;
+    if (threadIdx.x == 0) {
+        int a = 0;
+        for (int i = 0; i < no; ++i) {
+            s_pstart[i] = (int16_t)a;
+            s_pfill[i] = (int16_t)a;
+            a += s_pcnt[i];
+        }
+        s_pool = 0;
+    }
+    __syncthreads();
+    // node slots: grouped by outlet, in the order the cells were reached
+    if (threadIdx.x < 32) {
+        const unsigned below = (1u << lx) - 1u;
+        for (int base = 0; base < nt; base += 32) {
+            const int i = base + lx;
+            int key = -1, c = 0;
+            if (i < nt) {
+                c = s_topo[i];
+                if (s_node[c]) key = s_oslot[s_ptr[c]];
+            }
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            const int fill = key >= 0 ? s_pfill[key] : 0;
+            __syncwarp();
+            if (key >= 0) {
+                s_pos[c] = (int16_t)(fill + __popc(peers & below));
+                if ((peers & below) == 0) s_pfill[key] = (int16_t)(fill + __popc(peers));
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    const size_t nbase = (size_t)t * kTile * kTile;
+    const size_t pool = (size_t)t * kPool;
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
+        if (!s_node[l]) continue;
+        const int pos = s_pos[l];
+        const int first = s_pstart[s_oslot[s_ptr[l]]];
+        int nin = 0;
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+            const int nlx = lx + dir_dx(d), nly = ly + dir_dy(d);
+            const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+            if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
+            if (!in_tile(nlx, nly) || (s_flag[nly * kTile + nlx] & kFTaint)) ++nin;
+        }
+        const int start = atomicAdd(&s_pool, nin);
+        if (start + nin > kPool) {
+            atomicOr(&sc->err, ErrFlags::kCapacity);
+            continue;
+        }
+        float C = 0.f;
+        int m = 0;
+#pragma unroll 1
+        for (int kk = 0; kk < 8; ++kk) {
+            const int d = scan_dir(kk);
+            const int nlx = lx + dir_dx(d), nly = ly + dir_dy(d);
+            const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+            if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
+            if (!in_tile(nlx, nly)) {
+                p_ref[pool + start + m] = (ty0 + nly) * W + tx0 + nlx;
+                p_map[pool + start + m] = map_identity();
+                ++m;
+                continue;
+            }
+            int cur = nly * kTile + nlx;
+            if (!(s_flag[cur] & kFTaint)) {
+                C = __fadd_rn(C, __fmul_rn(1.0f, s_new[cur]));
+                continue;
+            }
+            // follow the single-input cells up to the node that feeds this input
+            float4 H = map_identity();
+            for (int guard = 0; !s_node[cur] && guard < kTile * kTile; ++guard) {
+                const int cx = cur & (kTile - 1), cy = cur / kTile, ch = (cy + 1) * kTH + cx + 1;
+                float Cc = 0.f;
+                int up = cur;
+#pragma unroll
+                for (int k2 = 0; k2 < 8; ++k2) {
+                    const int d2 = scan_dir(k2);
+                    const int ulx = cx + dir_dx(d2), uly = cy + dir_dy(d2);
+                    const int uh = ch + dir_dy(d2) * kTH + dir_dx(d2);
+                    if (!in_tile(ulx, uly) || !donates(s_code[uh], d2) || s_cls[uh] != kCellIn) continue;
+                    const int u = uly * kTile + ulx;
+                    if (s_flag[u] & kFTaint)
+                        up = u;
+                    else
+                        Cc = __fadd_rn(Cc, __fmul_rn(1.0f, s_new[u]));
+                }
+                H = map_compose(H, map_cell(s_A[cur], s_B[cur], Cc, s_nz[cur] != 0, s_new[cur]));
+                if (up == cur) break;  // not reached: a waiting cell always has a waiting donor or an inflow
+                cur = up;
+            }
+            p_ref[pool + start + m] = -(s_pos[cur] - first + 1);
+            p_map[pool + start + m] = H;
+            ++m;
+        }
+        p_abc[nbase + pos] = make_float4(s_A[l], s_B[l], C, __int_as_float(start | (m << 11) | (s_nz[l] << 15)));
+    }
+    const int j = threadIdx.x;
+    bool ready = false;
+    int32_t og = 0;
+    if (j < no) {
+        const int o = s_olist[j];
+        const int32_t opend = ((s_flag[o] & kFDone) ? 0 : kBlocked) + s_ocnt[j];
+        og = (ty0 + o / kTile) * W + tx0 + (o & (kTile - 1));
+        t_orng[og] = ((int)s_pstart[j] << 16) | s_pcnt[j];
+        t_pend[og] = opend;
+        t_out[og] = make_float2(s_dep[o], s_stn[o]);
+        ready = (opend == 0);
+    }
+    wave_append(ready, og, srcs, &sc->tile_src, W * H, &sc->err);
+    done = wsum(done);
+    if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_done) atomicAdd(&sc->sed_done, s_done);
+}
+
+// One outlet of the coarse sediment wave: its program, then its own stores.
+struct SedCoarse {
+    const uint8_t* fd;
+    const int32_t* t_orng;
+    const int32_t* t_dst;
+    const float2* t_out;
+    const float4* p_abc;
+    const int32_t* p_ref;
+    const float4* p_map;
+    float* p_val;
+    float* depo;
+    float* stone;
+    float* fines;
+    float* soilT;
+    int W, TW;
+    __device__ __forceinline__ void cell(int32_t o, int x, int y) const {
+        const int rng = __ldg(t_orng + o);
+        const int cnt = rng & 0xffff;
+        if (cnt == 0) return;  // settled inside its tile
+        const int t = (y / kTile) * TW + x / kTile;
+        const size_t nbase = (size_t)t * kTile * kTile + (rng >> 16);
+        const size_t pool = (size_t)t * kPool;
+        float vals[kProgLocal];
+        float sn = 0.f;
+        bool nz = false;
+        for (int i = 0; i < cnt; ++i) {
+            const float4 r = __ldg(p_abc + nbase + i);
+            const int meta = __float_as_int(r.w);
+            const int start = meta & 2047, nin = (meta >> 11) & 15;
+            nz = (meta >> 15) & 1;
+            float from = r.z;
+            for (int jr = 0; jr < nin; ++jr) {
+                const int32_t ref = __ldg(p_ref + pool + start + jr);
+                const float4 mp = __ldg(p_map + pool + start + jr);
+                float v;
+                if (ref >= 0)
+                    v = __ldcg(stone + ref);
+                else if (-ref - 1 < kProgLocal)
+                    v = vals[-ref - 1];
+                else
+                    v = __ldcg(p_val + nbase - ref - 1);
+                from = __fadd_rn(from, __fmul_rn(1.0f, map_apply(mp, v)));
+            }
+            sn = nz ? sed_mix(r.x, r.y, from) : r.x;
+            if (i < kProgLocal)
+                vals[i] = sn;
+            else
+                __stcg(p_val + nbase + i, sn);
+        }
+        // the outlet is the last node of its program
+        const float2 out = __ldg(t_out + o);
+        depo[o] = out.x;
+        if (nz) {
+            __stcg(stone + o, sn);
+            fines[o] = __fsub_rn(100.0f, sn);
+        }
+        soilT[o] = out.y;
+    }
+    __device__ __forceinline__ int receivers(int32_t o, int x, int y, int32_t* r) const {
+        const int d = bit_dir(__ldg(fd + o));
+        const int32_t rc = (y + dir_dy(d)) * W + x + dir_dx(d);
+        const int32_t dst = __ldg(t_dst + rc);
+        r[0] = dst;
+        return dst >= 0 ? 1 : 0;
+    }
+};
+
+__global__ void k_sedt_coarse(const uint8_t* __restrict__ fd, const int32_t* __restrict__ t_orng,
+                              const int32_t* __restrict__ t_dst, const float2* __restrict__ t_out,
+                              const float4* __restrict__ p_abc, const int32_t* __restrict__ p_ref,
+                              const float4* __restrict__ p_map, float* p_val,
+                              float* depo, float* stone, float* fines, float* soilT, int32_t* t_pend,
+                              int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc) {
+    if (!sc->sed_tiled_ok) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->counters[0] = sc->tile_src;
+    const SedCoarse op{fd, t_orng, t_dst, t_out, p_abc, p_ref, p_map, p_val, depo, stone, fines, soilT,
+                       k.W, (k.W + kTile - 1) / kTile};
+    int done = wave_walk(op, t_pend, list_a, list_b, k.W, k.H, sc);
+    (void)done;
+}
+
+__global__ void __launch_bounds__(256)
+    k_sedt_final(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd, const float* __restrict__ ero,
+                 const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
+                 float* fines, float* soilT, const int32_t* __restrict__ t_pend, const uint8_t* __restrict__ t_stat,
+                 ModelConsts k, DevScalars* sc) {
+    if (!sc->sed_tiled_ok) return;
+    __shared__ uint8_t s_code[kTH * kTH];
+    __shared__ uint8_t s_cls[kTH * kTH];
+    __shared__ uint8_t s_hok[kTH * kTH];
+    __shared__ float s_hval[kTH * kTH];
+    __shared__ int32_t s_pend[kTile * kTile];
+    __shared__ float s_new[kTile * kTile];
+    __shared__ uint8_t s_stat[kTile * kTile];
+    __shared__ int s_done;
+    const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
+    const int t = blockIdx.x;
+    const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
+    sed_tile_load(mask, fd, W, H, tx0, ty0, s_code, s_cls);
+    if (threadIdx.x < kRing) {
+        const int h = ring_halo(threadIdx.x);
+        const int gx = tx0 - 1 + h % kTH, gy = ty0 - 1 + h / kTH;
+        uint8_t ok = 0;
+        float v = 0.f;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            const size_t g = (size_t)gy * W + gx;
+            ok = t_pend[g] == 0;
+            v = __ldcg(stone + g);
+        }
+        s_hok[h] = ok;
+        s_hval[h] = v;
+    }
+    if (threadIdx.x == 0) s_done = 0;
+    __syncthreads();
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
+    int done = 0;
+    bool src[4], outlet[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
+        int32_t pend = kBlocked;
+        uint8_t st = 0;
+        float v = 0.f;
+        outlet[q] = false;
+        if (s_cls[hc] == kCellIn) {
+            const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
+            pend = 0;
+#pragma unroll
+            for (int d = 0; d < 8; ++d) {
+                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+                if (!donates(s_code[nh], d)) continue;
+                const uint8_t cl = s_cls[nh];
+                if (cl == kCellBlock)
+                    pend |= kBlocked;
+                else if (cl == kCellIn) {
+                    if (in_tile(lx + dir_dx(d), ly + dir_dy(d)))
+                        ++pend;
+                    else if (!s_hok[nh])
+                        pend |= kBlocked;
+                }
+            }
+            const int d = bit_dir(s_code[hc]);
+            if (d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn &&
+                !in_tile(lx + dir_dx(d), ly + dir_dy(d))) {
+                outlet[q] = true;
+                if (t_stat[g] == 2 && t_pend[g] == 0) ++done;
+            }
+            st = t_stat[g];
+            v = __ldcg(stone + g);
+        }
+        s_pend[l] = pend;
+        s_stat[l] = st;
+        s_new[l] = v;
+        src[q] = pend == 0;
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        int cur = src[q] ? (ly0 + 8 * q) * kTile + lx : -1;
+        for (int guard = 0; cur >= 0 && guard < kTile * kTile; ++guard) {
+            const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
+            const int d = bit_dir(s_code[hc]);
+            const int rlx = cx + (d >= 0 ? dir_dx(d) : 0), rly = cy + (d >= 0 ? dir_dy(d) : 0);
+            const bool rin = d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn;
+            if (rin && !in_tile(rlx, rly)) break;  // an outlet: the coarse wave stored it
+            if (s_stat[cur] == 2) {
+                float from = 0.f;
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk) {
+                    const int dd = scan_dir(kk);
+                    const int nlx = cx + dir_dx(dd), nly = cy + dir_dy(dd);
+                    const int nh = hc + dir_dy(dd) * kTH + dir_dx(dd);
+                    if (!donates(s_code[nh], dd) || s_cls[nh] != kCellIn) continue;
+                    from = __fadd_rn(from, __fmul_rn(1.0f, in_tile(nlx, nly) ? s_new[nly * kTile + nlx] : s_hval[nh]));
+                }
+                const SedInit in = sed_init(s_code, s_cls, cx, cy, tx0, ty0, W, ero, inci, geli, soilT, stone, k);
+                const float sn = in.L.nz ? sed_mix(in.L.A, in.L.B, from) : s_new[cur];
+                s_new[cur] = sn;
+                sed_store((size_t)(ty0 + cy) * W + tx0 + cx, in.L, sn, depo, stone, fines, soilT);
+                ++done;
+            }
+            __threadfence_block();
+            int nxt = -1;
+            if (rin) {
+                const int r = rly * kTile + rlx;
+                if (atomicSub(&s_pend[r], 1) == 1) {
+                    __threadfence_block();
+                    nxt = r;
+                }
+            }
+            cur = nxt;
+        }
+    }
+    done = wsum(done);
+    if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_done) atomicAdd(&sc->sed_done, s_done);
 }
 
 __device__ __forceinline__ float dreybrodt(const float* tab, float T) {
@@ -451,9 +1118,11 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-__global__ void k_mod_reset(DevScalars* sc) {
+__global__ void k_mod_reset(DevScalars* sc, int tiled) {
     sc->counters[0] = 0;
     sc->sed_done = 0;
+    sc->sed_tiled_ok = tiled;
+    sc->tile_src = 0;
     sc->tot_e = sc->tot_i = sc->tot_g = sc->tot_d = sc->tot_wc = sc->tot_wp = sc->tot_bio = 0.0;
     sc->fa_max_key = 0ull;
 }
@@ -466,14 +1135,47 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, const Climate
     const int T = 256;
     size_t nb = (N + T - 1) / T;
     const int blocks = (int)(nb > 152 * 32 ? 152 * 32 : nb);
-    LEM_LAUNCH(L, k_mod_reset, 1, 1, s.sc);
+    const float* prop = (k.flow_type != 0 && k.mfd_props) ? s.prop : nullptr;
+    const int tiled = (k.flow_type == 0 && !prop) ? 1 : 0;
+    LEM_LAUNCH(L, k_mod_reset, 1, 1, s.sc, tiled);
     LEM_LAUNCH(L, k_erosion, blocks, T, s.z, s.z_init, s.mask, s.slopes, s.fa, s.fines, s.nut, s.soilT, s.stone,
                s.totB, s.slopeptr, s.ero, s.inci, s.geli, k, c, s.sc);
     LEM_LAUNCH(L, k_sed_prep, blocks, T, s.mask, s.fd, s.depo, s.pending, s.list_a, k, s.sc);
+    if (tiled) {
+        const int tiles = ((k.W + kTile - 1) / kTile) * ((k.H + kTile - 1) / kTile);
+        LEM_LAUNCH(L, k_sedt_local, tiles, 256, s.mask, s.fd, s.ero, s.inci, s.geli, s.depo, s.stone, s.fines,
+                   s.soilT, s.t_dst, s.t_pend, s.t_orng, s.t_la, s.p_abc, s.p_ref, s.p_map, s.t_stat, s.list_b, k,
+                   s.sc);
+        const uint8_t* fd = s.fd;
+        const int32_t* torng = s.t_orng;
+        const int32_t* tdst = s.t_dst;
+        const float2* tout = s.t_la;
+        const float4* pabc = s.p_abc;
+        const int32_t* pref = s.p_ref;
+        const float4* pmap = s.p_map;
+        float* pval = s.p_val;
+        float* depo = s.depo;
+        float* stone = s.stone;
+        float* fines = s.fines;
+        float* soilT = s.soilT;
+        int32_t* tpend = s.t_pend;
+        int32_t* la = s.list_b;  // the outlets k_sedt_local found ready
+        int32_t* lb = s.list_a;
+        ModelConsts kk = k;
+        DevScalars* sc = s.sc;
+        void* args[] = {(void*)&fd,    (void*)&torng, (void*)&tdst,  (void*)&tout, (void*)&pabc, (void*)&pref,
+                        (void*)&pmap,  (void*)&pval,  (void*)&depo,  (void*)&stone, (void*)&fines, (void*)&soilT, (void*)&tpend,
+                        (void*)&la,    (void*)&lb,    (void*)&kk,    (void*)&sc};
+        L.pre("k_sedt_coarse");
+        LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sedt_coarse, dim3(s.max_coop_blocks), dim3(256),
+                                                 args, 0, L.st));
+        L.post();
+        LEM_LAUNCH(L, k_sedt_final, tiles, 256, s.mask, s.fd, s.ero, s.inci, s.geli, s.depo, s.stone, s.fines,
+                   s.soilT, s.t_pend, s.t_stat, k, s.sc);
+    }
     {
         const uint8_t* mask = s.mask;
         const uint8_t* fd = s.fd;
-        const float* prop = (k.flow_type != 0 && k.mfd_props) ? s.prop : nullptr;
         const float* ero = s.ero;
         const float* inci = s.inci;
         const float* geli = s.geli;
@@ -486,9 +1188,10 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, const Climate
         int32_t* lb = s.list_b;
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
+        int gate = tiled;
         void* args[] = {(void*)&mask, (void*)&fd,    (void*)&prop,  (void*)&ero,     (void*)&inci,
                         (void*)&geli, (void*)&depo,  (void*)&stone, (void*)&fines,   (void*)&soilT,
-                        (void*)&pending, (void*)&la, (void*)&lb,    (void*)&kk,      (void*)&sc};
+                        (void*)&pending, (void*)&la, (void*)&lb,    (void*)&kk,      (void*)&sc, (void*)&gate};
         L.pre("k_sed_walk");
         LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sed_walk, dim3(s.max_coop_blocks), dim3(256), args,
                                                  0, L.st));
@@ -502,7 +1205,7 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, const Climate
     return LEM_OK;
 }
 
-const void* mod_coop_kernels[] = {(const void*)k_sed_walk};
-extern const int mod_coop_kernel_count = 1;
+const void* mod_coop_kernels[] = {(const void*)k_sed_walk, (const void*)k_sedt_coarse};
+extern const int mod_coop_kernel_count = 2;
 
 }  // namespace lem

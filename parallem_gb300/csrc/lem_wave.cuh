@@ -169,6 +169,27 @@ __device__ int wave_walk(const Op& op, int32_t* pending, int32_t* list_a, int32_
     return done;
 }
 
+// ---------------------------------------------------------------------------
+// 32x32 tiles of the two waves: cell classes of the halo, the kind of a cell's
+// receiver, and the halo ring in a fixed order.
+constexpr int kTH = kTile + 2;  // tile with its one-cell halo
+constexpr uint8_t kKindIn = 0, kKindOutlet = 1, kKindEnd = 2;  // receiver: in the tile / in another tile / none
+constexpr uint8_t kCellOff = 0;    // never a donor (outside the grid; for accumulation also nodata outside the catchment)
+constexpr uint8_t kCellIn = 1;     // a cell the wave computes
+constexpr uint8_t kCellBlock = 2;  // a donor that never completes
+
+__device__ __forceinline__ bool in_tile(int lx, int ly) { return lx >= 0 && lx < kTile && ly >= 0 && ly < kTile; }
+
+// The halo ring in a fixed order: top row, bottom row, left column, right column.
+constexpr int kRing = 4 * kTH - 4;
+constexpr int kRingChunks = (kRing + 31) / 32;
+__device__ __forceinline__ int ring_halo(int i) {
+    if (i < kTH) return i;
+    if (i < 2 * kTH) return (kTH - 1) * kTH + (i - kTH);
+    if (i < 2 * kTH + kTile) return (i - 2 * kTH + 1) * kTH;
+    return (i - 2 * kTH - kTile + 1) * kTH + kTH - 1;
+}
+
 // Receivers of cell (x, y) by its direction code: in-grid, in-catchment cells.
 __device__ __forceinline__ int code_receivers(const uint8_t* __restrict__ fd, const uint8_t* __restrict__ mask,
                                               int32_t cur, int x, int y, int W, int H, int32_t* r) {
