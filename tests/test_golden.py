@@ -1,0 +1,150 @@
+"""The oracle and the CUDA path against golden vectors of the reference's own kernels.
+
+tests/golden/*.npz were written by tests/golden/make_golden.py, which runs the
+reference's kernel bodies (compiled for the CPU from the reference sources by
+oracle/ref_build.py) for one timestep on small seeded grids.  These tests need
+no reference sources, so they pin parity wherever the repository runs:
+
+* the oracle, stage by stage from the reference's own stage inputs: direction
+  codes identical except at plateau ties (both answers attain the cell's
+  plateau distance), distances, sink counts, raised DEM and basin partition
+  identical on grids without flats; accumulation and the process stage
+  bit-identical;
+* the CUDA path (gpu): one whole step from the golden inputs, with the
+  tolerances of the GPU parity tests (codes and counts exact, accumulation
+  1e-5 relative, process grids 1e-5 relative + 1e-6 of the field's maximum,
+  DEM 1e-9 relative + 1e-6 m).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+NAMES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz")))
+DX = [0, 1, 1, 1, 0, -1, -1, -1]
+DY = [-1, -1, 0, 1, 1, 1, 0, -1]
+CODE = [64, 128, 1, 2, 4, 8, 16, 32]
+SOIL = ("stone", "fines", "soilT", "soilM", "soilB", "nut", "totB")
+MOD = ("slopeptr", "ero", "inci", "geli", "depo", "stone", "fines", "soilT", "soilM", "soilB", "nut", "totB")
+TOTALS = ("totE", "totI", "totG", "totD", "totWC", "totWP", "totbio")
+
+
+def load(name):
+    with np.load(os.path.join(HERE, name + ".npz")) as f:
+        return {k: f[k] for k in f.files}
+
+
+def strict(name):
+    return "plateaus" not in name  # no flat in the input DEM: pass-1 basins cannot depend on a tie
+
+
+def state_of(g):
+    st = {f: g["in_" + f] for f in SOIL}
+    st["mask"] = g["in_mask"]
+    st["outlet"] = int(g["in_outlet"])
+    return st
+
+
+def points_to_tie(zr, sp, y, x, code):
+    if code not in CODE:
+        return False
+    d = CODE.index(code)
+    ny, nx = y + DY[d], x + DX[d]
+    dc = np.float32(1.0 if d % 2 == 0 else 1.41)
+    return zr[ny, nx] == zr[y, x] and np.float32(sp[ny, nx] + dc) == sp[y, x]
+
+
+def test_golden_files_present():
+    assert len(NAMES) >= 4
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_golden(name):
+    from oracle import oracle
+    oracle.build()
+    g = load(name)
+    params = oracle.make_params(flow_direction_type=int(g["flow_direction_type"]),
+                                mfd_proportions=int(g["mfd_proportions"]))
+    o = oracle.OracleModel(g["in_dem"], 30.0, state_of(g), float(g["init_rain"]), float(g["init_temp"]),
+                           params=params)
+    if "rain" in g:
+        o.s.last_rain, o.s.last_temp = o.s.rain, o.s.temp
+        o.s.rain, o.s.temp = float(g["rain"]), float(g["temp"])
+        oracle.lib().oracle_set_climate(oracle.C.byref(o.s), 0)
+    o.flow_direction()
+    assert o.s.init_sinks == int(g["fd_init_sinks"]) and o.s.init_flats == int(g["fd_init_flats"])
+    mask = g["in_mask"] == 1
+    same_spill = np.array_equal(o["dem_routed"], g["fd_dem_routed"])
+    if strict(name):
+        assert same_spill  # no plateau in the input: no tie can change a spill
+    if same_spill:
+        # plateau distances are the unique least fixpoint; codes may differ only at ties
+        np.testing.assert_array_equal(o["shortest_paths"], g["fd_shortest_paths"])
+        np.testing.assert_array_equal(o["dem"], g["fd_dem"])
+        assert o.s.sinkcount == int(g["fd_sinkcount"]) and o.outlet == int(g["fd_outlet"])
+        pairs = set(zip(o["watershed"][mask].tolist(), g["fd_watershed"][mask].tolist()))
+        assert len(pairs) == len(set(g["fd_watershed"][mask].tolist()))
+        for y, x in np.argwhere(o["sfd"] != g["fd_sfd"]):
+            assert points_to_tie(o["dem_routed"], o["shortest_paths"], y, x, int(g["fd_sfd"][y, x]))
+            assert points_to_tie(o["dem_routed"], o["shortest_paths"], y, x, int(o["sfd"][y, x]))
+        ds = o["slopes"] != g["fd_slopes"]
+        assert np.all((o["slopes"][ds] == 0.0001) | (g["fd_slopes"][ds] == 0.0001))
+    # the rest of the step from the reference's own stage inputs: bit-identical
+    for f in ("fd", "sfd", "slopes", "dem"):
+        o[f][...] = g["fd_" + f]
+    o.s.outlet = int(g["fd_outlet"])
+    o.flow_accumulation()
+    for f in ("runoff", "soilM", "fa", "prop"):
+        np.testing.assert_array_equal(o[f], g["fa_" + f], err_msg=f)
+    assert o.s.FA_max == float(g["fa_FA_max"]) and o.s.fa_uncomputed == int(g["fa_fa_uncomputed"])
+    o.erosion()
+    for f in MOD + ("dz", "wC", "wP", "dem"):
+        np.testing.assert_array_equal(o[f], g["mod_" + f], err_msg=f)
+    for k in TOTALS:
+        a, b = getattr(o.s, k), float(g["mod_" + k])
+        assert a == b or (np.isnan(a) and np.isnan(b)), k
+    assert o.outlet == int(g["mod_outlet"]) and o.s.sed_uncomputed == int(g["mod_sed_uncomputed"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_matches_golden(name):
+    from parallem_gb300 import build, lem
+    from tests.test_gpu_parity import close
+    build.build()
+    g = load(name)
+    kw = dict(flow_direction_type=int(g["flow_direction_type"]), mfd_proportions=int(g["mfd_proportions"]))
+    m = lem.Model(g["in_dem"], 30.0, float(g["init_rain"]), float(g["init_temp"]), params=lem.make_params(**kw))
+    m.set_state(state_of(g))
+    mask = g["in_mask"] == 1
+    if "rain" in g:
+        m.step(float(g["rain"]), float(g["temp"]), True)
+    else:
+        m.step(float(g["init_rain"]), float(g["init_temp"]), False)
+    sfd = m.get("sfd")
+    t = m.totals()
+    assert t["initial_sinks"] == int(g["fd_init_sinks"]) and t["initial_flats"] == int(g["fd_init_flats"])
+    if not np.array_equal(sfd, g["fd_sfd"]):
+        # a plateau tie the reference's thread schedule broke the other way:
+        # the later stages are compared from identical inputs in the oracle tests
+        same_spill = np.array_equal(m.get("dem_routed"), g["fd_dem_routed"])
+        if same_spill:
+            for y, x in np.argwhere(sfd != g["fd_sfd"]):
+                assert points_to_tie(g["fd_dem_routed"], g["fd_shortest_paths"], y, x, int(sfd[y, x]))
+        assert not strict(name) or same_spill
+        m.close()
+        pytest.skip("tie broken the other way; codes checked as ties")
+    np.testing.assert_array_equal(m.get("fd"), g["fd_fd"])
+    assert t["sinkcount"] == int(g["fd_sinkcount"]) and t["outlet"] == int(g["mod_outlet"])
+    close("fa", m.get("fa"), g["fa_fa"], mask, rtol=1e-5, afrac=0.0)
+    close("runoff", m.get("runoff"), g["fa_runoff"], mask, rtol=1e-6)
+    for f in MOD:
+        close(f, m.get(f), g["mod_" + f], mask, afrac=1e-6)
+    close("dem", m.get("dem"), g["mod_dem"], mask, rtol=1e-9, afrac=0.0, atol=1e-6)
+    for k, gk in (("tot_e", "totE"), ("tot_i", "totI"), ("tot_g", "totG"), ("tot_d", "totD"),
+                  ("tot_weather_c", "totWC"), ("tot_weather_p", "totWP"), ("tot_bio", "totbio")):
+        a, b = t[k], float(g["mod_" + gk])
+        assert (np.isnan(a) and np.isnan(b)) or abs(a - b) <= 1e-5 * abs(b) + 1e-12, k
+    m.close()
