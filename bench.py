@@ -1,20 +1,27 @@
 """Benchmark of the GB300 landscape-evolution step (prints one JSON line).
 
-Workload: the single-large-grid configuration -- a 4096x4096 fp32 spectral DEM
-(Hurst 0.7, relief 0-1500 m, 30 m cells, 2% nodata border, 5000 pits, 300
-plateaus) driven by a per-step climate series (rain lognormal mean 900 cv 0.3,
-temperature N(9, 2)).  A "step" is one model timestep of the hot path: flow
-direction with plateau routing and sink flooding, runoff and flow
-accumulation, erosion, sediment routing and the surface/soil/vegetation update.
+Workloads (--workload):
+* ensemble (default): the batched ensemble -- 64 square fp32 spectral DEMs with
+  sides log-uniform in [256, 2048] (Hurst U(0.6, 0.9), relief U(200, 2000) m,
+  30 m cells, 1-5 % nodata border, pits and plateaus at the density of the
+  4096x4096 grid), each with its own climate series, packed into one canvas
+  and stepped together (lem_step_batch: one launch per kernel for all DEMs).
+  The plain path on the same DEMs (one grid at a time) is timed beside it on
+  a sample of the DEMs and reported as `plain`;
+* grid: the single large grid -- 4096x4096 (Hurst 0.7, relief 0-1500 m, 2 %
+  nodata, 5000 pits, 300 plateaus), one DEM per handle.
+A "step" is one model timestep of the hot path for every DEM: flow direction
+with plateau routing and sink flooding, runoff and flow accumulation, erosion,
+sediment routing and the surface/soil/vegetation update.
 
 * value: cell-timesteps/s (masked-in cells x steps / s) with the state resident
   on the device, timed with CUDA events on the library's stream;
 * e2e: the same metric through the public C ABI with the host side of the
-  reference driver: each step uploads its climate and reads back the budget
-  row, and every 50th/100th step downloads the grids lem.cpp writes then
-  (writegrids, MEM_kernels/io.cpp:201-230);
+  reference driver: each step uploads every DEM's climate and reads back its
+  budget row, and every 50th/100th step downloads the grids lem.cpp writes
+  then (writegrids, MEM_kernels/io.cpp:201-230);
 * roofline: the dominant kernel's algorithmic bytes / its event-timed duration
-  against the measured HBM copy bandwidth;
+  against the measured HBM copy bandwidth, and the step-level figure;
 * cpu_baseline: the FP64 oracle on the host cores on a bounded sample.
 
 Multi-GPU (torchrun): every rank runs an independent replica (the path does
@@ -157,14 +164,14 @@ def barrier(dist):
         dist.barrier()
 
 
-def cpu_sample(scenario_mod, seconds=12.0, n=1024, max_steps=8):
-    """The FP64 oracle on a bounded sample: one 1024x1024 window of the workload
-    (same generator, Hurst, relief and border) stepped until `seconds` pass."""
+def cpu_sample(sc, seconds=12.0, max_steps=8, label=""):
+    """The FP64 oracle on a bounded sample of the workload: one DEM of it stepped
+    until `seconds` pass."""
+    from parallem_gb300 import scenario as S
     from oracle import oracle
     oracle.build()
     threads = oracle.num_threads()
-    sc = scenario_mod.config_large(2, n=n, steps=max_steps)
-    st = scenario_mod.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+    st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
     m = oracle.OracleModel(sc.dem, 30.0, st, sc.init_rain, sc.init_temp, diagnostics=False)
     cells = int((st["mask"] == 1).sum())
     t0 = time.perf_counter()
@@ -175,57 +182,219 @@ def cpu_sample(scenario_mod, seconds=12.0, n=1024, max_steps=8):
         if time.perf_counter() - t0 > seconds:
             break
     dt = time.perf_counter() - t0
+    n = sc.dem.shape[0]
     return {"value": cells * steps / dt, "unit": "cell-timesteps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} timesteps of a {n}x{n} grid from the same generator ({cells} active cells), "
+            "sample": f"{steps} timesteps of {label}a {n}x{n} DEM of the workload ({cells} active cells), "
                       f"FP64 oracle, {threads} OpenMP threads, {dt:.1f} s"}
+
+
+def sample_scenario(args):
+    """The DEM the host-core samples run on: for the ensemble its largest DEM
+    below 1024x1024, for the single grid a 1024x1024 grid of the same generator."""
+    from parallem_gb300 import scenario as S
+    if args.workload == "ensemble":
+        ens = S.config_ensemble(count=args.dems, steps=8)
+        small = [x for x in ens if x.dem.shape[0] <= 1024]
+        return max(small or ens, key=lambda x: x.dem.size)
+    return S.config_large(2, n=1024, steps=8)
 
 
 def run_reference(args):
     """The reference's algorithm on the host cores (the oracle port: the reference
     itself is CUDA and has no CPU implementation; its kernels compile on the CPU
-    only where its sources are present)."""
+    only where its sources are present), on a bounded sample of the workload."""
     rank, world, local = dist_env()
     if rank != 0:
         return 0
     from parallem_gb300 import scenario as S
-    n = args.ref_grid
     from oracle import oracle
     oracle.build()
     threads = oracle.num_threads()
-    sc = S.config_large(2, n=n, steps=args.warmup + args.steps)
+    sc = sample_scenario(args)
     st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
     m = oracle.OracleModel(sc.dem, 30.0, st, sc.init_rain, sc.init_temp, diagnostics=False)
     cells = int((st["mask"] == 1).sum())
+    n = sc.dem.shape[0]
+    rain = list(sc.rain) * (1 + (args.warmup + args.steps) // len(sc.rain))
+    temp = list(sc.temp) * (1 + (args.warmup + args.steps) // len(sc.temp))
     for i in range(args.warmup):
-        m.step(sc.rain[i], sc.temp[i], True)
+        m.step(rain[i], temp[i], True)
     t0 = time.perf_counter()
     for i in range(args.warmup, args.warmup + args.steps):
-        m.step(sc.rain[i], sc.temp[i], True)
+        m.step(rain[i], temp[i], True)
     dt = time.perf_counter() - t0
     value = cells * args.steps / dt
     line = {
         "impl": "reference", "metric": "cell-timesteps/s", "value": value, "unit": "cell-timesteps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"single large grid, sampled at {n}x{n} on the host", "grid": n,
-                   "cellsize_m": 30, "climate": "per-step series"},
+        "config": {"workload": workload_name(args) + f", sampled on the host as one {n}x{n} DEM",
+                   "sample_dem": n, "cellsize_m": 30, "climate": "per-step series"},
         "cpu_baseline": {"value": value, "unit": "cell-timesteps/s", "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} timesteps of a {n}x{n} grid ({cells} active cells)"},
+                         "sample": f"{args.steps} timesteps of one {n}x{n} DEM of the workload ({cells} active cells)"},
         "e2e": {"value": value, "unit": "cell-timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
 
 
+def workload_name(args):
+    if args.workload == "ensemble":
+        return f"batched ensemble of {args.dems} DEMs, sides log-uniform in [256, 2048], per-DEM climate series"
+    return f"single large grid {args.grid}x{args.grid}, per-step climate series"
+
+
+class GridWork:
+    """One large grid on one handle (the plain path)."""
+
+    def __init__(self, lem, S, args, rank, total_steps):
+        self.sc = S.config_large(2 + rank, n=args.grid, steps=total_steps)
+        st = S.initial_state(self.sc.dem, 30.0, self.sc.init_rain, self.sc.init_temp)
+        self.cells = int((st["mask"] == 1).sum())
+        self.g = lem.Model(self.sc.dem, 30.0, self.sc.init_rain, self.sc.init_temp)
+        self.g.set_state(st)
+        self.lem = lem
+
+    def step(self, i):
+        self.g.step(self.sc.rain[i], self.sc.temp[i], True)
+
+    def e2e_step(self, i, j):
+        import ctypes as C
+        lem = self.lem
+        L = lem.load()
+        clim = lem.Climate(float(self.sc.rain[i]), float(self.sc.temp[i]), 1)
+        lem._check(L.lem_step(self.g.h, C.byref(clim), 0), "lem_step")
+        tot = lem.Totals()
+        lem._check(L.lem_get_totals(self.g.h, C.byref(tot)), "lem_get_totals")  # the budget row of the step
+        h2d, d2h = C.sizeof(clim), C.sizeof(tot)
+        if j % 50 == 0:  # writegrids: fd, fa, dem every 50 steps; erosion grids every 100
+            for f in ("fd", "fa", "dem"):
+                d2h += self.g.get(f).nbytes
+        if j % 100 == 0:
+            for f in ("ero", "inci", "geli", "depo"):
+                d2h += self.g.get(f).nbytes
+        return h2d, d2h
+
+    def config(self, args):
+        return {"workload": workload_name(args), "grid": args.grid, "active_cells": self.cells, "cellsize_m": 30,
+                "hurst": 0.7, "relief_m": 1500, "nodata": 0.02, "pits": 5000 if args.grid == 4096 else "scaled",
+                "plateaus": 300, "l2": "resident state ~5 GB, larger than L2 (no flush needed)"}
+
+    def close(self):
+        self.g.close()
+
+
+class EnsembleWork:
+    """The batched ensemble: every DEM in one canvas, one lem_step_batch per step."""
+
+    def __init__(self, lem, S, args, rank, total_steps):
+        from parallem_gb300.packing import TilePacker
+        self.lem = lem
+        self.ens = S.config_ensemble(4 + rank, count=args.dems, steps=max(total_steps, 8))
+        order = sorted(range(len(self.ens)), key=lambda i: -self.ens[i].dem.size)
+        W = args.canvas
+        H = 1024
+        while True:  # the smallest canvas height that holds every DEM (largest first)
+            p = TilePacker(W, H)
+            if all(p.alloc(self.ens[i].dem.shape[1], self.ens[i].dem.shape[0]) is not None for i in order):
+                break
+            H += 512
+        self.canvas = (W, H)
+        self.b = lem.Batch(W, H, 30.0, max_dems=len(self.ens))
+        self.ids = [None] * len(self.ens)
+        self.cells = 0
+        for i in order:
+            sc = self.ens[i]
+            st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+            k = self.b.add(sc.dem, sc.init_rain, sc.init_temp)
+            self.b.set_state(k, st)
+            self.ids[i] = k
+            self.cells += int((st["mask"] == 1).sum())
+        self.g = self.b  # timing, profiling and launch counts of the batch handle
+
+    def step(self, i):
+        for sc, k in zip(self.ens, self.ids):
+            self.b.set_climate(k, float(sc.rain[i]), float(sc.temp[i]), True)
+        self.b.step()
+
+    def e2e_step(self, i, j):
+        import ctypes as C
+        lem = self.lem
+        L = lem.load()
+        h2d = d2h = 0
+        for sc, k in zip(self.ens, self.ids):
+            clim = lem.Climate(float(sc.rain[i]), float(sc.temp[i]), 1)
+            lem._check(L.lem_dem_set_climate(self.b.h, k, C.byref(clim)), "lem_dem_set_climate")
+            h2d += C.sizeof(clim)
+        lem._check(L.lem_step_batch(self.b.h, 0), "lem_step_batch")
+        tot = lem.Totals()
+        for k in self.ids:
+            lem._check(L.lem_dem_get_totals(self.b.h, k, C.byref(tot)), "lem_dem_get_totals")
+            d2h += C.sizeof(tot)
+        if j % 50 == 0:
+            for k in self.ids:
+                for f in ("fd", "fa", "dem"):
+                    d2h += self.b.get(k, f).nbytes
+        if j % 100 == 0:
+            for k in self.ids:
+                for f in ("ero", "inci", "geli", "depo"):
+                    d2h += self.b.get(k, f).nbytes
+        return h2d, d2h
+
+    def plain_sample(self, args, steps=3, budget_s=20.0):
+        """The plain path on the same DEMs, one handle and one grid at a time:
+        every fourth DEM by size (all sizes covered), `steps` timed steps each."""
+        lem = self.lem
+        from parallem_gb300 import scenario as S
+        order = sorted(range(len(self.ens)), key=lambda i: self.ens[i].dem.size)
+        pick = order[::4]
+        cells = 0
+        secs = 0.0
+        t_start = time.perf_counter()
+        done = 0
+        for i in pick:
+            sc = self.ens[i]
+            st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+            m = lem.Model(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+            m.set_state(st)
+            m.step(sc.rain[0], sc.temp[0], True)
+            m.synchronize()
+            m.record(0)
+            for s in range(1, 1 + steps):
+                m.step(sc.rain[s], sc.temp[s], True)
+            m.record(1)
+            secs += m.elapsed_ms(0, 1) / 1e3
+            cells += int((st["mask"] == 1).sum()) * steps
+            m.close()
+            done += 1
+            if time.perf_counter() - t_start > budget_s:
+                break
+        return {"value": cells / secs, "unit": "cell-timesteps/s",
+                "sample": f"{done} of the {len(self.ens)} DEMs (every fourth by size), each on its own handle, "
+                          f"{steps} device-timed steps each"}
+
+    def config(self, args):
+        sides = sorted(x.dem.shape[0] for x in self.ens)
+        return {"workload": workload_name(args), "dems": len(self.ens), "active_cells": self.cells,
+                "canvas": f"{self.canvas[0]}x{self.canvas[1]}", "sides": [sides[0], sides[len(sides) // 2], sides[-1]],
+                "cellsize_m": 30, "l2": "resident state ~20 GB, larger than L2 (no flush needed)"}
+
+    def close(self):
+        self.b.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--grid", type=int, default=4096)
-    ap.add_argument("--ref-grid", type=int, default=512)
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "grid"])
+    ap.add_argument("--grid", type=int, default=4096, help="side of the single grid")
+    ap.add_argument("--dems", type=int, default=64, help="DEMs of the ensemble")
+    ap.add_argument("--canvas", type=int, default=8192, help="width of the ensemble's canvas")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-path sample of the ensemble")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -241,15 +410,13 @@ def main():
     barrier(dist)
     lem.select_device(local)
     total_steps = args.warmup + 2 * args.steps
-    sc = S.config_large(2 + rank, n=args.grid, steps=total_steps)
-    st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
-    cells = int((st["mask"] == 1).sum())
-    g = lem.Model(sc.dem, 30.0, sc.init_rain, sc.init_temp)
-    g.set_state(st)
+    work = (EnsembleWork if args.workload == "ensemble" else GridWork)(lem, S, args, rank, total_steps)
+    g = work.g
+    cells = work.cells
 
     # warm-up steps (untimed)
     for i in range(args.warmup):
-        g.step(sc.rain[i], sc.temp[i], True)
+        work.step(i)
     g.synchronize()
     barrier(dist)
 
@@ -259,7 +426,7 @@ def main():
     with ClockSampler(local) as clk:
         g.record(0)
         for i in range(args.warmup, args.warmup + args.steps):
-            g.step(sc.rain[i], sc.temp[i], True)
+            work.step(i)
         g.record(1)
         ms = g.elapsed_ms(0, 1)
     prof = g.profile()
@@ -273,28 +440,17 @@ def main():
     # timed region 2: end to end through the C ABI with host buffers
     barrier(dist)
     h2d = d2h = 0
-    import ctypes as C
-    tot = lem.Totals()
-    L = lem.load()
     t0 = time.perf_counter()
     for j, i in enumerate(range(args.warmup + args.steps, args.warmup + 2 * args.steps)):
-        clim = lem.Climate(float(sc.rain[i]), float(sc.temp[i]), 1)
-        lem._check(L.lem_step(g.h, C.byref(clim), 0), "lem_step")
-        h2d += C.sizeof(clim)
-        lem._check(L.lem_get_totals(g.h, C.byref(tot)), "lem_get_totals")  # the budget row of the step
-        d2h += C.sizeof(tot)
-        if j % 50 == 0:  # writegrids: fd, fa, dem every 50 steps; erosion grids every 100
-            for f in ("fd", "fa", "dem"):
-                d2h += g.get(f).nbytes
-        if j % 100 == 0:
-            for f in ("ero", "inci", "geli", "depo"):
-                d2h += g.get(f).nbytes
+        a, b = work.e2e_step(i, j)
+        h2d += a
+        d2h += b
     g.synchronize()
     e2e_s = reduce_max(dist, time.perf_counter() - t0)
     e2e = cells_all * args.steps / e2e_s
 
     if rank != 0:
-        g.close()
+        work.close()
         if dist is not None:
             dist.destroy_process_group()
         return 0
@@ -308,7 +464,7 @@ def main():
     tfile = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
     if os.path.exists(tfile):
         try:
-            traffic = json.load(open(tfile)).get(kname)
+            traffic = json.load(open(tfile)).get(args.workload, {}).get(kname)
         except Exception:
             traffic = None
     bytes_source = "algorithmic"
@@ -317,18 +473,19 @@ def main():
         kbytes_per_launch = traffic
         bytes_source = "ncu dram bytes per launch (data-dependent kernel)"
     achieved = kbytes_per_launch / (kms / klaunches / 1e3) / 1e9 if kms > 0 else 0.0
-    cpu = None if args.no_cpu else cpu_sample(S)
+    plain = None
+    if args.workload == "ensemble" and not args.no_plain:
+        plain = work.plain_sample(args)
+    cpu = None if args.no_cpu else cpu_sample(sample_scenario(args))
     step_ms = ms_max / args.steps
+    config = work.config(args)
+    config["parallelism"] = f"replicas x{world}"
     line = {
         "metric": "cell-timesteps/s", "value": value, "unit": "cell-timesteps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded spectral DEM and climate series)",
-        "config": {"workload": f"single large grid {args.grid}x{args.grid}, per-step climate series",
-                   "grid": args.grid, "active_cells": cells, "cellsize_m": 30, "hurst": 0.7, "relief_m": 1500,
-                   "nodata": 0.02, "pits": 5000 if args.grid == 4096 else "scaled", "plateaus": 300,
-                   "parallelism": f"replicas x{world}",
-                   "l2": "resident state ~1.6 GB per replica, larger than L2 (no flush needed)"},
+        "data": "synthetic (seeded spectral DEMs and climate series)",
+        "config": config,
         "e2e": {"value": e2e, "unit": "cell-timesteps/s", "h2d_bytes_per_step": h2d / args.steps,
                 "d2h_bytes_per_step": d2h / args.steps},
         "gpu_launches": launches,
@@ -344,8 +501,11 @@ def main():
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
     }
+    if plain is not None:
+        line["plain"] = plain
+        line["batched_over_plain"] = value / plain["value"]
     print(json.dumps(line))
-    g.close()
+    work.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0

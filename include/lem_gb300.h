@@ -209,6 +209,35 @@ uint64_t lem_launch_count(lem_handle* h);
 
 const char* lem_status_string(lem_status s);
 
+/* ---- Batches: many DEMs of uneven sizes stepped together.
+ * No counterpart in the reference, which runs one grid per process
+ * (lem.cpp:67-97).  A batch handle owns one grid (the canvas); each DEM lives
+ * in its own region of it, placed by the caller at multiples of 32 cells, and
+ * must carry a nodata ring (all its border cells -9999), so no in-catchment
+ * cell of one DEM sees another.  One lem_step_batch runs the three stages of
+ * every active DEM with one launch per kernel; each DEM keeps its own outlet,
+ * climate and budget totals, and its grids equal those of the same DEM run
+ * alone.  Cell indices of a DEM (outlet, totals) are indices of the DEM's own
+ * grid.  The canvas width must be a multiple of 32; max_dems < 65535. */
+lem_status lem_create_batch(const lem_grid_desc* canvas, const lem_params* params, int32_t max_dems,
+                            lem_handle** out);
+/* Adds a DEM at (x0, y0) of the canvas (x0, y0 multiples of 32; the 32-rounded
+ * extents of two DEMs may not overlap).  Its other fields start at zero; set
+ * the soil state with lem_dem_set_field and the outlet with lem_dem_set_outlet
+ * before the next step.  LEM_ERR_CAPACITY: no free DEM slot. */
+lem_status lem_dem_add(lem_handle* h, int32_t x0, int32_t y0, int32_t width, int32_t height, const double* dem,
+                       double init_rain, double init_temp, int32_t* id);
+lem_status lem_dem_remove(lem_handle* h, int32_t id);       /* its region returns to nodata */
+lem_status lem_dem_set_field(lem_handle* h, int32_t id, lem_field f, const void* host);  /* width*height */
+lem_status lem_dem_get_field(lem_handle* h, int32_t id, lem_field f, void* host);
+lem_status lem_dem_set_outlet(lem_handle* h, int32_t id, int32_t cell);
+lem_status lem_dem_set_climate(lem_handle* h, int32_t id, const lem_climate* c);
+/* Flags for this DEM's next step only (LEM_STEP_SET_OUTLET_FROM_FA for its first). */
+lem_status lem_dem_set_step_flags(lem_handle* h, int32_t id, uint32_t flags);
+lem_status lem_dem_get_totals(lem_handle* h, int32_t id, lem_totals* out);  /* synchronous */
+/* One timestep of every active DEM; flags as lem_step, for all DEMs. */
+lem_status lem_step_batch(lem_handle* h, uint32_t flags);
+
 /* Flow accumulation that allocates nothing.  No counterpart in the reference:
  * it serves callers that must not allocate device memory themselves or through
  * this library -- e.g. a host program that hands the path only buffers from its

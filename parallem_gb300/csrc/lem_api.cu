@@ -69,20 +69,36 @@ lem_status cuda_fail(cudaError_t e, const char* what, const char* file, int line
 
 using namespace lem;
 
+// A DEM of the handle as the host tracks it: its region and its climate state.
+struct HostDem {
+    bool active = false;
+    int32_t x0 = 0, y0 = 0, w = 0, h = 0;
+    double rain = 0, temp = 0, rain0 = 0, temp0 = 0;
+    bool from_current = false;     // a recompute = 1 climate has been set
+    bool outlet_set = false;
+    uint32_t next_flags = 0;       // one-shot step flags of this DEM
+};
+
 struct lem_handle {
     DevState s{};
     ModelConsts k{};
-    ClimateNow c{};
     lem_params p{};
     cudaStream_t st = nullptr;
     int device = 0;
-    bool dem_set = false;
+    bool batch = false;            // several DEMs packed into the grid
+    bool dem_set = false;          // a single grid: its DEM was uploaded
     size_t N = 0;
     uint64_t launches = 0;
     std::vector<void*> allocs;
-    void* staging = nullptr;  // pinned host buffer of 8*N floats / doubles
+    std::vector<HostDem> dems;
+    DemIn* dem_in = nullptr;       // device copies
+    DemOut* dem_out = nullptr;
+    uint16_t* dem_of = nullptr;
+    int32_t* chunks = nullptr;
+    DemOut* host_out = nullptr;    // pinned mirror of dem_out
+    void* staging = nullptr;       // pinned host buffer for field conversions, grown on demand
     size_t staging_bytes = 0;
-    DevScalars* host_sc = nullptr;  // pinned mirror of the device scalars
+    DevScalars* host_sc = nullptr; // pinned mirror of the device scalars
     Profiler prof;
     bool profiling = false;
     cudaEvent_t events[16] = {};
@@ -156,7 +172,278 @@ float* float_field(lem_handle* h, lem_field f) {
 
 lem_status sync_scalars(lem_handle* h) {
     LEM_CUDA_TRY(cudaMemcpyAsync(h->host_sc, h->s.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->st));
+    LEM_CUDA_TRY(cudaMemcpyAsync(h->host_out, h->dem_out, sizeof(DemOut) * h->dems.size(), cudaMemcpyDeviceToHost,
+                                 h->st));
     LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    return LEM_OK;
+}
+
+lem_status ensure_staging(lem_handle* h, size_t bytes) {
+    if (bytes <= h->staging_bytes) return LEM_OK;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    if (h->staging) cudaFreeHost(h->staging);
+    h->staging = nullptr;
+    h->staging_bytes = 0;
+    if (cudaMallocHost(&h->staging, bytes) != cudaSuccess) return LEM_ERR_NOMEM;
+    h->staging_bytes = bytes;
+    return LEM_OK;
+}
+
+__global__ void k_fill_f64(double* p, size_t n, double v) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+__global__ void k_fill_u16(uint16_t* p, size_t n, uint16_t v) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// A DEM joins (id >= 0) or leaves (id < 0) its region of the grid.  Joining:
+// the DEM was uploaded into z; the mask follows it (createmask,
+// MEM_kernels/memory.cu:229-238), the initial climate grids take it as their
+// DEM, and every other field of the region starts at zero as in a new handle.
+// Leaving: the region returns to nodata outside every DEM.
+__global__ void k_region(DevState s, uint16_t* of, int W, int x0, int y0, int w, int h, int id) {
+    const size_t n = (size_t)w * h;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t g = (size_t)(y0 + i / w) * W + x0 + i % w;
+        if (id < 0) s.z[g] = kNoData;
+        if (of) of[g] = id < 0 ? kNoDem : (uint16_t)id;
+        const double zv = s.z[g];
+        s.z_init[g] = zv;
+        s.zf[g] = zv;
+        s.mask[g] = (id >= 0 && zv != kNoData) ? 1 : 0;
+        s.sfd[g] = s.mfd[g] = s.fd[g] = s.sfd1[g] = kMaskedCode;
+        for (int j = 0; j < 8; ++j) s.slopes[8 * g + j] = 0.f;
+        s.fa[g] = make_float2(0.f, 0.f);
+        s.w[g] = s.slopeptr[g] = 0.f;
+        s.stone[g] = s.fines[g] = s.soilT[g] = s.soilM[g] = s.soilB[g] = s.nut[g] = s.totB[g] = 0.f;
+        s.ero[g] = s.inci[g] = s.geli[g] = s.depo[g] = s.dz[g] = s.wc[g] = s.wp[g] = 0.f;
+        s.contrib[g] = 0;
+        s.ws[g] = 0;
+    }
+}
+
+lem_status region_op(lem_handle* h, const HostDem& r, int id) {
+    const size_t n = (size_t)r.w * r.h;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
+    k_region<<<blocks, 256, 0, h->st>>>(h->s, h->dem_of, h->k.W, r.x0, r.y0, r.w, r.h, id);
+    LEM_CUDA_TRY(cudaGetLastError());
+    return LEM_OK;
+}
+
+// Per-DEM inputs of the next stage (region, climate, flags) and the chunks of
+// the streaming passes.
+lem_status prepare(lem_handle* h) {
+    const int n = (int)h->dems.size();
+    std::vector<DemIn> in(n);
+    std::vector<int32_t> chunk(n + 1, 0);
+    bool any = false;
+    for (int d = 0; d < n; ++d) {
+        const HostDem& r = h->dems[d];
+        DemIn& o = in[d];
+        std::memset(&o, 0, sizeof o);
+        chunk[d + 1] = chunk[d];
+        if (!r.active) continue;
+        if (h->batch && !r.outlet_set) return LEM_ERR_STATE;
+        any = true;
+        o.x0 = r.x0;
+        o.y0 = r.y0;
+        o.w = r.w;
+        o.h = r.h;
+        o.active = 1;
+        o.from_current_dem = r.from_current ? 1 : 0;
+        o.outlet_from_fa = (r.next_flags & LEM_STEP_SET_OUTLET_FROM_FA) ? 1 : 0;
+        o.rain = r.rain;
+        o.temp = r.temp;
+        o.rain_inc = (r.rain * 2 - r.rain) / r.h;  // Data.cpp:246-249, rows of the DEM
+        o.rain0 = r.rain0;
+        o.temp0 = r.temp0;
+        o.rain0_inc = (r.rain0 * 2 - r.rain0) / r.h;
+        chunk[d + 1] += (int32_t)(((int64_t)r.w * r.h + kChunk - 1) / kChunk);
+    }
+    if (!any) return LEM_ERR_STATE;
+    // pageable sources: the copies take the data before returning
+    LEM_CUDA_TRY(cudaMemcpyAsync(h->dem_in, in.data(), sizeof(DemIn) * n, cudaMemcpyHostToDevice, h->st));
+    LEM_CUDA_TRY(cudaMemcpyAsync(h->chunks, chunk.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, h->st));
+    h->s.n_chunks = chunk[n];
+    return LEM_OK;
+}
+
+bool any_flag(const lem_handle* h, uint32_t f) {
+    for (const HostDem& r : h->dems)
+        if (r.active && (r.next_flags & f)) return true;
+    return false;
+}
+
+// ---- field transfers of one DEM region (the whole grid for a single DEM)
+
+lem_status set_region_field(lem_handle* h, const HostDem& r, lem_field f, const void* host) {
+    const size_t n = (size_t)r.w * r.h;
+    const size_t W = (size_t)h->k.W;
+    const size_t off = (size_t)r.y0 * W + r.x0;
+    DevState& s = h->s;
+    lem_status st;
+    if ((st = ensure_staging(h, n * 8 * sizeof(float))) != LEM_OK) return st;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    if (f == LEM_F_DEM) {
+        LEM_CUDA_TRY(cudaMemcpy2DAsync(s.z + off, W * 8, host, r.w * 8, r.w * 8, r.h, cudaMemcpyHostToDevice, h->st));
+    } else if (f == LEM_F_SLOPES) {
+        const double* src = static_cast<const double*>(host);
+        float* t = static_cast<float*>(h->staging);
+        for (size_t i = 0; i < 8 * n; ++i) t[i] = (float)src[i];
+        LEM_CUDA_TRY(cudaMemcpy2DAsync(s.slopes + 8 * off, W * 32, t, r.w * 32, r.w * 32, r.h, cudaMemcpyHostToDevice,
+                                       h->st));
+    } else if (f == LEM_F_FA) {
+        const double* src = static_cast<const double*>(host);
+        float2* t = static_cast<float2*>(h->staging);
+        for (size_t i = 0; i < n; ++i) {
+            const float hi = (float)src[i];
+            t[i] = make_float2(hi, (float)(src[i] - (double)hi));
+        }
+        LEM_CUDA_TRY(cudaMemcpy2DAsync(s.fa + off, W * 8, t, r.w * 8, r.w * 8, r.h, cudaMemcpyHostToDevice, h->st));
+    } else if (f == LEM_F_FD || f == LEM_F_SFD) {
+        // int32 codes; -9999 (outside the catchment) keeps its low byte 0xF1
+        const int32_t* src = static_cast<const int32_t*>(host);
+        uint8_t* t = static_cast<uint8_t*>(h->staging);
+        for (size_t i = 0; i < n; ++i) t[i] = (uint8_t)(src[i] & 0xff);
+        LEM_CUDA_TRY(cudaMemcpy2DAsync((f == LEM_F_FD ? s.fd : s.sfd) + off, W, t, r.w, r.w, r.h,
+                                       cudaMemcpyHostToDevice, h->st));
+    } else {
+        if (field_is_int(f)) return LEM_ERR_INVALID;  // the mask, counts and labels are computed, not set
+        float* dst = float_field(h, f);
+        if (!dst) return LEM_ERR_INVALID;
+        const double* src = static_cast<const double*>(host);
+        float* t = static_cast<float*>(h->staging);
+        for (size_t i = 0; i < n; ++i) t[i] = (float)src[i];
+        LEM_CUDA_TRY(cudaMemcpy2DAsync(dst + off, W * 4, t, r.w * 4, r.w * 4, r.h, cudaMemcpyHostToDevice, h->st));
+    }
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    return LEM_OK;
+}
+
+lem_status get_region_field(lem_handle* h, const HostDem& r, int id, lem_field f, void* host) {
+    const size_t n = (size_t)r.w * r.h;
+    const size_t W = (size_t)h->k.W;
+    const size_t off = (size_t)r.y0 * W + r.x0;
+    DevState& s = h->s;
+    lem_status st;
+    if ((st = ensure_staging(h, n * 8 * sizeof(float))) != LEM_OK) return st;
+    if ((st = sync_scalars(h)) != LEM_OK) return st;
+    const DemOut& o = h->host_out[id];
+    auto get2d = [&](void* dst, const void* src, size_t elem) {
+        return cudaMemcpy2D(dst, r.w * elem, src, W * elem, r.w * elem, r.h, cudaMemcpyDeviceToHost);
+    };
+    switch (f) {
+        case LEM_F_DEM:
+            LEM_CUDA_TRY(get2d(host, s.z + off, 8));
+            return LEM_OK;
+        case LEM_F_DEM_ROUTED:
+            // without sinks the second pass does not run and the stage's DEM is the routed one
+            LEM_CUDA_TRY(get2d(host, (o.sinkcount_pass1 ? s.zf : s.z) + off, 8));
+            return LEM_OK;
+        case LEM_F_MASK: {
+            uint8_t* m = static_cast<uint8_t*>(h->staging);
+            LEM_CUDA_TRY(get2d(m, s.mask + off, 1));
+            int32_t* out = static_cast<int32_t*>(host);
+            for (size_t i = 0; i < n; ++i) out[i] = m[i];
+            return LEM_OK;
+        }
+        case LEM_F_FD:
+        case LEM_F_SFD:
+        case LEM_F_SFD_PASS1: {
+            uint8_t* buf = static_cast<uint8_t*>(h->staging);
+            const uint8_t* src = f == LEM_F_FD ? s.fd : (f == LEM_F_SFD ? s.sfd : s.sfd1);
+            LEM_CUDA_TRY(get2d(buf, src + off, 1));
+            LEM_CUDA_TRY(get2d(buf + n, s.mask + off, 1));
+            const int64_t outlet = (int64_t)o.outlet;
+            const int64_t ol = (outlet / (int64_t)W - r.y0) * r.w + (outlet % (int64_t)W - r.x0);
+            int32_t* out = static_cast<int32_t*>(host);
+            for (size_t i = 0; i < n; ++i) {
+                int32_t v = buf[n + i] ? (int32_t)buf[i] : -9999;  // masked cells hold -9999 (newflow.cu:74)
+                if (f == LEM_F_FD && (int64_t)i == ol) v = 16;       // routeflow.cu:953
+                out[i] = v;
+            }
+            return LEM_OK;
+        }
+        case LEM_F_CONTRIB:
+            LEM_CUDA_TRY(get2d(host, s.contrib + off, 4));
+            return LEM_OK;
+        case LEM_F_WATERSHED:
+            LEM_CUDA_TRY(get2d(host, s.ws + off, 4));
+            return LEM_OK;
+        case LEM_F_SLOPES: {
+            float* t = static_cast<float*>(h->staging);
+            LEM_CUDA_TRY(get2d(t, s.slopes + 8 * off, 32));
+            double* out = static_cast<double*>(host);
+            for (size_t i = 0; i < 8 * n; ++i) out[i] = t[i];
+            return LEM_OK;
+        }
+        case LEM_F_FA: {
+            float2* t = static_cast<float2*>(h->staging);
+            LEM_CUDA_TRY(get2d(t, s.fa + off, 8));
+            double* out = static_cast<double*>(host);
+            for (size_t i = 0; i < n; ++i) out[i] = (double)t[i].x + (double)t[i].y;
+            return LEM_OK;
+        }
+        default: {
+            float* src = float_field(h, f);
+            if (!src) return LEM_ERR_INVALID;
+            float* t = static_cast<float*>(h->staging);
+            LEM_CUDA_TRY(get2d(t, src + off, 4));
+            double* out = static_cast<double*>(host);
+            for (size_t i = 0; i < n; ++i) out[i] = t[i];
+            return LEM_OK;
+        }
+    }
+}
+
+lem_status totals_of(lem_handle* h, int id, lem_totals* o) {
+    lem_status r = sync_scalars(h);
+    if (r != LEM_OK) return r;
+    const DevScalars& g = *h->host_sc;
+    const DemOut& d = h->host_out[id];
+    std::memset(o, 0, sizeof *o);
+    o->tot_e = d.tot_e;
+    o->tot_i = d.tot_i;
+    o->tot_g = d.tot_g;
+    o->tot_d = d.tot_d;
+    o->tot_weather_c = d.tot_wc;
+    o->tot_weather_p = d.tot_wp;
+    o->tot_bio = d.tot_bio;
+    {
+        // FA_max from its ordered key (the hi and lo words are ordered fp32 keys)
+        auto unkey = [](uint32_t k) {
+            uint32_t b = (k >> 31) ? (k & 0x7fffffffu) : ~k;
+            float f;
+            std::memcpy(&f, &b, 4);
+            return f;
+        };
+        const unsigned long long fk = d.fa_max_key;
+        double v = fk ? (double)unkey((uint32_t)(fk >> 32)) + (double)unkey((uint32_t)fk) : 0.0;
+        o->fa_max = v > 0.0 ? v : 0.0;
+    }
+    const HostDem& hd = h->dems[id];
+    o->rain = hd.rain;
+    o->temp = hd.temp;
+    o->sinkcount = d.sinkcount;
+    // the outlet as an index of the DEM's own grid
+    o->outlet = (int32_t)(((int64_t)d.outlet / h->k.W - hd.y0) * hd.w + ((int64_t)d.outlet % h->k.W - hd.x0));
+    o->initial_sinks = d.sink_counter;
+    o->initial_flats = d.flat_counter;
+    o->plateau_sweeps = g.plateau_sweeps;
+    o->flood_edges = g.n_edges;
+    o->fa_uncomputed = d.n_active - d.fa_done;
+    o->sed_uncomputed = d.n_active - d.sed_done;
+    return LEM_OK;
+}
+
+lem_status set_climate(HostDem& r, const lem_climate* c) {
+    if (c->recompute) {
+        r.rain = c->rain;
+        r.temp = c->temp;
+        r.from_current = true;
+    } else if (r.from_current) {
+        return LEM_ERR_STATE;
+    }
     return LEM_OK;
 }
 
@@ -177,17 +464,24 @@ const char* lem_status_string(lem_status s) {
     return "unknown status";
 }
 
-lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, double init_rain, double init_temp,
-                      lem_handle** out) {
+}  // extern "C"
+
+namespace {
+
+lem_status create_common(const lem_grid_desc* grid, const lem_params* params, int max_dems, bool batch,
+                         lem_handle** out) {
     if (!grid || !params || !out) return LEM_ERR_INVALID;
     *out = nullptr;
     if (grid->width < 1 || grid->height < 1 || !(grid->cellsize > 0)) return LEM_ERR_INVALID;
     const size_t N = (size_t)grid->width * grid->height;
     if (N >= (size_t)0x7ffffff0) return LEM_ERR_INVALID;  // int32 cell indices
     if ((int)grid->cellsize < 1) return LEM_ERR_INVALID;
+    if (max_dems < 1 || max_dems >= (int)kNoDem) return LEM_ERR_INVALID;
     lem_handle* h = new lem_handle();
     h->N = N;
     h->p = *params;
+    h->batch = batch;
+    h->dems.resize(max_dems);
     // mfd_accum.cu:406-407 clamps the travel distances before the first use
     if (h->p.ddk > 0.95) h->p.ddk = 0.95;
     if (h->p.dck > 0.9) h->p.dck = 0.9;
@@ -230,11 +524,6 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
     k.rescale_weather = (float)(10000 * (10000 / (cs * cs)));
     k.rescale_veg = (float)(10000 / (cs * cs));
     k.erod_const = (float)((0.043 * (params->soil_struct - 2.)) + (0.033 * (params->profile_permeability - 3.)));
-    ClimateNow& c = h->c;
-    c.rain = c.rain0 = init_rain;
-    c.temp = c.temp0 = init_temp;
-    c.rain_inc = c.rain0_inc = (init_rain * 2 - init_rain) / grid->height;
-    c.from_current_dem = 0;
 
     DevState& s = h->s;
     lem_status r = LEM_OK;
@@ -307,21 +596,41 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
     ALLOC(s.cmaxw, N + 1);
     ALLOC(s.sc, 1);
     ALLOC(s.temp_tab, (size_t)kTabN);
+    ALLOC(h->dem_in, (size_t)max_dems);
+    ALLOC(h->dem_out, (size_t)max_dems);
+    ALLOC(h->chunks, (size_t)max_dems + 1);
+    if (batch) {
+        ALLOC(h->dem_of, N);
+    }
 #undef ALLOC
+    s.chunk_start = h->chunks;
+    s.dems = DemCtx{h->dem_of, h->dem_in, h->dem_out, max_dems};
     std::vector<float> tab;
     dreybrodt_table(tab);
     e = cudaMemcpyAsync(s.temp_tab, tab.data(), sizeof(float) * kTabN, cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess) e = cudaMallocHost(&h->host_sc, sizeof(DevScalars));
-    h->staging_bytes = 8 * N * sizeof(double);
-    if (e == cudaSuccess) e = cudaMallocHost(&h->staging, h->staging_bytes);
+    if (e == cudaSuccess) e = cudaMallocHost(&h->host_out, sizeof(DemOut) * max_dems);
     if (e != cudaSuccess) {
         lem_destroy(h);
         return LEM_ERR_NOMEM;
     }
     std::memset(h->host_sc, 0, sizeof(DevScalars));
     h->host_sc->round_id = 1;
-    h->host_sc->lowest_key = ~0ull;
+    std::memset(h->host_out, 0, sizeof(DemOut) * max_dems);
     e = cudaMemcpyAsync(s.sc, h->host_sc, sizeof(DevScalars), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess && batch) {
+        // a batch grid starts as nodata outside every DEM
+        const int blocks = (int)std::min<size_t>((N + 255) / 256, 152 * 32);
+        k_fill_f64<<<blocks, 256, 0, h->st>>>(s.z, N, kNoData);
+        k_fill_f64<<<blocks, 256, 0, h->st>>>(s.z_init, N, kNoData);
+        k_fill_f64<<<blocks, 256, 0, h->st>>>(s.zf, N, kNoData);
+        k_fill_u16<<<blocks, 256, 0, h->st>>>(h->dem_of, N, kNoDem);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemsetAsync(s.sfd, kMaskedCode, N, h->st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s.mfd, kMaskedCode, N, h->st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s.fd, kMaskedCode, N, h->st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s.sfd1, kMaskedCode, N, h->st);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     if (e != cudaSuccess) {
         lem_destroy(h);
@@ -336,6 +645,37 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
     return LEM_OK;
 }
 
+lem_status run_stage(lem_handle* h, int stage, uint32_t flags) {
+    lem_status r = prepare(h);
+    if (r != LEM_OK) return r;
+    const Launch L = h->launch();
+    if (stage == 0) return launch_flow_direction(h->s, h->k, L);
+    if (stage == 1) {
+        uint32_t f = flags & ~LEM_STEP_SET_OUTLET_FROM_FA;
+        if (any_flag(h, LEM_STEP_SET_OUTLET_FROM_FA)) f |= LEM_STEP_SET_OUTLET_FROM_FA;
+        return launch_flow_accumulation(h->s, h->k, f, L);
+    }
+    return launch_erosion(h->s, h->k, flags, L);
+}
+
+}  // namespace
+
+extern "C" {
+
+lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, double init_rain, double init_temp,
+                      lem_handle** out) {
+    lem_status r = create_common(grid, params, 1, false, out);
+    if (r != LEM_OK) return r;
+    HostDem& d = (*out)->dems[0];
+    d.x0 = d.y0 = 0;
+    d.w = grid->width;
+    d.h = grid->height;
+    d.rain = d.rain0 = init_rain;
+    d.temp = d.temp0 = init_temp;
+    d.outlet_set = true;  // cell 0 until lem_set_outlet
+    return LEM_OK;
+}
+
 lem_status lem_destroy(lem_handle* h) {
     if (!h) return LEM_ERR_INVALID;
     if (h->st) cudaStreamSynchronize(h->st);
@@ -345,6 +685,7 @@ lem_status lem_destroy(lem_handle* h) {
     for (void* q : h->allocs) cudaFree(q);
     if (h->staging) cudaFreeHost(h->staging);
     if (h->host_sc) cudaFreeHost(h->host_sc);
+    if (h->host_out) cudaFreeHost(h->host_out);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
     return LEM_OK;
@@ -352,174 +693,66 @@ lem_status lem_destroy(lem_handle* h) {
 
 lem_status lem_set_field(lem_handle* h, lem_field f, const void* host) {
     if (!h || !host || f < 0 || f >= LEM_F_COUNT) return LEM_ERR_INVALID;
-    const size_t N = h->N;
-    DevState& s = h->s;
+    if (h->batch) return LEM_ERR_STATE;
+    HostDem& d = h->dems[0];
+    lem_status r = set_region_field(h, d, f, host);
+    if (r != LEM_OK || f != LEM_F_DEM || h->dem_set) return r;
+    // createmask (MEM_kernels/memory.cu:229-238) and the DEM of the initial climate grids
+    const double* dem = static_cast<const double*>(host);
+    uint8_t* m = static_cast<uint8_t*>(h->staging);
+    for (size_t i = 0; i < h->N; ++i) m[i] = (dem[i] == -9999) ? 0 : 1;
+    LEM_CUDA_TRY(cudaMemcpyAsync(h->s.mask, m, h->N, cudaMemcpyHostToDevice, h->st));
+    LEM_CUDA_TRY(cudaMemcpyAsync(h->s.z_init, dem, sizeof(double) * h->N, cudaMemcpyHostToDevice, h->st));
     LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
-    if (f == LEM_F_DEM) {
-        const double* dem = static_cast<const double*>(host);
-        LEM_CUDA_TRY(cudaMemcpyAsync(s.z, dem, sizeof(double) * N, cudaMemcpyHostToDevice, h->st));
-        if (!h->dem_set) {
-            // createmask (MEM_kernels/memory.cu:229-238) and the DEM of the initial climate grids
-            uint8_t* m = static_cast<uint8_t*>(h->staging);
-            for (size_t i = 0; i < N; ++i) m[i] = (dem[i] == -9999) ? 0 : 1;
-            LEM_CUDA_TRY(cudaMemcpyAsync(s.mask, m, N, cudaMemcpyHostToDevice, h->st));
-            LEM_CUDA_TRY(cudaMemcpyAsync(s.z_init, dem, sizeof(double) * N, cudaMemcpyHostToDevice, h->st));
-            h->dem_set = true;
-        }
-        LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
-        return LEM_OK;
-    }
-    if (f == LEM_F_SLOPES || f == LEM_F_FA) {
-        const double* src = static_cast<const double*>(host);
-        if (f == LEM_F_SLOPES) {
-            float* t = static_cast<float*>(h->staging);
-            for (size_t i = 0; i < 8 * N; ++i) t[i] = (float)src[i];
-            LEM_CUDA_TRY(cudaMemcpyAsync(s.slopes, t, sizeof(float) * 8 * N, cudaMemcpyHostToDevice, h->st));
-        } else {
-            float2* t = static_cast<float2*>(h->staging);
-            for (size_t i = 0; i < N; ++i) {
-                const float hi = (float)src[i];
-                t[i] = make_float2(hi, (float)(src[i] - (double)hi));
-            }
-            LEM_CUDA_TRY(cudaMemcpyAsync(s.fa, t, sizeof(float2) * N, cudaMemcpyHostToDevice, h->st));
-        }
-        LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
-        return LEM_OK;
-    }
-    if (f == LEM_F_FD || f == LEM_F_SFD) {
-        // int32 codes; -9999 (outside the catchment) keeps its low byte 0xF1
-        const int32_t* src = static_cast<const int32_t*>(host);
-        uint8_t* t = static_cast<uint8_t*>(h->staging);
-        for (size_t i = 0; i < N; ++i) t[i] = (uint8_t)(src[i] & 0xff);
-        LEM_CUDA_TRY(cudaMemcpyAsync(f == LEM_F_FD ? s.fd : s.sfd, t, N, cudaMemcpyHostToDevice, h->st));
-        LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
-        return LEM_OK;
-    }
-    if (field_is_int(f)) return LEM_ERR_INVALID;  // the mask, counts and labels are computed, not set
-    float* dst = float_field(h, f);
-    if (!dst) return LEM_ERR_INVALID;
-    const double* src = static_cast<const double*>(host);
-    float* t = static_cast<float*>(h->staging);
-    for (size_t i = 0; i < N; ++i) t[i] = (float)src[i];
-    LEM_CUDA_TRY(cudaMemcpyAsync(dst, t, sizeof(float) * N, cudaMemcpyHostToDevice, h->st));
-    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    h->dem_set = true;
+    d.active = true;
     return LEM_OK;
 }
 
 lem_status lem_get_field(lem_handle* h, lem_field f, void* host) {
     if (!h || !host || f < 0 || f >= LEM_F_COUNT) return LEM_ERR_INVALID;
-    const size_t N = h->N;
-    DevState& s = h->s;
-    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
-    switch (f) {
-        case LEM_F_DEM:
-            LEM_CUDA_TRY(cudaMemcpy(host, s.z, sizeof(double) * N, cudaMemcpyDeviceToHost));
-            return LEM_OK;
-        case LEM_F_DEM_ROUTED: {
-            const lem_status rs = sync_scalars(h);
-            if (rs != LEM_OK) return rs;
-            // without sinks the second pass does not run and the stage's DEM is the routed one
-            LEM_CUDA_TRY(cudaMemcpy(host, h->host_sc->sinkcount_pass1 ? s.zf : s.z, sizeof(double) * N,
-                                    cudaMemcpyDeviceToHost));
-            return LEM_OK;
-        }
-        case LEM_F_MASK: {
-            uint8_t* m = static_cast<uint8_t*>(h->staging);
-            LEM_CUDA_TRY(cudaMemcpy(m, s.mask, N, cudaMemcpyDeviceToHost));
-            int32_t* o = static_cast<int32_t*>(host);
-            for (size_t i = 0; i < N; ++i) o[i] = m[i];
-            return LEM_OK;
-        }
-        case LEM_F_FD:
-        case LEM_F_SFD:
-        case LEM_F_SFD_PASS1: {
-            uint8_t* buf = static_cast<uint8_t*>(h->staging);
-            const uint8_t* src = f == LEM_F_FD ? s.fd : (f == LEM_F_SFD ? s.sfd : s.sfd1);
-            LEM_CUDA_TRY(cudaMemcpy(buf, src, N, cudaMemcpyDeviceToHost));
-            LEM_CUDA_TRY(cudaMemcpy(buf + N, s.mask, N, cudaMemcpyDeviceToHost));
-            const lem_status rs = sync_scalars(h);
-            if (rs != LEM_OK) return rs;
-            const int outlet = h->host_sc->outlet;
-            int32_t* o = static_cast<int32_t*>(host);
-            for (size_t i = 0; i < N; ++i) {
-                int32_t v = buf[N + i] ? (int32_t)buf[i] : -9999;  // masked cells hold -9999 (newflow.cu:74)
-                if (f == LEM_F_FD && (int)i == outlet) v = 16;       // routeflow.cu:953
-                o[i] = v;
-            }
-            return LEM_OK;
-        }
-        case LEM_F_CONTRIB:
-            LEM_CUDA_TRY(cudaMemcpy(host, s.contrib, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
-            return LEM_OK;
-        case LEM_F_WATERSHED:
-            LEM_CUDA_TRY(cudaMemcpy(host, s.ws, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
-            return LEM_OK;
-        case LEM_F_SLOPES: {
-            float* t = static_cast<float*>(h->staging);
-            LEM_CUDA_TRY(cudaMemcpy(t, s.slopes, sizeof(float) * 8 * N, cudaMemcpyDeviceToHost));
-            double* o = static_cast<double*>(host);
-            for (size_t i = 0; i < 8 * N; ++i) o[i] = t[i];
-            return LEM_OK;
-        }
-        case LEM_F_FA: {
-            float2* t = static_cast<float2*>(h->staging);
-            LEM_CUDA_TRY(cudaMemcpy(t, s.fa, sizeof(float2) * N, cudaMemcpyDeviceToHost));
-            double* o = static_cast<double*>(host);
-            for (size_t i = 0; i < N; ++i) o[i] = (double)t[i].x + (double)t[i].y;
-            return LEM_OK;
-        }
-        default: {
-            float* src = float_field(h, f);
-            if (!src) return LEM_ERR_INVALID;
-            float* t = static_cast<float*>(h->staging);
-            LEM_CUDA_TRY(cudaMemcpy(t, src, sizeof(float) * N, cudaMemcpyDeviceToHost));
-            double* o = static_cast<double*>(host);
-            for (size_t i = 0; i < N; ++i) o[i] = t[i];
-            return LEM_OK;
-        }
-    }
+    if (h->batch) return LEM_ERR_STATE;
+    return get_region_field(h, h->dems[0], 0, f, host);
 }
 
 lem_status lem_set_outlet(lem_handle* h, int32_t cell) {
     if (!h || cell < 0 || (size_t)cell >= h->N) return LEM_ERR_INVALID;
-    LEM_CUDA_TRY(cudaMemcpyAsync(&h->s.sc->outlet, &cell, sizeof(int32_t), cudaMemcpyHostToDevice, h->st));
+    if (h->batch) return LEM_ERR_STATE;
+    LEM_CUDA_TRY(cudaMemcpyAsync(&h->dem_out[0].outlet, &cell, sizeof(int32_t), cudaMemcpyHostToDevice, h->st));
     LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
     return LEM_OK;
 }
 
 lem_status lem_set_climate(lem_handle* h, const lem_climate* c) {
     if (!h || !c) return LEM_ERR_INVALID;
-    if (c->recompute) {
-        h->c.rain = c->rain;
-        h->c.temp = c->temp;
-        h->c.rain_inc = (c->rain * 2 - c->rain) / h->k.H;
-        h->c.from_current_dem = 1;
-    } else if (h->c.from_current_dem) {
-        return LEM_ERR_STATE;
-    }
-    return LEM_OK;
+    if (h->batch) return LEM_ERR_STATE;
+    return set_climate(h->dems[0], c);
 }
 
 lem_status lem_flow_direction(lem_handle* h) {
     if (!h) return LEM_ERR_INVALID;
-    if (!h->dem_set) return LEM_ERR_STATE;
-    return launch_flow_direction(h->s, h->k, h->launch());
+    if (!h->batch && !h->dem_set) return LEM_ERR_STATE;
+    return run_stage(h, 0, 0);
 }
 
 lem_status lem_flow_accumulation(lem_handle* h, uint32_t flags) {
     if (!h) return LEM_ERR_INVALID;
-    if (!h->dem_set) return LEM_ERR_STATE;
-    return launch_flow_accumulation(h->s, h->k, h->c, flags, h->launch());
+    if (!h->batch && !h->dem_set) return LEM_ERR_STATE;
+    if (!h->batch) h->dems[0].next_flags = flags;
+    lem_status r = run_stage(h, 1, flags);
+    if (!h->batch) h->dems[0].next_flags = 0;
+    return r;
 }
 
 lem_status lem_erosion(lem_handle* h, uint32_t flags) {
     if (!h) return LEM_ERR_INVALID;
-    if (!h->dem_set) return LEM_ERR_STATE;
-    return launch_erosion(h->s, h->k, h->c, flags, h->launch());
+    if (!h->batch && !h->dem_set) return LEM_ERR_STATE;
+    return run_stage(h, 2, flags);
 }
 
 lem_status lem_step(lem_handle* h, const lem_climate* c, uint32_t flags) {
     lem_status r;
+    if (!h) return LEM_ERR_INVALID;
     if (c && (r = lem_set_climate(h, c)) != LEM_OK) return r;
     if ((r = lem_flow_direction(h)) != LEM_OK) return r;
     if ((r = lem_flow_accumulation(h, flags)) != LEM_OK) return r;
@@ -542,40 +775,131 @@ lem_status lem_synchronize(lem_handle* h) {
 
 lem_status lem_get_totals(lem_handle* h, lem_totals* o) {
     if (!h || !o) return LEM_ERR_INVALID;
-    lem_status r = sync_scalars(h);
-    if (r != LEM_OK) return r;
-    const DevScalars& d = *h->host_sc;
-    std::memset(o, 0, sizeof *o);
-    o->tot_e = d.tot_e;
-    o->tot_i = d.tot_i;
-    o->tot_g = d.tot_g;
-    o->tot_d = d.tot_d;
-    o->tot_weather_c = d.tot_wc;
-    o->tot_weather_p = d.tot_wp;
-    o->tot_bio = d.tot_bio;
-    {
-        // FA_max from its ordered key (the hi and lo words are ordered fp32 keys)
-        auto unkey = [](uint32_t k) {
-            uint32_t b = (k >> 31) ? (k & 0x7fffffffu) : ~k;
-            float f;
-            std::memcpy(&f, &b, 4);
-            return f;
-        };
-        const unsigned long long fk = d.fa_max_key;
-        double v = fk ? (double)unkey((uint32_t)(fk >> 32)) + (double)unkey((uint32_t)fk) : 0.0;
-        o->fa_max = v > 0.0 ? v : 0.0;
+    if (h->batch) return LEM_ERR_STATE;
+    return totals_of(h, 0, o);
+}
+
+// ---- batches
+
+lem_status lem_create_batch(const lem_grid_desc* grid, const lem_params* params, int32_t max_dems,
+                            lem_handle** out) {
+    if (!grid || grid->width % kTile != 0) return LEM_ERR_INVALID;
+    return create_common(grid, params, max_dems, true, out);
+}
+
+lem_status lem_dem_add(lem_handle* h, int32_t x0, int32_t y0, int32_t width, int32_t height, const double* dem,
+                       double init_rain, double init_temp, int32_t* id) {
+    if (!h || !dem || !id || !h->batch) return LEM_ERR_INVALID;
+    if (x0 < 0 || y0 < 0 || width < 3 || height < 3 || x0 % kTile || y0 % kTile) return LEM_ERR_INVALID;
+    if ((int64_t)x0 + width > h->k.W || (int64_t)y0 + height > h->k.H) return LEM_ERR_INVALID;
+    // the tiles a DEM occupies belong to it alone
+    auto ext = [](int32_t v) { return (v + kTile - 1) / kTile * kTile; };
+    int slot = -1;
+    for (int d = 0; d < (int)h->dems.size(); ++d) {
+        const HostDem& o = h->dems[d];
+        if (!o.active) {
+            if (slot < 0) slot = d;
+            continue;
+        }
+        if (x0 < o.x0 + ext(o.w) && o.x0 < x0 + ext(width) && y0 < o.y0 + ext(o.h) && o.y0 < y0 + ext(height))
+            return LEM_ERR_INVALID;
     }
-    o->rain = h->c.rain;
-    o->temp = h->c.temp;
-    o->sinkcount = d.sinkcount;
-    o->outlet = d.outlet;
-    o->initial_sinks = d.sink_counter;
-    o->initial_flats = d.flat_counter;
-    o->plateau_sweeps = d.plateau_sweeps;
-    o->flood_edges = d.n_edges;
-    o->fa_uncomputed = d.n_active - d.fa_done;
-    o->sed_uncomputed = d.n_active - d.sed_done;
+    if (slot < 0) return LEM_ERR_CAPACITY;
+    // a nodata ring: no in-catchment cell of the DEM has a neighbour outside it
+    for (int32_t x = 0; x < width; ++x)
+        if (dem[x] != -9999 || dem[(size_t)(height - 1) * width + x] != -9999) return LEM_ERR_INVALID;
+    for (int32_t y = 0; y < height; ++y)
+        if (dem[(size_t)y * width] != -9999 || dem[(size_t)y * width + width - 1] != -9999) return LEM_ERR_INVALID;
+    HostDem& d = h->dems[slot];
+    d = HostDem{};
+    d.x0 = x0;
+    d.y0 = y0;
+    d.w = width;
+    d.h = height;
+    d.rain = d.rain0 = init_rain;
+    d.temp = d.temp0 = init_temp;
+    lem_status r = set_region_field(h, d, LEM_F_DEM, dem);
+    if (r != LEM_OK) return r;
+    if ((r = region_op(h, d, slot)) != LEM_OK) return r;
+    DemOut zero{};
+    zero.lowest_key = ~0ull;
+    LEM_CUDA_TRY(cudaMemcpyAsync(&h->dem_out[slot], &zero, sizeof zero, cudaMemcpyHostToDevice, h->st));
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    d.active = true;
+    *id = slot;
     return LEM_OK;
+}
+
+static lem_status dem_check(lem_handle* h, int32_t id) {
+    if (!h || !h->batch || id < 0 || id >= (int32_t)h->dems.size() || !h->dems[id].active) return LEM_ERR_INVALID;
+    return LEM_OK;
+}
+
+lem_status lem_dem_remove(lem_handle* h, int32_t id) {
+    lem_status r = dem_check(h, id);
+    if (r != LEM_OK) return r;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    if ((r = region_op(h, h->dems[id], -1)) != LEM_OK) return r;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    h->dems[id] = HostDem{};
+    return LEM_OK;
+}
+
+lem_status lem_dem_set_field(lem_handle* h, int32_t id, lem_field f, const void* host) {
+    lem_status r = dem_check(h, id);
+    if (r != LEM_OK) return r;
+    if (!host || f < 0 || f >= LEM_F_COUNT) return LEM_ERR_INVALID;
+    return set_region_field(h, h->dems[id], f, host);
+}
+
+lem_status lem_dem_get_field(lem_handle* h, int32_t id, lem_field f, void* host) {
+    lem_status r = dem_check(h, id);
+    if (r != LEM_OK) return r;
+    if (!host || f < 0 || f >= LEM_F_COUNT) return LEM_ERR_INVALID;
+    return get_region_field(h, h->dems[id], id, f, host);
+}
+
+lem_status lem_dem_set_outlet(lem_handle* h, int32_t id, int32_t cell) {
+    lem_status r = dem_check(h, id);
+    if (r != LEM_OK) return r;
+    HostDem& d = h->dems[id];
+    if (cell < 0 || cell >= d.w * d.h) return LEM_ERR_INVALID;
+    const int32_t g = (d.y0 + cell / d.w) * h->k.W + d.x0 + cell % d.w;
+    LEM_CUDA_TRY(cudaMemcpyAsync(&h->dem_out[id].outlet, &g, sizeof g, cudaMemcpyHostToDevice, h->st));
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    d.outlet_set = true;
+    return LEM_OK;
+}
+
+lem_status lem_dem_set_climate(lem_handle* h, int32_t id, const lem_climate* c) {
+    lem_status r = dem_check(h, id);
+    if (r != LEM_OK) return r;
+    if (!c) return LEM_ERR_INVALID;
+    return set_climate(h->dems[id], c);
+}
+
+lem_status lem_dem_set_step_flags(lem_handle* h, int32_t id, uint32_t flags) {
+    lem_status r = dem_check(h, id);
+    if (r != LEM_OK) return r;
+    h->dems[id].next_flags = flags;
+    return LEM_OK;
+}
+
+lem_status lem_dem_get_totals(lem_handle* h, int32_t id, lem_totals* out) {
+    lem_status r = dem_check(h, id);
+    if (r != LEM_OK) return r;
+    if (!out) return LEM_ERR_INVALID;
+    return totals_of(h, id, out);
+}
+
+lem_status lem_step_batch(lem_handle* h, uint32_t flags) {
+    if (!h || !h->batch) return LEM_ERR_INVALID;
+    lem_status r;
+    if ((r = run_stage(h, 0, 0)) != LEM_OK) return r;
+    if ((r = run_stage(h, 1, flags)) != LEM_OK) return r;
+    r = run_stage(h, 2, flags);
+    for (HostDem& d : h->dems) d.next_flags = 0;
+    return r;
 }
 
 void* lem_stream(lem_handle* h) { return h ? (void*)h->st : nullptr; }

@@ -75,30 +75,62 @@ struct ErrFlags {  // bits of the device error word
 
 // Device-side scalars of one handle (one allocation, read back only on request).
 struct DevScalars {
-    unsigned long long lowest_key;   // min masked-in DEM key (testoutletislowest)
-    int32_t outlet;
-    int32_t sink_counter, flat_counter;
-    int32_t sinkcount_pass1;         // masked-in SFD == 0 after the first plateau pass
-    int32_t sinkcount;               // Data.sinkcount
+    int32_t sinkcount_pass1;         // masked-in SFD == 0 after the first plateau pass, all DEMs
     int32_t plateau_sweeps;
     int32_t n_cand;                  // plateau candidates
     int32_t n_sinks;                 // sink cells of the flooding
     int32_t n_edges;                 // distinct basin pairs
     int32_t n_basins;
-    int32_t fa_done, sed_done, n_active;
     int32_t flood_sweeps, label_rounds, spill_rounds;
     uint32_t err;
     int32_t round_id;                // monotonic id of worklist rounds (de-duplication marks)
-    double base_level;               // update_newSurface base (updates.cu:151)
-    double outlet_z_clim;            // z[outlet] as seen by the climate grids
-    unsigned long long fa_max_key;   // FA_max as an ordered key of hi+lo
-    double tot_e, tot_i, tot_g, tot_d, tot_wc, tot_wp, tot_bio;
     int32_t flag[4];                 // convergence flags of the cooperative loops
     int32_t counters[8];
     int32_t tiled_ok;                // 1: this step's accumulation may take the tiled path
     int32_t tile_src;                // tile outlets with no pending inflow (coarse sources)
     int32_t sed_tiled_ok;            // 1: this step's sediment routing may take the tiled path
 };
+
+// The DEMs of a handle.  A single grid is one DEM covering the whole grid; a
+// batch packs several DEMs into one grid, each in its own region (32-aligned,
+// with a nodata ring, so no in-catchment cell of one DEM sees another DEM).
+constexpr uint16_t kNoDem = 0xFFFF;  // a cell outside every DEM's region
+
+// Per-DEM inputs owned by the host, uploaded before each stage: the region and
+// the climate scalars of the step (SetClimateMatrices, Data.cpp:211-303).
+struct DemIn {
+    int32_t x0, y0, w, h;            // region in the grid
+    int32_t active;
+    int32_t from_current_dem;        // temperature from the DEM at step start (1) or the initial DEM (0)
+    int32_t outlet_from_fa;          // this step moves the outlet to the largest accumulation
+    int32_t pad;
+    double rain, temp, rain_inc;     // rain row gradient (2R - R) / h
+    double rain0, temp0, rain0_inc;  // initial ("last") scalars
+};
+
+// Per-DEM results kept on the device.
+struct DemOut {
+    unsigned long long lowest_key;   // min masked-in DEM key (testoutletislowest)
+    unsigned long long fa_max_key;   // FA_max as an ordered key of hi+lo
+    double base_level;               // update_newSurface base (updates.cu:151)
+    double outlet_z_clim;            // z[outlet] as seen by the climate grids
+    double tot_e, tot_i, tot_g, tot_d, tot_wc, tot_wp, tot_bio;
+    int32_t outlet;                  // grid cell index
+    int32_t sink_counter, flat_counter;
+    int32_t sinkcount_pass1;         // this DEM's share of DevScalars::sinkcount_pass1
+    int32_t sinkcount;               // Data.sinkcount
+    int32_t fa_done, sed_done, n_active;
+    int32_t argmax;                  // first cell holding FA_max
+    int32_t zero_seen;               // epoch of the last sinkcount that counted basin 0
+};
+
+struct DemCtx {
+    const uint16_t* of;  // DEM of each cell; null: every cell belongs to DEM 0
+    const DemIn* in;
+    DemOut* out;
+    int32_t n;           // DEM slots
+};
+__device__ __forceinline__ int dem_at(const DemCtx& dc, size_t cell) { return dc.of ? (int)dc.of[cell] : 0; }
 
 }  // namespace lem
 

@@ -34,14 +34,6 @@ struct ModelConsts {  // per-handle constants derived on the host in double
     float erod_const;       // 0.043*(struct-2) + 0.033*(perm-3)
 };
 
-struct ClimateNow {  // the climate grids of the current step, generated on the fly
-    double rain, temp;      // scalars of the last SetClimateMatrices
-    double rain_inc;        // (2R - R) / H
-    double rain0, temp0;    // initial ("last") scalars
-    double rain0_inc;
-    int32_t from_current_dem; // 1: temperature from the DEM at step start, 0: from the initial DEM
-    int32_t pad;
-};
 
 struct DevState {
     // grids
@@ -92,9 +84,43 @@ struct DevState {
     unsigned long long* cdist;  //   their minimax distance to the component's label basin
     unsigned long long* cmaxw;  //   the component's largest spanning-tree edge
     DevScalars* sc;
+    DemCtx dems;                // the DEMs of the grid
+    int32_t* chunk_start;       // streaming passes: first chunk of each DEM (n + 1 entries)
+    int32_t n_chunks;
     float* temp_tab;
     int32_t max_coop_blocks;    // co-resident blocks of the cooperative kernels
 };
+
+// Streaming passes over the DEMs' regions run one block per chunk of kChunk
+// cells, every chunk inside one DEM, so block sums go to that DEM's totals.
+constexpr int kChunk = 4096;
+struct Chunk {
+    int d;          // DEM
+    int64_t first;  // first region-linear cell of the chunk
+    int64_t end;    // one past the last
+};
+__device__ __forceinline__ Chunk chunk_of(const int32_t* chunk_start, int n, const DemIn* in) {
+    // the DEM whose chunk range holds blockIdx.x (n is small: binary search)
+    int lo = 0, hi = n;
+    const int b = blockIdx.x;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (chunk_start[mid] <= b) lo = mid; else hi = mid;
+    }
+    Chunk c;
+    c.d = lo;
+    c.first = (int64_t)(b - chunk_start[lo]) * kChunk;
+    const int64_t cells = (int64_t)in[lo].w * in[lo].h;
+    c.end = c.first + kChunk < cells ? c.first + kChunk : cells;
+    return c;
+}
+// grid index of region-linear cell i of DEM region r
+__device__ __forceinline__ size_t region_cell(const DemIn& r, int64_t i, int W, int* x, int* y) {
+    const int ry = (int)(i / r.w), rx = (int)(i - (int64_t)ry * r.w);
+    *x = r.x0 + rx;
+    *y = r.y0 + ry;
+    return (size_t)(*y) * W + *x;
+}
 
 // Optional per-kernel timing with CUDA events on the handle's stream.
 struct Profiler;
@@ -125,9 +151,9 @@ struct Launch {
 
 // stage launchers (stream-ordered, no host synchronisation)
 lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const Launch& L);
-lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
+lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, uint32_t flags,
                                     const Launch& L);
-lem_status launch_erosion(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
+lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flags,
                           const Launch& L);
 int coop_blocks_for(const void* kernel, int threads, size_t smem);
 

@@ -29,21 +29,26 @@ __global__ void k_fa_prep(const double* __restrict__ z, const uint8_t* __restric
                           const uint8_t* __restrict__ fd, const float* __restrict__ stone,
                           const float* __restrict__ totB, float* __restrict__ soilM, float* __restrict__ w,
                           float2* __restrict__ fa, int32_t* __restrict__ pending, int32_t* __restrict__ contrib,
-                          int32_t* ready, ModelConsts k, ClimateNow c, DevScalars* sc) {
+                          int32_t* ready, const int32_t* __restrict__ chunk_start, ModelConsts k, DemCtx dc,
+                          DevScalars* sc) {
     const int W = k.W, H = k.H;
     const size_t N = (size_t)W * H;
-    const float rain0 = (float)c.rain, rinc = (float)c.rain_inc;
+    const Chunk ch = chunk_of(chunk_start, dc.n, dc.in);
+    const DemIn& r = dc.in[ch.d];
+    const float rain0 = (float)r.rain, rinc = (float)r.rain_inc;
     int nact = 0;
-    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += (size_t)gridDim.x * blockDim.x) {
-        const size_t i = base + threadIdx.x;
+    for (int64_t base = ch.first; base < ch.end; base += blockDim.x) {
+        const int64_t ri = base + threadIdx.x;
         bool src = false;
-        if (i < N) {
-            const int x = (int)(i % W), y = (int)(i / W);
+        size_t i = 0;
+        if (ri < ch.end) {
+            int x, y;
+            i = region_cell(r, ri, W, &x, &y);
             if (mask[i]) {
                 ++nact;
                 const float coeff = (1.0f - 0.0085f * stone[i]) * expf(-0.0025f * totB[i] / 76.5f) *
                                     tanhf(0.6f + soilM[i] / 0.2f);
-                const float myppt = (rain0 + (float)y * rinc) / 1000.0f;
+                const float myppt = (rain0 + (float)(y - r.y0) * rinc) / 1000.0f;
                 const float wi = myppt * coeff;
                 float sm = soilM[i] + myppt * (1.0f - coeff);
                 if (sm > 0.5f) sm = 0.5f;
@@ -77,7 +82,7 @@ __global__ void k_fa_prep(const double* __restrict__ z, const uint8_t* __restric
         wave_append(src, (int32_t)i, ready, &sc->counters[0], (int)N, &sc->err);
     }
     nact = wsum(nact);
-    if ((threadIdx.x & 31) == 0 && nact) atomicAdd(&sc->n_active, nact);
+    if ((threadIdx.x & 31) == 0 && nact) atomicAdd(&dc.out[ch.d].n_active, nact);
 }
 
 // calcprops (runoffweight.cu:141-354): slope-proportional partition, forcing a
@@ -123,8 +128,10 @@ struct FaCell {
     const float* prop;
     float2* fa;
     int32_t* contrib;
+    DemCtx dc;
     int W, H;
     __device__ __forceinline__ void cell(int32_t cur, int x, int y) const {
+        if (dc.of) atomicAdd(&dc.out[dc.of[cur]].fa_done, 1);  // a batch: count per DEM
         float2 acc = make_float2(0.f, 0.f);
         int32_t cacc = 1;
 #pragma unroll
@@ -153,12 +160,12 @@ struct FaCell {
 __global__ void k_fa_walk(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                           const float* __restrict__ w, const float* __restrict__ prop, float2* fa, int32_t* pending,
                           int32_t* contrib, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc,
-                          int gate) {
+                          DemCtx dc, int gate) {
     if (gate && sc->tiled_ok) return;  // the tiled kernels did this step
-    const FaCell op{mask, fd, w, prop, fa, contrib, k.W, k.H};
+    const FaCell op{mask, fd, w, prop, fa, contrib, dc, k.W, k.H};
     int done = wave_walk(op, pending, list_a, list_b, k.W, k.H, sc);
     done = wsum(done);
-    if ((threadIdx.x & 31) == 0 && done) atomicAdd(&sc->fa_done, done);
+    if (!dc.of && (threadIdx.x & 31) == 0 && done) atomicAdd(&dc.out[0].fa_done, done);
 }
 
 // ---------------------------------------------------------------------------
@@ -450,7 +457,7 @@ __global__ void k_fat_coarse(const uint8_t* __restrict__ mask, const uint8_t* __
 __global__ void __launch_bounds__(256)
     k_fat_final(const double* __restrict__ z, const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                 const float* __restrict__ w, const int32_t* __restrict__ t_pend, float2* fa, ModelConsts k,
-                DevScalars* sc) {
+                DevScalars* sc, DemCtx dc) {
     if (!sc->tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -458,7 +465,7 @@ __global__ void __launch_bounds__(256)
     __shared__ float2 s_hval[kTH * kTH];
     __shared__ int32_t s_pend[kTile * kTile];
     __shared__ float2 s_val[kTile * kTile];
-    __shared__ int s_done;
+    __shared__ int s_done, s_dem;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = blockIdx.x;
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
@@ -478,7 +485,7 @@ __global__ void __launch_bounds__(256)
         s_hok[j] = ok;
         s_hval[j] = v;
     }
-    if (threadIdx.x == 0) s_done = 0;
+    if (threadIdx.x == 0) s_done = 0, s_dem = -1;
     __syncthreads();
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     int done = 0;
@@ -512,6 +519,7 @@ __global__ void __launch_bounds__(256)
                 if (t_pend[(size_t)(ty0 + ly) * W + tx0 + lx] == 0) ++done;
             }
             wl = w[(size_t)(ty0 + ly) * W + tx0 + lx];
+            atomicMax(&s_dem, dem_at(dc, (size_t)(ty0 + ly) * W + tx0 + lx));  // one DEM per tile
         }
         s_pend[l] = pend;
         src[q] = pend == 0 && !outlet[q];
@@ -563,56 +571,74 @@ __global__ void __launch_bounds__(256)
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();
-    if (threadIdx.x == 0 && s_done) atomicAdd(&sc->fa_done, s_done);
+    if (threadIdx.x == 0 && s_done && s_dem >= 0) atomicAdd(&dc.out[s_dem].fa_done, s_done);
 }
 
 // correctmfdflow's first-iteration branch (mfd_simple.cu:336-349): the outlet
 // becomes the first cell holding the largest accumulation.
-__global__ void k_fa_argmax(const float2* __restrict__ fa, size_t N, DevScalars* sc, int phase) {
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+__global__ void k_fa_argmax(const float2* __restrict__ fa, const int32_t* __restrict__ chunk_start, int W,
+                            DemCtx dc, int phase) {
+    const Chunk ch = chunk_of(chunk_start, dc.n, dc.in);
+    const DemIn& r = dc.in[ch.d];
+    DemOut& o = dc.out[ch.d];
+    if (!r.outlet_from_fa) return;
+    for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
+        int x, y;
+        const size_t i = region_cell(r, ri, W, &x, &y);
         const float2 v = fa[i];
         if (v.x != v.x) continue;  // NaN never wins the host scan (mfd_simple.cu:341)
         const unsigned long long kk = ffkey(v);
         if (phase == 0)
-            atomicMax(&sc->fa_max_key, kk);
-        else if (kk == sc->fa_max_key)
-            atomicMin(&sc->counters[7], (int32_t)i);
+            atomicMax(&o.fa_max_key, kk);
+        else if (kk == o.fa_max_key)
+            atomicMin(&o.argmax, (int32_t)i);
     }
 }
 
-__global__ void k_fa_argmax_set(DevScalars* sc) {
+// The DEM's outlet becomes the first cell of the largest accumulation; with
+// none above zero the reference's scan leaves index 0, the region's first cell.
+__global__ void k_fa_argmax_set(int W, DemCtx dc) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= dc.n || !dc.in[d].active || !dc.in[d].outlet_from_fa) return;
     const unsigned long long zero = ffkey(make_float2(0.f, 0.f));
-    sc->outlet = (sc->fa_max_key > zero) ? sc->counters[7] : 0;
+    DemOut& o = dc.out[d];
+    o.outlet = (o.fa_max_key > zero) ? o.argmax : dc.in[d].y0 * W + dc.in[d].x0;
 }
 
-__global__ void k_fa_reset(DevScalars* sc, int tiled) {
-    sc->counters[0] = 0;
-    sc->tiled_ok = tiled;
-    sc->tile_src = 0;
-    sc->fa_done = 0;
-    sc->n_active = 0;
-    sc->fa_max_key = 0ull;
-    sc->counters[7] = 0x7fffffff;
+__global__ void k_fa_reset(DevScalars* sc, DemCtx dc, int tiled) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d == 0) {
+        sc->counters[0] = 0;
+        sc->tiled_ok = tiled;
+        sc->tile_src = 0;
+    }
+    if (d < dc.n) {
+        DemOut& o = dc.out[d];
+        o.fa_done = 0;
+        o.n_active = 0;
+        o.fa_max_key = 0ull;
+        o.argmax = 0x7fffffff;
+    }
 }
 
 }  // namespace
 
-lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
-                                    const Launch& L) {
+lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, uint32_t flags, const Launch& L) {
     const size_t N = (size_t)k.W * k.H;
     const int T = 256;
     size_t nb = (N + T - 1) / T;
     const int blocks = (int)(nb > 152 * 32 ? 152 * 32 : nb);
+    const int dem_blocks = (s.dems.n + 127) / 128;
     int32_t* contrib = (flags & LEM_STEP_CONTRIB) ? s.contrib : nullptr;
     const int tiled = (k.flow_type == 0 && !contrib) ? 1 : 0;
-    LEM_LAUNCH(L, k_fa_reset, 1, 1, s.sc, tiled);
+    LEM_LAUNCH(L, k_fa_reset, dem_blocks, 128, s.sc, s.dems, tiled);
     const float* prop = nullptr;
     if (k.flow_type != 0 && k.mfd_props) {
         LEM_LAUNCH(L, k_calcprops, blocks, T, s.mask, s.fd, s.slopes, s.prop, N);
         prop = s.prop;
     }
-    LEM_LAUNCH(L, k_fa_prep, blocks, T, s.z, s.mask, s.fd, s.stone, s.totB, s.soilM, s.w, s.fa, s.pending, contrib,
-               s.list_a, k, c, s.sc);
+    LEM_LAUNCH(L, k_fa_prep, s.n_chunks, T, s.z, s.mask, s.fd, s.stone, s.totB, s.soilM, s.w, s.fa, s.pending,
+               contrib, s.list_a, s.chunk_start, k, s.dems, s.sc);
     if (tiled) {
         const int tiles = ((k.W + kTile - 1) / kTile) * ((k.H + kTile - 1) / kTile);
         LEM_LAUNCH(L, k_fat_local, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_la, s.t_dst, s.t_pend, s.t_orng, s.t_ent,
@@ -635,7 +661,7 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, con
         LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fat_coarse, dim3(s.max_coop_blocks), dim3(256),
                                                  args, 0, L.st));
         L.post();
-        LEM_LAUNCH(L, k_fat_final, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_pend, s.fa, k, s.sc);
+        LEM_LAUNCH(L, k_fat_final, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_pend, s.fa, k, s.sc, s.dems);
     }
     {
         const uint8_t* mask = s.mask;
@@ -647,18 +673,20 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, con
         int32_t* lb = s.list_b;
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
+        DemCtx dc = s.dems;
         int gate = tiled;
-        void* args[] = {(void*)&mask, (void*)&fd, (void*)&w, (void*)&prop, (void*)&fa, (void*)&pending,
-                        (void*)&contrib, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc, (void*)&gate};
+        void* args[] = {(void*)&mask,    (void*)&fd, (void*)&w,  (void*)&prop, (void*)&fa,  (void*)&pending,
+                        (void*)&contrib, (void*)&la, (void*)&lb, (void*)&kk,   (void*)&sc,  (void*)&dc,
+                        (void*)&gate};
         L.pre("k_fa_walk");
         LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fa_walk, dim3(s.max_coop_blocks), dim3(256), args,
                                                  0, L.st));
         L.post();
     }
-    if (flags & LEM_STEP_SET_OUTLET_FROM_FA) {
-        LEM_LAUNCH(L, k_fa_argmax, blocks, T, s.fa, N, s.sc, 0);
-        LEM_LAUNCH(L, k_fa_argmax, blocks, T, s.fa, N, s.sc, 1);
-        LEM_LAUNCH(L, k_fa_argmax_set, 1, 1, s.sc);
+    if (flags & LEM_STEP_SET_OUTLET_FROM_FA) {  // some DEM moves its outlet this step
+        LEM_LAUNCH(L, k_fa_argmax, s.n_chunks, T, s.fa, s.chunk_start, k.W, s.dems, 0);
+        LEM_LAUNCH(L, k_fa_argmax, s.n_chunks, T, s.fa, s.chunk_start, k.W, s.dems, 1);
+        LEM_LAUNCH(L, k_fa_argmax_set, dem_blocks, 128, k.W, s.dems);
     }
     LEM_CUDA_TRY(cudaGetLastError());
     return LEM_OK;
@@ -670,8 +698,9 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, con
 namespace {
 
 constexpr size_t kNaCells = LEM_NOALLOC_MAX_CELLS;
-constexpr size_t kNaHead = 1024;  // DevScalars, rounded up
-static_assert(sizeof(DevScalars) <= kNaHead, "scalar block");
+constexpr size_t kNaHead = 1024;  // DevScalars and one DemOut, rounded up
+constexpr size_t kNaOffDem = 512;
+static_assert(sizeof(DevScalars) <= kNaOffDem && kNaOffDem + sizeof(DemOut) <= kNaHead, "scalar block");
 constexpr size_t kNaOffCode = kNaHead;
 constexpr size_t kNaOffMask = kNaOffCode + kNaCells;
 constexpr size_t kNaOffPend = kNaOffMask + kNaCells;          // int32
@@ -691,9 +720,9 @@ struct NaDevice {
 std::mutex g_na_mutex;
 NaDevice g_na[64];
 
-__global__ void k_na_reset(DevScalars* sc) {
+__global__ void k_na_reset(DevScalars* sc, DemOut* dem) {
+    dem->fa_done = 0;
     sc->counters[0] = sc->counters[1] = sc->counters[2] = 0;
-    sc->fa_done = 0;
     sc->err = 0;
 }
 
@@ -762,6 +791,7 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     DevScalars* sc = reinterpret_cast<DevScalars*>(nd.base);
+    DemOut* dem = reinterpret_cast<DemOut*>(nd.base + kNaOffDem);
     uint8_t* code = nd.base + kNaOffCode;
     uint8_t* mask = nd.base + kNaOffMask;
     int32_t* pending = reinterpret_cast<int32_t*>(nd.base + kNaOffPend);
@@ -771,7 +801,7 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
     float2* fa = reinterpret_cast<float2*>(nd.base + kNaOffFa);
     const int T = 256;
     const int blocks = (int)std::min<size_t>((N + T - 1) / T, 152 * 32);
-    k_na_reset<<<1, 1, 0, st>>>(sc);  // the array keeps the previous call's contents
+    k_na_reset<<<1, 1, 0, st>>>(sc, dem);  // the array keeps the previous call's contents
     k_na_prep<<<blocks, T, 0, st>>>(d_fd, d_weight, d_dem, code, mask, w, fa, pending, la, width, height, sc);
     LEM_CUDA_TRY(cudaGetLastError());
     {
@@ -784,8 +814,9 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
         k.W = width;
         k.H = height;
         int gate = 0;
+        DemCtx dc{nullptr, nullptr, dem, 1};
         void* args[] = {(void*)&m, (void*)&c, (void*)&ww, (void*)&prop, (void*)&fa, (void*)&pending,
-                        (void*)&contrib, (void*)&la, (void*)&lb, (void*)&k, (void*)&sc, (void*)&gate};
+                        (void*)&contrib, (void*)&la, (void*)&lb, (void*)&k, (void*)&sc, (void*)&dc, (void*)&gate};
         LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fa_walk, dim3(nd.blocks), dim3(256), args, 0, st));
     }
     k_na_out<<<blocks, T, 0, st>>>(fa, d_fa, N);

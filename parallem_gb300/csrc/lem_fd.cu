@@ -25,6 +25,10 @@ constexpr int kMaxRounds = 1 << 16;
 __device__ __forceinline__ unsigned long long key_nodata() { return dkey(-9999.0); }
 
 __device__ __forceinline__ int warp_sum(int v) { return __reduce_add_sync(0xffffffffu, v); }
+// The DEM of a warp's valid lanes (a warp of 32 aligned cells lies in one DEM), -1 without one.
+__device__ __forceinline__ int warp_dem(const DemCtx& dc, size_t cell, bool valid) {
+    return __reduce_max_sync(0xffffffffu, valid ? dem_at(dc, cell) : -1);
+}
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
     for (int o = 16; o > 0; o >>= 1) {
@@ -60,7 +64,8 @@ __device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t* l
 // sink/flat counters and lowest elevation; pass 2 writes codes only.
 __global__ void __launch_bounds__(FD_BX* FD_BY)
     k_flowdirs(const double* __restrict__ z, const uint8_t* __restrict__ mask, float* __restrict__ slopes,
-               uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, ModelConsts k, DevScalars* sc, int pass) {
+               uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, ModelConsts k, DevScalars* sc, DemCtx dc,
+               int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
     __shared__ unsigned long long skey[FD_BY + 2][FD_BX + 2];
     __shared__ float shi[FD_BY + 2][FD_BX + 2];
@@ -192,10 +197,12 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     if (pass == 1) {
         const int s1 = warp_sum(is_sink), f1 = warp_sum(is_flat);
         low = warp_min_u64(low);
-        if ((threadIdx.x & 31) == 0) {
-            if (s1) atomicAdd(&sc->sink_counter, s1);
-            if (f1) atomicAdd(&sc->flat_counter, f1);
-            if (low != ~0ull) atomicMin(&sc->lowest_key, low);
+        const int d = warp_dem(dc, (size_t)y * W + x, x < W && y < H && mask[(size_t)y * W + x]);
+        if ((threadIdx.x & 31) == 0 && d >= 0) {
+            DemOut& o = dc.out[d];
+            if (s1) atomicAdd(&o.sink_counter, s1);
+            if (f1) atomicAdd(&o.flat_counter, f1);
+            if (low != ~0ull) atomicMin(&o.lowest_key, low);
         }
     }
 }
@@ -407,7 +414,7 @@ __global__ void k_plateau_final(const double* __restrict__ z, const float* __res
 // other cells point at their SFD receiver, masked and edge cells are basin 0.
 __global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
                              uint8_t* __restrict__ sfd1, int32_t* ws, int32_t* sinks, unsigned long long* raise,
-                             ModelConsts k, DevScalars* sc) {
+                             ModelConsts k, DevScalars* sc, DemCtx dc) {
     const int W = k.W, H = k.H;
     const size_t N = (size_t)W * H;
     int nsink = 0;
@@ -437,7 +444,12 @@ __global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __
             }
             ws[c] = v;
         }
-        nsink += warp_sum(sink ? 1 : 0) * ((threadIdx.x & 31) == 0);
+        const int ws_ = warp_sum(sink ? 1 : 0);
+        const int d = warp_dem(dc, c, sink);
+        if ((threadIdx.x & 31) == 0 && ws_) {
+            nsink += ws_;
+            atomicAdd(&dc.out[d].sinkcount_pass1, ws_);
+        }
         warp_append(sink, (int32_t)c, sinks, &sc->n_sinks, (int)N, &sc->err);
     }
     if (nsink) atomicAdd(&sc->sinkcount_pass1, nsink);
@@ -600,7 +612,8 @@ __global__ void k_flood_edges(const double* __restrict__ z, const uint8_t* __res
 // (data->sinkcount, newflow.cu:1044-1045).  Labels on edges start unreached.
 __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, const unsigned long long* __restrict__ ewt,
                                 int64_t cap, int32_t* ea, int32_t* eb, unsigned long long* ew,
-                                unsigned long long* raise, int32_t* seen, int32_t epoch, DevScalars* sc) {
+                                unsigned long long* raise, int32_t* seen, int32_t epoch, DevScalars* sc,
+                                DemCtx dc) {
     if (sc->sinkcount_pass1 == 0) return;
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)cap; base += (size_t)gridDim.x * blockDim.x) {
         const size_t i = base + threadIdx.x;
@@ -614,10 +627,12 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
                 a = (int32_t)(key >> 32);
                 b = (int32_t)(key & 0xffffffffu);
                 w = ewt[i];
-                int nd = 0;
-                if (atomicExch(seen + a, epoch) != epoch) ++nd;
-                if (atomicExch(seen + b, epoch) != epoch) ++nd;
-                if (nd) atomicAdd(&sc->sinkcount, nd);
+                // labels are cell + 1 of one DEM; basin 0 is counted once per DEM it borders
+                const int d = dem_at(dc, (size_t)(a != 0 ? a : b) - 1);
+                if (a != 0 && atomicExch(seen + a, epoch) != epoch) atomicAdd(&dc.out[d].sinkcount, 1);
+                if (b != 0 && atomicExch(seen + b, epoch) != epoch) atomicAdd(&dc.out[d].sinkcount, 1);
+                if ((a == 0 || b == 0) && atomicExch(&dc.out[d].zero_seen, epoch) != epoch)
+                    atomicAdd(&dc.out[d].sinkcount, 1);
                 if (a != 0) raise[a] = ~0ull;
                 if (b != 0) raise[b] = ~0ull;
             }
@@ -765,12 +780,13 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
 // raise_watershedMFD (newflow.cu:879-894) into the scratch DEM of pass 2.
 __global__ void k_flood_raise(const double* __restrict__ z, const uint8_t* __restrict__ mask,
                               const int32_t* __restrict__ ws, const unsigned long long* __restrict__ raise,
-                              double* __restrict__ zf, ModelConsts k, DevScalars* sc) {
+                              double* __restrict__ zf, ModelConsts k, DevScalars* sc, DemCtx dc) {
     if (sc->sinkcount_pass1 == 0) return;
     const size_t N = (size_t)k.W * k.H;
     for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
         double v = z[c];
-        if (mask[c]) {
+        // a DEM without sinks keeps its DEM: its second pass repeats the first
+        if (mask[c] && dc.out[dem_at(dc, c)].sinkcount_pass1 != 0) {
             const unsigned long long r = raise[ws[c]];
             const unsigned long long kv = dkey(v);
             if (kv != 0 && kv < r) v = dkey_inv(r);  // zs < raise is false for NaN
@@ -782,36 +798,48 @@ __global__ void k_flood_raise(const double* __restrict__ z, const uint8_t* __res
 // Epilogue of cuFlowDirection (routeflow.cu:934-953) and the host outlet check
 // of routeflow.cu:738-741, which the reference applies after its device copy.
 __global__ void k_fd_epilogue(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
-                              const uint8_t* __restrict__ mfd, uint8_t* __restrict__ fd, double* z, ModelConsts k,
-                              DevScalars* sc) {
+                              const uint8_t* __restrict__ mfd, uint8_t* __restrict__ fd, ModelConsts k) {
     const size_t N = (size_t)k.W * k.H;
-    const int outlet = sc->outlet;
     for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
         uint8_t v = sfd[c];
         if (k.flow_type != 0 && mask[c] && mfd[c] != 0) v = mfd[c];
-        if ((int)c == outlet) v = 16;
         fd[c] = v;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (sc->sinkcount_pass1 == 0) sc->sinkcount = 0;
-        const double zo = z[outlet];
-        sc->outlet_z_clim = zo;
-        unsigned long long low = sc->lowest_key;
-        const unsigned long long k1000 = dkey(1000.0);
-        if (low > k1000) low = k1000;
-        if (low < dkey(zo)) z[outlet] = dkey_inv(low) - 0.0001;
     }
 }
 
-__global__ void k_fd_reset(DevScalars* sc) {
-    sc->lowest_key = ~0ull;
-    sc->sink_counter = sc->flat_counter = 0;
-    sc->sinkcount_pass1 = 0;
-    sc->sinkcount = 0;
-    sc->plateau_sweeps = 0;
-    sc->n_cand = 0;
-    sc->n_sinks = 0;
-    sc->n_edges = 0;
+// Per DEM: the outlet flows west (routeflow.cu:953) and testoutletislowest
+// (routeflow.cu:171-199,740-741) lowers it below the lowest cell of the DEM.
+__global__ void k_fd_outlets(uint8_t* __restrict__ fd, double* z, DemCtx dc) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= dc.n || !dc.in[d].active) return;
+    DemOut& o = dc.out[d];
+    const int outlet = o.outlet;
+    fd[outlet] = 16;
+    if (o.sinkcount_pass1 == 0) o.sinkcount = 0;
+    const double zo = z[outlet];
+    o.outlet_z_clim = zo;
+    unsigned long long low = o.lowest_key;
+    const unsigned long long k1000 = dkey(1000.0);
+    if (low > k1000) low = k1000;
+    if (low < dkey(zo)) z[outlet] = dkey_inv(low) - 0.0001;
+}
+
+__global__ void k_fd_reset(DevScalars* sc, DemCtx dc) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d == 0) {
+        sc->sinkcount_pass1 = 0;
+        sc->plateau_sweeps = 0;
+        sc->n_cand = 0;
+        sc->n_sinks = 0;
+        sc->n_edges = 0;
+    }
+    if (d < dc.n) {
+        DemOut& o = dc.out[d];
+        o.lowest_key = ~0ull;
+        o.sink_counter = o.flat_counter = 0;
+        o.sinkcount_pass1 = 0;
+        o.sinkcount = 0;
+    }
 }
 
 __global__ void k_cand_reset(DevScalars* sc) { sc->n_cand = 0; }
@@ -850,7 +878,7 @@ static lem_status direction_pass(const DevState& s, const ModelConsts& k, const 
     const double* zz = pass == 1 ? s.z : s.zf;
     float* slopes = pass == 1 ? s.slopes : nullptr;
     if (pass == 2) LEM_LAUNCH(L, k_cand_reset, 1, 1, s.sc);
-    LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, k, s.sc, pass);
+    LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, k, s.sc, s.dems, pass);
     LEM_LAUNCH(L, k_plateau_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, pass);
     {
         // candidates in list_a; frontiers in list_b and `pending` (an int32 grid unused in this stage)
@@ -875,10 +903,11 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
     const size_t N = (size_t)k.W * k.H;
     const int T = 256, big = 152 * 32;
     lem_status r;
-    LEM_LAUNCH(L, k_fd_reset, 1, 1, s.sc);
+    LEM_LAUNCH(L, k_fd_reset, (s.dems.n + 127) / 128, 128, s.sc, s.dems);
     if ((r = direction_pass(s, k, L, 1)) != LEM_OK) return r;
     // sink flooding on the pass-1 codes
-    LEM_LAUNCH(L, k_flood_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.sfd1, s.ws, s.list_b, s.raise, k, s.sc);
+    LEM_LAUNCH(L, k_flood_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.sfd1, s.ws, s.list_b, s.raise, k, s.sc,
+               s.dems);
     {
         const double* zz = s.z;
         int32_t* ws = s.ws;
@@ -905,7 +934,7 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
     static int32_t epoch = 0;
     ++epoch;
     LEM_LAUNCH(L, k_flood_compact, flat_blocks((size_t)s.ecap, T, big), T, s.ekey, s.ewt, s.ecap, s.edge_a, s.edge_b,
-               s.edge_w, s.raise, s.label_seen, epoch, s.sc);
+               s.edge_w, s.raise, s.label_seen, epoch, s.sc, s.dems);
     {
         const int32_t* ea = s.edge_a;
         const int32_t* eb = s.edge_b;
@@ -919,9 +948,10 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
                         (void*)&cmaxw, (void*)&sc};
         if ((r = coop("k_flood_spill", (const void*)k_flood_spill, s.max_coop_blocks, args, L)) != LEM_OK) return r;
     }
-    LEM_LAUNCH(L, k_flood_raise, flat_blocks(N, T, big), T, s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc);
+    LEM_LAUNCH(L, k_flood_raise, flat_blocks(N, T, big), T, s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc, s.dems);
     if ((r = direction_pass(s, k, L, 2)) != LEM_OK) return r;
-    LEM_LAUNCH(L, k_fd_epilogue, flat_blocks(N, T, big), T, s.mask, s.sfd, s.mfd, s.fd, s.z, k, s.sc);
+    LEM_LAUNCH(L, k_fd_epilogue, flat_blocks(N, T, big), T, s.mask, s.sfd, s.mfd, s.fd, k);
+    LEM_LAUNCH(L, k_fd_outlets, (s.dems.n + 127) / 128, 128, s.fd, s.z, s.dems);
     LEM_CUDA_TRY(cudaGetLastError());
     return LEM_OK;
 }

@@ -27,7 +27,7 @@ constexpr double kMinHeight = 467.228;  // Data.cpp:252
 // Temperature of cell i (tempmat): T - (z - 467.228) * 0.0065 with z the DEM the
 // grids were built from (the initial DEM during run-in, the DEM at the start of
 // the step otherwise; the outlet uses its value before the stage-1 adjustment).
-__device__ __forceinline__ float clim_temp(const ClimateNow& c, const double* z, const double* z_init, size_t i,
+__device__ __forceinline__ float clim_temp(const DemIn& c, const double* z, const double* z_init, size_t i,
                                            int outlet, double outlet_z) {
     double zc = c.from_current_dem ? (((int)i == outlet) ? outlet_z : z[i]) : z_init[i];
     float hi, lo;
@@ -72,16 +72,22 @@ __global__ void __launch_bounds__(256)
               const float* __restrict__ slopes, const float2* __restrict__ fa, const float* __restrict__ fines,
               const float* __restrict__ nut, const float* __restrict__ soilT, const float* __restrict__ stone,
               const float* __restrict__ totB, float* __restrict__ slopeptr, float* __restrict__ ero,
-              float* __restrict__ inci, float* __restrict__ geli, ModelConsts k, ClimateNow c, DevScalars* sc) {
+              float* __restrict__ inci, float* __restrict__ geli, const int32_t* __restrict__ chunk_start,
+              ModelConsts k, DemCtx dc) {
     __shared__ double red[8];
     __shared__ unsigned long long redk[8];
-    const size_t N = (size_t)k.W * k.H;
-    const int outlet = sc->outlet;
-    const double outlet_z = sc->outlet_z_clim;
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->base_level = z[outlet] - 0.00012;  // updates.cu:151
+    const Chunk ch = chunk_of(chunk_start, dc.n, dc.in);
+    const DemIn& c = dc.in[ch.d];
+    DemOut& o = dc.out[ch.d];
+    const int W = k.W;
+    const int outlet = o.outlet;
+    const double outlet_z = o.outlet_z_clim;
+    if (ch.first == 0 && threadIdx.x == 0) o.base_level = z[outlet] - 0.00012;  // updates.cu:151
     float se = 0.f, si = 0.f, sg = 0.f;
     unsigned long long famax = 0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+    for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
+        int x, y;
+        const size_t i = region_cell(c, ri, W, &x, &y);
         const float2 f2 = fa[i];
         const unsigned long long fk = ffkey(f2);
         if (f2.x == f2.x) famax = fk > famax ? fk : famax;  // the reduction skips NaN (thrust::maximum order)
@@ -174,10 +180,10 @@ __global__ void __launch_bounds__(256)
     const double tg = block_sum_d(sg, red);
     const unsigned long long fm = block_max_u64(famax, redk);
     if (threadIdx.x == 0) {
-        atomicAdd(&sc->tot_e, te);
-        atomicAdd(&sc->tot_i, ti);
-        atomicAdd(&sc->tot_g, tg);
-        atomicMax(&sc->fa_max_key, fm);
+        atomicAdd(&o.tot_e, te);
+        atomicAdd(&o.tot_i, ti);
+        atomicAdd(&o.tot_g, tg);
+        atomicMax(&o.fa_max_key, fm);
     }
 }
 
@@ -279,9 +285,11 @@ struct SedCell {
     float* stone;
     float* fines;
     float* soilT;
+    DemCtx dc;
     int W, H;
     float ddk, dck, dgk;
     __device__ __forceinline__ void cell(int32_t cur, int x, int y) const {
+        if (dc.of) atomicAdd(&dc.out[dc.of[cur]].sed_done, 1);  // a batch: count per DEM
         const float omd = 1.0f - ddk, omc = 1.0f - dck, omg = 1.0f - dgk;
         float ad = 0.f, ac = 0.f, ag = 0.f, from = 0.f;
 #pragma unroll
@@ -312,12 +320,12 @@ __global__ void k_sed_walk(const uint8_t* __restrict__ mask, const uint8_t* __re
                            const float* __restrict__ prop, const float* __restrict__ ero,
                            const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
                            float* fines, float* soilT, int32_t* pending, int32_t* list_a, int32_t* list_b,
-                           ModelConsts k, DevScalars* sc, int gate) {
+                           ModelConsts k, DevScalars* sc, DemCtx dc, int gate) {
     if (gate && sc->sed_tiled_ok) return;
-    const SedCell op{mask, fd, prop, ero, inci, geli, depo, stone, fines, soilT, k.W, k.H, k.ddk, k.dck, k.dgk};
+    const SedCell op{mask, fd, prop, ero, inci, geli, depo, stone, fines, soilT, dc, k.W, k.H, k.ddk, k.dck, k.dgk};
     int done = wave_walk(op, pending, list_a, list_b, k.W, k.H, sc);
     done = wsum(done);
-    if ((threadIdx.x & 31) == 0 && done) atomicAdd(&sc->sed_done, done);
+    if (!dc.of && (threadIdx.x & 31) == 0 && done) atomicAdd(&dc.out[0].sed_done, done);
 }
 
 // ---------------------------------------------------------------------------
@@ -433,7 +441,7 @@ __global__ void __launch_bounds__(256)
                  float* fines, float* soilT, int32_t* __restrict__ t_dst, int32_t* __restrict__ t_pend,
                  int32_t* __restrict__ t_orng, float2* __restrict__ t_out, float4* __restrict__ p_abc,
                  int32_t* __restrict__ p_ref, float4* __restrict__ p_map, uint8_t* __restrict__ t_stat,
-                 int32_t* srcs, ModelConsts k, DevScalars* sc) {
+                 int32_t* srcs, ModelConsts k, DevScalars* sc, DemCtx dc) {
     if (!sc->sed_tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -456,7 +464,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int32_t s_pcnt[kTileEnt];
     __shared__ int16_t s_pstart[kTileEnt];
     __shared__ int16_t s_pfill[kTileEnt];
-    __shared__ int s_no, s_nt, s_done, s_pool;
+    __shared__ int s_no, s_nt, s_done, s_pool, s_dem;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = blockIdx.x;
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
@@ -465,7 +473,7 @@ __global__ void __launch_bounds__(256)
         s_ocnt[threadIdx.x] = 0;
         s_pcnt[threadIdx.x] = 0;
     }
-    if (threadIdx.x == 0) s_nt = s_done = 0;
+    if (threadIdx.x == 0) s_nt = s_done = 0, s_dem = -1;
     __syncthreads();
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     bool src[4];
@@ -486,6 +494,7 @@ __global__ void __launch_bounds__(256)
             stn = in.L.stn;
             nz = in.L.nz;
             snew = __ldcg(stone + (size_t)(ty0 + ly) * W + tx0 + lx);
+            atomicMax(&s_dem, dem_at(dc, (size_t)(ty0 + ly) * W + tx0 + lx));  // one DEM per tile
             const int d = bit_dir(s_code[hc]);
             if (d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn) {
                 const int rlx = lx + dir_dx(d), rly = ly + dir_dy(d);
@@ -755,7 +764,7 @@ __global__ void __launch_bounds__(256)
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();
-    if (threadIdx.x == 0 && s_done) atomicAdd(&sc->sed_done, s_done);
+    if (threadIdx.x == 0 && s_done && s_dem >= 0) atomicAdd(&dc.out[s_dem].sed_done, s_done);
 }
 
 // One outlet of the coarse sediment wave: its program, then its own stores.
@@ -843,7 +852,7 @@ __global__ void __launch_bounds__(256)
     k_sedt_final(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd, const float* __restrict__ ero,
                  const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
                  float* fines, float* soilT, const int32_t* __restrict__ t_pend, const uint8_t* __restrict__ t_stat,
-                 ModelConsts k, DevScalars* sc) {
+                 ModelConsts k, DevScalars* sc, DemCtx dc) {
     if (!sc->sed_tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -852,7 +861,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int32_t s_pend[kTile * kTile];
     __shared__ float s_new[kTile * kTile];
     __shared__ uint8_t s_stat[kTile * kTile];
-    __shared__ int s_done;
+    __shared__ int s_done, s_dem;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = blockIdx.x;
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
@@ -870,7 +879,7 @@ __global__ void __launch_bounds__(256)
         s_hok[h] = ok;
         s_hval[h] = v;
     }
-    if (threadIdx.x == 0) s_done = 0;
+    if (threadIdx.x == 0) s_done = 0, s_dem = -1;
     __syncthreads();
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     int done = 0;
@@ -907,6 +916,7 @@ __global__ void __launch_bounds__(256)
             }
             st = t_stat[g];
             v = __ldcg(stone + g);
+            atomicMax(&s_dem, dem_at(dc, g));  // one DEM per tile
         }
         s_pend[l] = pend;
         s_stat[l] = st;
@@ -954,7 +964,7 @@ __global__ void __launch_bounds__(256)
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();
-    if (threadIdx.x == 0 && s_done) atomicAdd(&sc->sed_done, s_done);
+    if (threadIdx.x == 0 && s_done && s_dem >= 0) atomicAdd(&dc.out[s_dem].sed_done, s_done);
 }
 
 __device__ __forceinline__ float dreybrodt(const float* tab, float T) {
@@ -971,18 +981,22 @@ __global__ void __launch_bounds__(256)
             const float* __restrict__ geli, const float* __restrict__ depo, float* __restrict__ soilT,
             float* __restrict__ stone, float* __restrict__ fines, float* __restrict__ soilM,
             float* __restrict__ soilB, float* __restrict__ nut, float* __restrict__ totB, float* __restrict__ dz_out,
-            float* __restrict__ wc_out, float* __restrict__ wp_out, const float* __restrict__ tab, ModelConsts k,
-            ClimateNow c, DevScalars* sc) {
+            float* __restrict__ wc_out, float* __restrict__ wp_out, const float* __restrict__ tab,
+            const int32_t* __restrict__ chunk_start, ModelConsts k, DemCtx dc) {
     __shared__ double red[8];
     const int W = k.W;
-    const size_t N = (size_t)W * k.H;
-    const int outlet = sc->outlet;
-    const double outlet_z = sc->outlet_z_clim;
-    const double base = sc->base_level;
+    const Chunk ch = chunk_of(chunk_start, dc.n, dc.in);
+    const DemIn& c = dc.in[ch.d];
+    DemOut& o = dc.out[ch.d];
+    const int outlet = o.outlet;
+    const double outlet_z = o.outlet_z_clim;
+    const double base = o.base_level;
     const float rain0 = (float)c.rain, rinc = (float)c.rain_inc;
     const float dtemp_scalar = (float)(c.temp - c.temp0);
     float swc = 0.f, swp = 0.f, sbio = 0.f, sd = 0.f;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+    for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
+        int x, y;
+        const size_t i = region_cell(c, ri, W, &x, &y);
         sd += depo[i];
         if (!mask[i]) {
             totB[i] = 0.0f;  // grow_vegetation (updates.cu:102-105)
@@ -993,7 +1007,6 @@ __global__ void __launch_bounds__(256)
             }
             continue;
         }
-        const int y = (int)(i / W);
         const float e = ero[i];
         const float dz = depo[i] - e - inci[i] - geli[i];  // surface_change (eroincidep.cu:404)
         const double zold = z[i];
@@ -1001,7 +1014,7 @@ __global__ void __launch_bounds__(256)
         float zch, zcl;
         dsplit(zc, zch, zcl);
         const float T = (float)c.temp - ((zch - (float)kMinHeight) + zcl) * 0.0065f;
-        const float rain = rain0 + (float)y * rinc;
+        const float rain = rain0 + (float)(y - c.y0) * rinc;
         const float2 f2 = fa[i];
         const float fav = f2.x + f2.y;
         // weathering type 1 (eroincidep.cu:220-327)
@@ -1111,41 +1124,46 @@ __global__ void __launch_bounds__(256)
     const double t3 = block_sum_d(sbio, red);
     const double t4 = block_sum_d(sd, red);
     if (threadIdx.x == 0) {
-        atomicAdd(&sc->tot_wc, t1);
-        atomicAdd(&sc->tot_wp, t2);
-        atomicAdd(&sc->tot_bio, t3);
-        atomicAdd(&sc->tot_d, t4);
+        atomicAdd(&o.tot_wc, t1);
+        atomicAdd(&o.tot_wp, t2);
+        atomicAdd(&o.tot_bio, t3);
+        atomicAdd(&o.tot_d, t4);
     }
 }
 
-__global__ void k_mod_reset(DevScalars* sc, int tiled) {
-    sc->counters[0] = 0;
-    sc->sed_done = 0;
-    sc->sed_tiled_ok = tiled;
-    sc->tile_src = 0;
-    sc->tot_e = sc->tot_i = sc->tot_g = sc->tot_d = sc->tot_wc = sc->tot_wp = sc->tot_bio = 0.0;
-    sc->fa_max_key = 0ull;
+__global__ void k_mod_reset(DevScalars* sc, DemCtx dc, int tiled) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d == 0) {
+        sc->counters[0] = 0;
+        sc->sed_tiled_ok = tiled;
+        sc->tile_src = 0;
+    }
+    if (d < dc.n) {
+        DemOut& o = dc.out[d];
+        o.sed_done = 0;
+        o.tot_e = o.tot_i = o.tot_g = o.tot_d = o.tot_wc = o.tot_wp = o.tot_bio = 0.0;
+        o.fa_max_key = 0ull;
+    }
 }
 
 }  // namespace
 
-lem_status launch_erosion(const DevState& s, const ModelConsts& k, const ClimateNow& c, uint32_t flags,
-                          const Launch& L) {
+lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flags, const Launch& L) {
     const size_t N = (size_t)k.W * k.H;
     const int T = 256;
     size_t nb = (N + T - 1) / T;
     const int blocks = (int)(nb > 152 * 32 ? 152 * 32 : nb);
     const float* prop = (k.flow_type != 0 && k.mfd_props) ? s.prop : nullptr;
     const int tiled = (k.flow_type == 0 && !prop) ? 1 : 0;
-    LEM_LAUNCH(L, k_mod_reset, 1, 1, s.sc, tiled);
-    LEM_LAUNCH(L, k_erosion, blocks, T, s.z, s.z_init, s.mask, s.slopes, s.fa, s.fines, s.nut, s.soilT, s.stone,
-               s.totB, s.slopeptr, s.ero, s.inci, s.geli, k, c, s.sc);
+    LEM_LAUNCH(L, k_mod_reset, (s.dems.n + 127) / 128, 128, s.sc, s.dems, tiled);
+    LEM_LAUNCH(L, k_erosion, s.n_chunks, T, s.z, s.z_init, s.mask, s.slopes, s.fa, s.fines, s.nut, s.soilT, s.stone,
+               s.totB, s.slopeptr, s.ero, s.inci, s.geli, s.chunk_start, k, s.dems);
     LEM_LAUNCH(L, k_sed_prep, blocks, T, s.mask, s.fd, s.depo, s.pending, s.list_a, k, s.sc);
     if (tiled) {
         const int tiles = ((k.W + kTile - 1) / kTile) * ((k.H + kTile - 1) / kTile);
         LEM_LAUNCH(L, k_sedt_local, tiles, 256, s.mask, s.fd, s.ero, s.inci, s.geli, s.depo, s.stone, s.fines,
                    s.soilT, s.t_dst, s.t_pend, s.t_orng, s.t_la, s.p_abc, s.p_ref, s.p_map, s.t_stat, s.list_b, k,
-                   s.sc);
+                   s.sc, s.dems);
         const uint8_t* fd = s.fd;
         const int32_t* torng = s.t_orng;
         const int32_t* tdst = s.t_dst;
@@ -1171,7 +1189,7 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, const Climate
                                                  args, 0, L.st));
         L.post();
         LEM_LAUNCH(L, k_sedt_final, tiles, 256, s.mask, s.fd, s.ero, s.inci, s.geli, s.depo, s.stone, s.fines,
-                   s.soilT, s.t_pend, s.t_stat, k, s.sc);
+                   s.soilT, s.t_pend, s.t_stat, k, s.sc, s.dems);
     }
     {
         const uint8_t* mask = s.mask;
@@ -1188,19 +1206,21 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, const Climate
         int32_t* lb = s.list_b;
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
+        DemCtx dc = s.dems;
         int gate = tiled;
         void* args[] = {(void*)&mask, (void*)&fd,    (void*)&prop,  (void*)&ero,     (void*)&inci,
                         (void*)&geli, (void*)&depo,  (void*)&stone, (void*)&fines,   (void*)&soilT,
-                        (void*)&pending, (void*)&la, (void*)&lb,    (void*)&kk,      (void*)&sc, (void*)&gate};
+                        (void*)&pending, (void*)&la, (void*)&lb,    (void*)&kk,      (void*)&sc, (void*)&dc,
+                        (void*)&gate};
         L.pre("k_sed_walk");
         LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sed_walk, dim3(s.max_coop_blocks), dim3(256), args,
                                                  0, L.st));
         L.post();
     }
     const bool diag = (flags & LEM_STEP_KEEP_DIAGNOSTICS) != 0;
-    LEM_LAUNCH(L, k_final, blocks, T, s.z, s.z_init, s.mask, s.fa, s.ero, s.inci, s.geli, s.depo, s.soilT, s.stone,
-               s.fines, s.soilM, s.soilB, s.nut, s.totB, diag ? s.dz : nullptr, diag ? s.wc : nullptr,
-               diag ? s.wp : nullptr, s.temp_tab, k, c, s.sc);
+    LEM_LAUNCH(L, k_final, s.n_chunks, T, s.z, s.z_init, s.mask, s.fa, s.ero, s.inci, s.geli, s.depo, s.soilT,
+               s.stone, s.fines, s.soilM, s.soilB, s.nut, s.totB, diag ? s.dz : nullptr, diag ? s.wc : nullptr,
+               diag ? s.wp : nullptr, s.temp_tab, s.chunk_start, k, s.dems);
     LEM_CUDA_TRY(cudaGetLastError());
     return LEM_OK;
 }

@@ -100,6 +100,17 @@ SIGNATURES = {
     "lem_profile_read": (C.c_int, [_H, C.POINTER(KernelStat), C.c_int32, C.POINTER(C.c_int32)]),
     "lem_accumulate_flow_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                               C.c_int32, C.c_void_p]),
+    "lem_create_batch": (C.c_int, [C.POINTER(GridDesc), C.POINTER(Params), C.c_int32, C.POINTER(_H)]),
+    "lem_dem_add": (C.c_int, [_H, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_double, C.c_double,
+                              C.POINTER(C.c_int32)]),
+    "lem_dem_remove": (C.c_int, [_H, C.c_int32]),
+    "lem_dem_set_field": (C.c_int, [_H, C.c_int32, C.c_int, C.c_void_p]),
+    "lem_dem_get_field": (C.c_int, [_H, C.c_int32, C.c_int, C.c_void_p]),
+    "lem_dem_set_outlet": (C.c_int, [_H, C.c_int32, C.c_int32]),
+    "lem_dem_set_climate": (C.c_int, [_H, C.c_int32, C.POINTER(Climate)]),
+    "lem_dem_set_step_flags": (C.c_int, [_H, C.c_int32, C.c_uint32]),
+    "lem_dem_get_totals": (C.c_int, [_H, C.c_int32, C.POINTER(Totals)]),
+    "lem_step_batch": (C.c_int, [_H, C.c_uint32]),
 }
 
 _lib = None
@@ -238,3 +249,131 @@ class Model:
 
 def select_device(device: int):
     _check(load().lem_select_device(int(device)), "lem_select_device")
+
+
+class Batch:
+    """Many DEMs stepped together (lem_create_batch): one canvas grid, each DEM
+    in its own 32-aligned region with its own outlet, climate and totals.  One
+    step runs every active DEM with one launch per kernel."""
+
+    def __init__(self, width: int, height: int, cellsize: float, max_dems: int = 256,
+                 params: Params | None = None):
+        from .packing import TilePacker
+        L = load()
+        self.W, self.H = int(width), int(height)
+        self.params = params if params is not None else make_params()
+        h = _H()
+        _check(L.lem_create_batch(C.byref(GridDesc(self.W, self.H, float(cellsize))), C.byref(self.params),
+                                  int(max_dems), C.byref(h)), "lem_create_batch")
+        self.h = h
+        self.packer = TilePacker(self.W, self.H)
+        self.shape = {}   # id -> (height, width)
+        self.place = {}   # id -> region handle of the packer
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().lem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, dem: np.ndarray, init_rain: float, init_temp: float, at: tuple | None = None) -> int:
+        """Places the DEM (first fit unless `at` = (x0, y0)) and uploads it; None when it does not fit."""
+        hgt, wid = dem.shape
+        if at is None:
+            r = self.packer.alloc(wid, hgt)
+            if r is None:
+                return None
+            x0, y0 = r[0], r[1]
+        else:
+            x0, y0 = at
+            r = self.packer.take(x0, y0, wid, hgt)
+        a = np.ascontiguousarray(dem, dtype=np.float64)
+        i = C.c_int32()
+        code = load().lem_dem_add(self.h, x0, y0, wid, hgt, a.ctypes.data, float(init_rain), float(init_temp),
+                                  C.byref(i))
+        if code != 0:
+            self.packer.free(r)
+            _check(code, "lem_dem_add")
+        self.shape[i.value] = (hgt, wid)
+        self.place[i.value] = r
+        return i.value
+
+    def remove(self, i: int):
+        _check(load().lem_dem_remove(self.h, i), "lem_dem_remove")
+        self.packer.free(self.place.pop(i))
+        self.shape.pop(i)
+
+    def set(self, i: int, name: str, arr: np.ndarray):
+        hgt, wid = self.shape[i]
+        n = 8 * hgt * wid if name == "slopes" else hgt * wid
+        a = np.ascontiguousarray(arr, dtype=np.int32 if name in INT_FIELDS else np.float64).reshape(-1)
+        if a.size != n:
+            raise ValueError(f"{name}: expected {n} values, got {a.size}")
+        _check(load().lem_dem_set_field(self.h, i, FIELDS[name], a.ctypes.data), f"lem_dem_set_field({name})")
+
+    def get(self, i: int, name: str) -> np.ndarray:
+        hgt, wid = self.shape[i]
+        if name in INT_FIELDS:
+            out = np.empty((hgt, wid), np.int32)
+        elif name == "slopes":
+            out = np.empty((hgt, wid, 8), np.float64)
+        else:
+            out = np.empty((hgt, wid), np.float64)
+        _check(load().lem_dem_get_field(self.h, i, FIELDS[name], out.ctypes.data), f"lem_dem_get_field({name})")
+        return out
+
+    def set_state(self, i: int, state: dict):
+        for f in STATE_FIELDS:
+            if f in state:
+                self.set(i, f, state[f])
+        if "slopes" in state:
+            self.set(i, "slopes", state["slopes"])
+        _check(load().lem_dem_set_outlet(self.h, i, int(state["outlet"])), "lem_dem_set_outlet")
+
+    def set_climate(self, i: int, rain: float, temp: float, recompute: bool):
+        _check(load().lem_dem_set_climate(self.h, i, C.byref(Climate(rain, temp, int(bool(recompute))))),
+               "lem_dem_set_climate")
+
+    def set_step_flags(self, i: int, flags: int):
+        _check(load().lem_dem_set_step_flags(self.h, i, int(flags)), "lem_dem_set_step_flags")
+
+    def step(self, flags: int = 0):
+        _check(load().lem_step_batch(self.h, int(flags)), "lem_step_batch")
+
+    def synchronize(self):
+        _check(load().lem_synchronize(self.h), "lem_synchronize")
+
+    def totals(self, i: int) -> dict:
+        t = Totals()
+        _check(load().lem_dem_get_totals(self.h, i, C.byref(t)), "lem_dem_get_totals")
+        return {k: getattr(t, k) for k, _ in Totals._fields_}
+
+    @property
+    def stream(self) -> int:
+        return int(load().lem_stream(self.h) or 0)
+
+    @property
+    def launches(self) -> int:
+        return int(load().lem_launch_count(self.h))
+
+    def record(self, slot: int):
+        _check(load().lem_event_record(self.h, slot), "lem_event_record")
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        _check(load().lem_event_elapsed(self.h, a, b, C.byref(ms)), "lem_event_elapsed")
+        return float(ms.value)
+
+    def profiling(self, on: bool):
+        _check(load().lem_set_profiling(self.h, int(bool(on))), "lem_set_profiling")
+
+    def profile(self) -> dict:
+        arr = (KernelStat * 64)()
+        n = C.c_int32()
+        _check(load().lem_profile_read(self.h, arr, 64, C.byref(n)), "lem_profile_read")
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(min(n.value, 64))}
