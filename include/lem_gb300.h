@@ -100,6 +100,10 @@ typedef struct lem_totals {
     int32_t flood_edges;     /* distinct basin pairs of the sink flooding    */
     int32_t fa_uncomputed;   /* masked-in cells left out of accumulation     */
     int32_t sed_uncomputed;  /* masked-in cells left out of sediment routing */
+    int32_t merge_rounds;    /* sink flooding: rounds of the equal-height label merge   */
+    int32_t label_rounds;    /*   rounds of the basin labelling (pointer jumping)       */
+    int32_t spill_rounds;    /*   rounds of the minimax spill relaxation                */
+    int32_t pad;
 } lem_totals;
 
 /* Grid fields.  Element type per field: D = double[W*H], I = int32[W*H],
@@ -237,6 +241,19 @@ lem_status lem_dem_set_step_flags(lem_handle* h, int32_t id, uint32_t flags);
 lem_status lem_dem_get_totals(lem_handle* h, int32_t id, lem_totals* out);  /* synchronous */
 /* One timestep of every active DEM; flags as lem_step, for all DEMs. */
 lem_status lem_step_batch(lem_handle* h, uint32_t flags);
+
+/* Restart snapshot of one DEM's resident state: the DEM, the DEM of the
+ * initial climate grids, the mask, the persistent slopes (whose stale entries
+ * the next steps read), the seven soil and vegetation fields, the outlet and
+ * the climate scalars -- what the reference's restart rereads
+ * (retriveProcessMatrices, MEM_kernels/ioGDAL.cpp:662+), as one binary block
+ * instead of rasters.  id: 0 for a single-grid handle, a DEM of a batch.
+ * Loading needs a DEM of the same size (a new single-grid handle may load
+ * before any lem_set_field); the steps after a load equal the steps after the
+ * save. */
+size_t lem_snapshot_bytes(lem_handle* h, int32_t id);
+lem_status lem_snapshot_save(lem_handle* h, int32_t id, void* host, size_t bytes);
+lem_status lem_snapshot_load(lem_handle* h, int32_t id, const void* host, size_t bytes);
 
 /* Flow accumulation that allocates nothing.  No counterpart in the reference:
  * it serves callers that must not allocate device memory themselves or through

@@ -433,6 +433,9 @@ lem_status totals_of(lem_handle* h, int id, lem_totals* o) {
     o->flood_edges = g.n_edges;
     o->fa_uncomputed = d.n_active - d.fa_done;
     o->sed_uncomputed = d.n_active - d.sed_done;
+    o->merge_rounds = g.flood_sweeps;
+    o->label_rounds = g.label_rounds;
+    o->spill_rounds = g.spill_rounds;
     return LEM_OK;
 }
 
@@ -890,6 +893,124 @@ lem_status lem_dem_get_totals(lem_handle* h, int32_t id, lem_totals* out) {
     if (r != LEM_OK) return r;
     if (!out) return LEM_ERR_INVALID;
     return totals_of(h, id, out);
+}
+
+// ---- restart snapshots of one DEM's resident state
+
+namespace {
+struct SnapHeader {
+    uint32_t magic, version;
+    int32_t w, h;
+    double rain, temp, rain0, temp0;
+    int32_t from_current, outlet;  // outlet: index of the DEM's own grid
+    uint32_t pad[2];
+};
+constexpr uint32_t kSnapMagic = 0x534d454cu;  // "LEMS"
+struct SnapField {
+    void* dev;
+    size_t elem;  // bytes per cell
+};
+void snap_fields(lem_handle* h, SnapField* f) {
+    DevState& s = h->s;
+    f[0] = {s.z, 8};
+    f[1] = {s.z_init, 8};
+    f[2] = {s.mask, 1};
+    f[3] = {s.slopes, 32};
+    f[4] = {s.stone, 4};
+    f[5] = {s.fines, 4};
+    f[6] = {s.soilT, 4};
+    f[7] = {s.soilM, 4};
+    f[8] = {s.soilB, 4};
+    f[9] = {s.nut, 4};
+    f[10] = {s.totB, 4};
+}
+constexpr int kSnapFields = 11;
+size_t snap_bytes(const HostDem& r) { return sizeof(SnapHeader) + (size_t)r.w * r.h * (8 + 8 + 1 + 32 + 7 * 4); }
+lem_status snap_target(lem_handle* h, int32_t id, HostDem** r) {
+    if (!h) return LEM_ERR_INVALID;
+    if (h->batch) {
+        lem_status st = dem_check(h, id);
+        if (st != LEM_OK) return st;
+    } else if (id != 0) {
+        return LEM_ERR_INVALID;
+    }
+    *r = &h->dems[id];
+    return LEM_OK;
+}
+}  // namespace
+
+size_t lem_snapshot_bytes(lem_handle* h, int32_t id) {
+    HostDem* r = nullptr;
+    if (snap_target(h, id, &r) != LEM_OK) return 0;
+    return snap_bytes(*r);
+}
+
+lem_status lem_snapshot_save(lem_handle* h, int32_t id, void* host, size_t bytes) {
+    HostDem* r = nullptr;
+    lem_status st = snap_target(h, id, &r);
+    if (st != LEM_OK) return st;
+    if (!host || bytes < snap_bytes(*r)) return LEM_ERR_INVALID;
+    if (!h->batch && !h->dem_set) return LEM_ERR_STATE;
+    if ((st = sync_scalars(h)) != LEM_OK) return st;
+    SnapHeader hd{};
+    hd.magic = kSnapMagic;
+    hd.version = 1;
+    hd.w = r->w;
+    hd.h = r->h;
+    hd.rain = r->rain;
+    hd.temp = r->temp;
+    hd.rain0 = r->rain0;
+    hd.temp0 = r->temp0;
+    hd.from_current = r->from_current ? 1 : 0;
+    const int64_t o = h->host_out[id].outlet;
+    hd.outlet = (int32_t)((o / h->k.W - r->y0) * r->w + (o % h->k.W - r->x0));
+    unsigned char* p = static_cast<unsigned char*>(host);
+    std::memcpy(p, &hd, sizeof hd);
+    p += sizeof hd;
+    SnapField f[kSnapFields];
+    snap_fields(h, f);
+    const size_t W = (size_t)h->k.W, off = (size_t)r->y0 * W + r->x0;
+    for (const SnapField& q : f) {
+        const unsigned char* src = static_cast<const unsigned char*>(q.dev) + off * q.elem;
+        LEM_CUDA_TRY(cudaMemcpy2D(p, r->w * q.elem, src, W * q.elem, r->w * q.elem, r->h, cudaMemcpyDeviceToHost));
+        p += (size_t)r->w * r->h * q.elem;
+    }
+    return LEM_OK;
+}
+
+lem_status lem_snapshot_load(lem_handle* h, int32_t id, const void* host, size_t bytes) {
+    HostDem* r = nullptr;
+    lem_status st = snap_target(h, id, &r);
+    if (st != LEM_OK) return st;
+    if (!host || bytes < sizeof(SnapHeader)) return LEM_ERR_INVALID;
+    SnapHeader hd;
+    std::memcpy(&hd, host, sizeof hd);
+    if (hd.magic != kSnapMagic || hd.version != 1 || hd.w != r->w || hd.h != r->h || bytes < snap_bytes(*r) ||
+        hd.outlet < 0 || hd.outlet >= r->w * r->h)
+        return LEM_ERR_INVALID;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    const unsigned char* p = static_cast<const unsigned char*>(host) + sizeof hd;
+    SnapField f[kSnapFields];
+    snap_fields(h, f);
+    const size_t W = (size_t)h->k.W, off = (size_t)r->y0 * W + r->x0;
+    for (const SnapField& q : f) {
+        unsigned char* dst = static_cast<unsigned char*>(q.dev) + off * q.elem;
+        LEM_CUDA_TRY(cudaMemcpy2D(dst, W * q.elem, p, r->w * q.elem, r->w * q.elem, r->h, cudaMemcpyHostToDevice));
+        p += (size_t)r->w * r->h * q.elem;
+    }
+    r->rain = hd.rain;
+    r->temp = hd.temp;
+    r->rain0 = hd.rain0;
+    r->temp0 = hd.temp0;
+    r->from_current = hd.from_current != 0;
+    const int32_t g = (r->y0 + hd.outlet / r->w) * h->k.W + r->x0 + hd.outlet % r->w;
+    LEM_CUDA_TRY(cudaMemcpy(&h->dem_out[id].outlet, &g, sizeof g, cudaMemcpyHostToDevice));
+    r->outlet_set = true;
+    if (!h->batch) {
+        h->dem_set = true;
+        r->active = true;
+    }
+    return LEM_OK;
 }
 
 lem_status lem_step_batch(lem_handle* h, uint32_t flags) {

@@ -620,6 +620,7 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
         bool has = false;
         int32_t a = 0, b = 0;
         unsigned long long w = 0;
+        int d = -1, nd = 0;
         if (i < (size_t)cap) {
             const unsigned long long key = ekey[i];
             if (key != ~0ull) {
@@ -628,15 +629,20 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
                 b = (int32_t)(key & 0xffffffffu);
                 w = ewt[i];
                 // labels are cell + 1 of one DEM; basin 0 is counted once per DEM it borders
-                const int d = dem_at(dc, (size_t)(a != 0 ? a : b) - 1);
-                if (a != 0 && atomicExch(seen + a, epoch) != epoch) atomicAdd(&dc.out[d].sinkcount, 1);
-                if (b != 0 && atomicExch(seen + b, epoch) != epoch) atomicAdd(&dc.out[d].sinkcount, 1);
-                if ((a == 0 || b == 0) && atomicExch(&dc.out[d].zero_seen, epoch) != epoch)
-                    atomicAdd(&dc.out[d].sinkcount, 1);
+                d = dem_at(dc, (size_t)(a != 0 ? a : b) - 1);
+                if (a != 0 && atomicExch(seen + a, epoch) != epoch) ++nd;
+                if (b != 0 && atomicExch(seen + b, epoch) != epoch) ++nd;
+                if ((a == 0 || b == 0) && *((volatile int32_t*)&dc.out[d].zero_seen) != epoch &&
+                    atomicExch(&dc.out[d].zero_seen, epoch) != epoch)
+                    ++nd;
                 if (a != 0) raise[a] = ~0ull;
                 if (b != 0) raise[b] = ~0ull;
             }
         }
+        // one atomic per DEM and warp for the label counts
+        const unsigned grp = __match_any_sync(0xffffffffu, nd ? d : -1);
+        const int gsum = __reduce_add_sync(grp, nd);
+        if (nd && (grp & ((1u << (threadIdx.x & 31)) - 1)) == 0) atomicAdd(&dc.out[d].sinkcount, gsum);
         unsigned ballot = __ballot_sync(0xffffffffu, has);
         if (!ballot) continue;
         const int lane = threadIdx.x & 31, leader = __ffs(ballot) - 1;
@@ -828,6 +834,7 @@ __global__ void k_fd_reset(DevScalars* sc, DemCtx dc) {
     const int d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d == 0) {
         sc->sinkcount_pass1 = 0;
+        sc->flood_sweeps = sc->label_rounds = sc->spill_rounds = 0;
         sc->plateau_sweeps = 0;
         sc->n_cand = 0;
         sc->n_sinks = 0;

@@ -68,6 +68,7 @@ class Totals(C.Structure):
         ("sinkcount", C.c_int32), ("outlet", C.c_int32), ("initial_sinks", C.c_int32),
         ("initial_flats", C.c_int32), ("plateau_sweeps", C.c_int32), ("flood_edges", C.c_int32),
         ("fa_uncomputed", C.c_int32), ("sed_uncomputed", C.c_int32),
+        ("merge_rounds", C.c_int32), ("label_rounds", C.c_int32), ("spill_rounds", C.c_int32), ("pad", C.c_int32),
     ]
 
 
@@ -111,7 +112,26 @@ SIGNATURES = {
     "lem_dem_set_step_flags": (C.c_int, [_H, C.c_int32, C.c_uint32]),
     "lem_dem_get_totals": (C.c_int, [_H, C.c_int32, C.POINTER(Totals)]),
     "lem_step_batch": (C.c_int, [_H, C.c_uint32]),
+    "lem_snapshot_bytes": (C.c_size_t, [_H, C.c_int32]),
+    "lem_snapshot_save": (C.c_int, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
+    "lem_snapshot_load": (C.c_int, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
 }
+
+
+def snapshot_save(h, i: int = 0) -> bytes:
+    """The restart snapshot of DEM `i` of handle `h` (0 for a single grid)."""
+    L = load()
+    n = int(L.lem_snapshot_bytes(h, i))
+    if n == 0:
+        raise LemError(1, "lem_snapshot_bytes")
+    buf = (C.c_char * n)()
+    _check(L.lem_snapshot_save(h, i, buf, n), "lem_snapshot_save")
+    return bytes(buf)
+
+
+def snapshot_load(h, data: bytes, i: int = 0):
+    buf = (C.c_char * len(data)).from_buffer_copy(data)
+    _check(load().lem_snapshot_load(h, i, buf, len(data)), "lem_snapshot_load")
 
 _lib = None
 
@@ -147,7 +167,7 @@ class Model:
     """One DEM and its model state resident on the current CUDA device."""
 
     def __init__(self, dem: np.ndarray, cellsize: float, init_rain: float, init_temp: float,
-                 params: Params | None = None):
+                 params: Params | None = None, upload: bool = True):
         L = load()
         self.H, self.W = dem.shape
         self.N = self.H * self.W
@@ -156,7 +176,14 @@ class Model:
         _check(L.lem_create(C.byref(GridDesc(self.W, self.H, float(cellsize))), C.byref(self.params),
                             float(init_rain), float(init_temp), C.byref(h)), "lem_create")
         self.h = h
-        self.set("dem", dem)
+        if upload:
+            self.set("dem", dem)
+
+    def snapshot(self) -> bytes:
+        return snapshot_save(self.h, 0)
+
+    def restore(self, data: bytes):
+        snapshot_load(self.h, data, 0)
 
     def close(self):
         if getattr(self, "h", None):
@@ -347,6 +374,12 @@ class Batch:
 
     def synchronize(self):
         _check(load().lem_synchronize(self.h), "lem_synchronize")
+
+    def snapshot(self, i: int) -> bytes:
+        return snapshot_save(self.h, i)
+
+    def restore(self, i: int, data: bytes):
+        snapshot_load(self.h, data, i)
 
     def totals(self, i: int) -> dict:
         t = Totals()

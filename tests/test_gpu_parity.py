@@ -260,3 +260,72 @@ def test_full_size_invariants_4096(libs):
     ero = g.get("ero")
     assert abs(t["tot_e"] - ero.sum()) <= 1e-5 * abs(ero.sum())
     assert np.isfinite(g.get("dem")[mask]).all()
+
+
+def test_full_size_tiled_waves_4096(libs):
+    """One C2 step at 4096x4096 on the tiled waves (no contributing counts): the
+    accumulation balances cell by cell (1e-5), and every routed cell's
+    deposition is its donors' formula (mfd_accum.cu:222, fp32: 1e-5)."""
+    oracle, lem = libs
+    sc = S.config_large(2, n=4096, steps=1)
+    st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+    g = lem.Model(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+    g.set_state(st)
+    g.step(sc.rain[0], sc.temp[0], True)
+    g.synchronize()
+    mask = st["mask"] == 1
+    fd = g.get("fd")
+    fa, w = g.get("fa"), g.get("runoff")
+    t = g.totals()
+    done = mask.copy()
+    if t["fa_uncomputed"]:
+        done &= ~np.isclose(fa, w, rtol=0, atol=0)
+    fd_m = np.where(mask, fd, fd & 0xFF)
+    balance = w + _donor_sum(fd_m, np.where(mask, fa, 0.0), True)
+    rel = np.abs(fa - balance) / np.maximum(np.abs(fa), 1e-30)
+    assert rel[done].max() < 1e-5
+    ero, inci, geli, depo = (g.get(f) for f in ("ero", "inci", "geli", "depo"))
+    p = S.DEFAULT_PAR
+    ddk, dck, dgk = min(p["ddk"], 0.95), min(p["dck"], 0.9), p["dgk"]
+    sed_mask = mask.copy()
+    sed_mask[0, :] = sed_mask[:, 0] = False
+    src = np.where(sed_mask, 1.0, 0.0)
+    ad = _donor_sum(fd_m, np.where(mask, ero, 0.0) * (1 - ddk), True)
+    ac = _donor_sum(fd_m, np.where(mask, inci, 0.0) * (1 - dck), True)
+    ag = _donor_sum(fd_m, np.where(mask, geli, 0.0) * (1 - dgk), True)
+    want = (ad + ero) * ddk + (ac + inci) * dck + (ag + geli) * dgk
+    routed = sed_mask & (depo != np.float32(1e-5)) & (src > 0)
+    err = np.abs(depo - want)[routed]
+    assert (err <= 1e-5 * np.abs(want[routed]) + 1e-9).all()
+    assert routed.sum() > 0.9 * mask.sum()
+    g.close()
+
+
+def test_routing_stress_8192_tiled_and_walk_agree(libs):
+    """The routing stress configuration (8192x8192, 10 % of cells in 1 m flats,
+    50k nested depressions): the tiled accumulation and the global wave give
+    the same accumulation from the same directions (1e-5), and the
+    contributing-cell counts balance exactly."""
+    oracle, lem = libs
+    sc = S.config_routing(3, n=8192)
+    st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+    g = lem.Model(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+    g.set_state(st)
+    g.flow_direction()
+    g.flow_accumulation(0)  # tiled
+    fa_tiled = g.get("fa")
+    t = g.totals()
+    assert t["plateau_sweeps"] > 0 and t["flood_edges"] > 0
+    g.set_state({f: st[f] for f in ("soilM",)})  # runoff changes soil moisture; start both from the same state
+    g.flow_accumulation(lem.STEP_CONTRIB)  # global wave
+    fa_walk, cnt = g.get("fa"), g.get("contrib")
+    mask = st["mask"] == 1
+    both_nan = np.isnan(fa_tiled) & np.isnan(fa_walk)
+    err = np.where(both_nan, 0.0, np.abs(fa_tiled - fa_walk))
+    assert (err[mask] <= 1e-5 * np.abs(fa_walk[mask])).all()
+    fd = g.get("fd")
+    fd_m = np.where(mask, fd, fd & 0xFF)
+    done = mask & (cnt > 0)
+    cbal = 1 + _donor_sum(fd_m, np.where(mask, cnt, 0).astype(np.float64), True)
+    assert np.array_equal(cnt[done], cbal[done].astype(np.int64))
+    g.close()
