@@ -239,6 +239,8 @@ def run_reference(args):
 
 
 def workload_name(args):
+    if args.workload == "serve":
+        return "serving: Poisson arrivals, sides log-uniform in [128, 4096], 10-500 steps, own climate series"
     if args.workload == "ensemble":
         return f"batched ensemble of {args.dems} DEMs, sides log-uniform in [256, 2048], per-DEM climate series"
     return f"single large grid {args.grid}x{args.grid}, per-step climate series"
@@ -383,13 +385,62 @@ class EnsembleWork:
         self.b.close()
 
 
+def run_serve(args):
+    """The serving workload: Poisson arrivals of landscape-scenario requests
+    (sides log-uniform in [128, 4096], 10-500 steps, own climate series)
+    admitted by canvas room and the HBM budget, continuously batched; one JSON
+    line with throughput and p50/p99 latency."""
+    rank, world, local = dist_env()
+    from parallem_gb300 import build, lem
+    from parallem_gb300 import serve as SV
+    build.build()
+    lem.select_device(local)
+    rng = np.random.default_rng(11 + rank)
+    t = 0.0
+    reqs = []
+    for i in range(args.requests):
+        t += float(rng.exponential(1.0 / args.rate))
+        reqs.append(SV.make_request(i, rng, t))
+    W, H = args.canvas_serve
+    srv = SV.Server(W, H, budget_bytes=args.budget_gb * 1e9, max_dems=max(64, args.requests))
+    # warm-up: one small request through the whole path
+    warm = SV.make_request(-1, np.random.default_rng(1), 0.0, side_lo=128, side_hi=256, steps_lo=3, steps_hi=3)
+    srv.run([warm])
+    srv.steps_run = 0
+    srv.b.synchronize()
+    with ClockSampler(local) as clk:
+        stats = srv.run(reqs)
+    srv.close()
+    if rank != 0:
+        return 0
+    line = {
+        "metric": "cell-timesteps/s", "value": stats["cell_timesteps_per_s"], "unit": "cell-timesteps/s",
+        "n_gpus": world, "steps": stats["batch_steps"], "warmup": 1, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded spectral DEMs and climate series)",
+        "config": {"workload": "serving: Poisson arrivals, sides log-uniform in [128, 4096], 10-500 steps",
+                   "rate_per_s": args.rate, "requests": args.requests, "canvas": f"{W}x{H}",
+                   "hbm_budget_gb": args.budget_gb, "parallelism": f"replicas x{world}"},
+        "latency": {"p50_s": stats["p50_latency_s"], "p99_s": stats["p99_latency_s"]},
+        "wall_s": stats["wall_s"], "requests_done": stats["requests"],
+        "e2e": {"value": stats["cell_timesteps_per_s"], "unit": "cell-timesteps/s",
+                "note": "arrival to result on the host, grids streamed back"},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "grid"])
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "grid", "serve"])
+    ap.add_argument("--rate", type=float, default=20.0, help="serving: arrivals per second")
+    ap.add_argument("--requests", type=int, default=24, help="serving: requests")
+    ap.add_argument("--canvas-serve", type=int, nargs=2, default=[16384, 12288], help="serving: canvas W H")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: HBM budget")
     ap.add_argument("--grid", type=int, default=4096, help="side of the single grid")
     ap.add_argument("--dems", type=int, default=64, help="DEMs of the ensemble")
     ap.add_argument("--canvas", type=int, default=8192, help="width of the ensemble's canvas")
@@ -400,6 +451,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serve":
+        return run_serve(args)
 
     rank, world, local = dist_env()
     dist = init_dist(world, local)

@@ -597,6 +597,11 @@ lem_status create_common(const lem_grid_desc* grid, const lem_params* params, in
     ALLOC(s.comp, N + 1);
     ALLOC(s.cdist, N + 1);
     ALLOC(s.cmaxw, N + 1);
+    ALLOC(s.bid, N + 1);
+    ALLOC(s.blab, N + 1);
+    ALLOC(s.boff, N + 2);
+    ALLOC(s.bdist, N + 1);
+    ALLOC(s.adj_v, 2 * (size_t)cap);
     ALLOC(s.sc, 1);
     ALLOC(s.temp_tab, (size_t)kTabN);
     ALLOC(h->dem_in, (size_t)max_dems);

@@ -83,6 +83,12 @@ struct DevState {
     int32_t* comp;              // component label of basins that never reach basin 0
     unsigned long long* cdist;  //   their minimax distance to the component's label basin
     unsigned long long* cmaxw;  //   the component's largest spanning-tree edge
+    // the basin graph with basins numbered 0..n_basins-1 per step
+    int32_t* bid;               // per label: its basin number
+    int32_t* blab;              // per basin: its label
+    int32_t* boff;              // per basin: the spill round that last lowered it
+    unsigned long long* bdist;  // per basin: minimax distance to basin 0 (ordered key)
+    int32_t* adj_v;             // per edge: its two basin numbers
     DevScalars* sc;
     DemCtx dems;                // the DEMs of the grid
     int32_t* chunk_start;       // streaming passes: first chunk of each DEM (n + 1 entries)

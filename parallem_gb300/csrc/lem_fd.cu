@@ -414,7 +414,7 @@ __global__ void k_plateau_final(const double* __restrict__ z, const float* __res
 // other cells point at their SFD receiver, masked and edge cells are basin 0.
 __global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
                              uint8_t* __restrict__ sfd1, int32_t* ws, int32_t* sinks, unsigned long long* raise,
-                             ModelConsts k, DevScalars* sc, DemCtx dc) {
+                             int32_t* bid, ModelConsts k, DevScalars* sc, DemCtx dc) {
     const int W = k.W, H = k.H;
     const size_t N = (size_t)W * H;
     int nsink = 0;
@@ -453,7 +453,10 @@ __global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __
         warp_append(sink, (int32_t)c, sinks, &sc->n_sinks, (int)N, &sc->err);
     }
     if (nsink) atomicAdd(&sc->sinkcount_pass1, nsink);
-    if (blockIdx.x == 0 && threadIdx.x == 0) raise[0] = dkey(0.0);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        raise[0] = dkey(0.0);
+        bid[0] = -1;  // numbered by the compaction once basin 0 is on an edge
+    }
 }
 
 // init_watershed_sinkMFD loop (newflow.cu:430-460): equal-height sink cells
@@ -612,8 +615,8 @@ __global__ void k_flood_edges(const double* __restrict__ z, const uint8_t* __res
 // (data->sinkcount, newflow.cu:1044-1045).  Labels on edges start unreached.
 __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, const unsigned long long* __restrict__ ewt,
                                 int64_t cap, int32_t* ea, int32_t* eb, unsigned long long* ew,
-                                unsigned long long* raise, int32_t* seen, int32_t epoch, DevScalars* sc,
-                                DemCtx dc) {
+                                unsigned long long* raise, int32_t* seen, int32_t epoch, int32_t* bid,
+                                int32_t* blab, DevScalars* sc, DemCtx dc) {
     if (sc->sinkcount_pass1 == 0) return;
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)cap; base += (size_t)gridDim.x * blockDim.x) {
         const size_t i = base + threadIdx.x;
@@ -630,8 +633,20 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
                 w = ewt[i];
                 // labels are cell + 1 of one DEM; basin 0 is counted once per DEM it borders
                 d = dem_at(dc, (size_t)(a != 0 ? a : b) - 1);
-                if (a != 0 && atomicExch(seen + a, epoch) != epoch) ++nd;
-                if (b != 0 && atomicExch(seen + b, epoch) != epoch) ++nd;
+                const bool fa_ = atomicExch(seen + a, epoch) != epoch;
+                const bool fb_ = atomicExch(seen + b, epoch) != epoch;
+                if (fa_) {  // number the basin on its first edge
+                    const int32_t id = atomicAdd(&sc->n_basins, 1);
+                    bid[a] = id;
+                    blab[id] = a;
+                }
+                if (fb_) {
+                    const int32_t id = atomicAdd(&sc->n_basins, 1);
+                    bid[b] = id;
+                    blab[id] = b;
+                }
+                if (a != 0 && fa_) ++nd;
+                if (b != 0 && fb_) ++nd;
                 if ((a == 0 || b == 0) && *((volatile int32_t*)&dc.out[d].zero_seen) != epoch &&
                     atomicExch(&dc.out[d].zero_seen, epoch) != epoch)
                     ++nd;
@@ -661,35 +676,52 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
 // that can drain to basin 0 the smallest height h at which it connects to
 // basin 0 through boundaries no higher than h (the bottleneck distance); it is
 // computed here as the fixpoint raise[a] = min(raise[a], max(w_ab, raise[b])).
+// Minimax distance of every basin to basin 0 over the basin-pair edges
+// (Kruskal's raise, routeflow.cu:520-572, as a fixpoint: raise(a) = min over
+// edges (a, b, w) of max(w, raise(b)), basin 0 at 0).  Basins are numbered
+// compactly; every round sweeps the edge list and relaxes the edges with an
+// endpoint lowered in the previous round or earlier in this one (a stamp per
+// basin), so improvements run along several edges in one sweep while settled
+// parts of the graph cost only the stamp test.
 __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __restrict__ eb,
                               const unsigned long long* __restrict__ ew, unsigned long long* raise, int32_t* comp,
-                              unsigned long long* cdist, unsigned long long* cmaxw, DevScalars* sc) {
+                              unsigned long long* cdist, unsigned long long* cmaxw, const int32_t* __restrict__ bid,
+                              const int32_t* __restrict__ blab, int32_t* stamp, unsigned long long* bdist,
+                              int32_t* euv, DevScalars* sc) {
     if (sc->sinkcount_pass1 == 0) return;
     cg::grid_group grid = cg::this_grid();
     const int n = sc->n_edges;
+    const int nb = sc->n_basins;
     const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t gstride = (size_t)gridDim.x * blockDim.x;
-    if (gtid == 0) {
-        raise[0] = 0ull;  // basin 0 is done
-        sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
+    const int32_t z = nb > 0 ? bid[0] : -1;  // basin 0 is on some edge whenever it borders a basin
+    for (size_t i = gtid; i < (size_t)nb; i += gstride) {
+        bdist[i] = (int32_t)i == z ? 0ull : ~0ull;
+        stamp[i] = (int32_t)i == z ? 0 : -2;
     }
+    for (size_t i = gtid; i < (size_t)n; i += gstride) {
+        euv[2 * i] = bid[ea[i]];
+        euv[2 * i + 1] = bid[eb[i]];
+    }
+    if (gtid == 0) sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
     grid.sync();
-    int round = 0;
+    int round = 1;
     for (;; ++round) {
         if (gtid == 0) sc->flag[(round + 1) % 3] = 0;  // next round's flag; this round's is read after the sync
         int changed = 0;
-        for (size_t i = gtid; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
-            const int32_t a = ea[i], b = eb[i];
+        for (size_t i = gtid; i < (size_t)n; i += gstride) {
+            const int2 uv = __ldcg(reinterpret_cast<const int2*>(euv) + i);
+            const int32_t su = __ldcg(stamp + uv.x), sv = __ldcg(stamp + uv.y);
+            if (su < round - 1 && sv < round - 1) continue;
             const unsigned long long w = ew[i];
-            const unsigned long long ra = __ldcg(raise + a), rb = __ldcg(raise + b);
-            const unsigned long long ca = w > rb ? w : rb;
-            const unsigned long long cb = w > ra ? w : ra;
-            if (a != 0 && ca < ra) {
-                atomicMin(raise + a, ca);
+            const unsigned long long du = __ldcg(bdist + uv.x), dv = __ldcg(bdist + uv.y);
+            const unsigned long long cu = w > dv ? w : dv, cv = w > du ? w : du;
+            if (cu < du && atomicMin(bdist + uv.x, cu) > cu) {
+                stamp[uv.x] = round;
                 changed = 1;
             }
-            if (b != 0 && cb < rb) {
-                atomicMin(raise + b, cb);
+            if (cv < dv && atomicMin(bdist + uv.y, cv) > cv) {
+                stamp[uv.y] = round;
                 changed = 1;
             }
         }
@@ -701,6 +733,11 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
             break;
         }
     }
+    for (size_t i = gtid; i < (size_t)nb; i += gstride) {
+        const int32_t L = blab[i];
+        if (L != 0) raise[L] = __ldcg(bdist + i);
+    }
+    if (gtid == 0) raise[0] = 0ull;
     if (gtid == 0) {
         sc->spill_rounds = round + 1;
         sc->flag[3] = 0;
@@ -839,6 +876,7 @@ __global__ void k_fd_reset(DevScalars* sc, DemCtx dc) {
         sc->n_cand = 0;
         sc->n_sinks = 0;
         sc->n_edges = 0;
+        sc->n_basins = 0;
     }
     if (d < dc.n) {
         DemOut& o = dc.out[d];
@@ -913,8 +951,8 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
     LEM_LAUNCH(L, k_fd_reset, (s.dems.n + 127) / 128, 128, s.sc, s.dems);
     if ((r = direction_pass(s, k, L, 1)) != LEM_OK) return r;
     // sink flooding on the pass-1 codes
-    LEM_LAUNCH(L, k_flood_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.sfd1, s.ws, s.list_b, s.raise, k, s.sc,
-               s.dems);
+    LEM_LAUNCH(L, k_flood_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.sfd1, s.ws, s.list_b, s.raise, s.bid, k,
+               s.sc, s.dems);
     {
         const double* zz = s.z;
         int32_t* ws = s.ws;
@@ -941,7 +979,7 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
     static int32_t epoch = 0;
     ++epoch;
     LEM_LAUNCH(L, k_flood_compact, flat_blocks((size_t)s.ecap, T, big), T, s.ekey, s.ewt, s.ecap, s.edge_a, s.edge_b,
-               s.edge_w, s.raise, s.label_seen, epoch, s.sc, s.dems);
+               s.edge_w, s.raise, s.label_seen, epoch, s.bid, s.blab, s.sc, s.dems);
     {
         const int32_t* ea = s.edge_a;
         const int32_t* eb = s.edge_b;
@@ -950,9 +988,15 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
         int32_t* comp = s.comp;
         unsigned long long* cdist = s.cdist;
         unsigned long long* cmaxw = s.cmaxw;
+        const int32_t* bidp = s.bid;
+        const int32_t* blab = s.blab;
+        int32_t* stamp = s.boff;
+        unsigned long long* bdist = s.bdist;
+        int32_t* euv = s.adj_v;
         DevScalars* sc = s.sc;
-        void* args[] = {(void*)&ea, (void*)&eb, (void*)&ew, (void*)&raise, (void*)&comp, (void*)&cdist,
-                        (void*)&cmaxw, (void*)&sc};
+        void* args[] = {(void*)&ea,   (void*)&eb,    (void*)&ew,    (void*)&raise, (void*)&comp, (void*)&cdist,
+                        (void*)&cmaxw, (void*)&bidp, (void*)&blab,  (void*)&stamp, (void*)&bdist, (void*)&euv,
+                        (void*)&sc};
         if ((r = coop("k_flood_spill", (const void*)k_flood_spill, s.max_coop_blocks, args, L)) != LEM_OK) return r;
     }
     LEM_LAUNCH(L, k_flood_raise, flat_blocks(N, T, big), T, s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc, s.dems);

@@ -23,7 +23,7 @@ from . import lem as L
 from . import scenario as S
 
 # device bytes per canvas cell of a batch handle (fields, tiles, flood tables)
-BYTES_PER_CELL = 340
+BYTES_PER_CELL = 390
 
 
 @dataclass
