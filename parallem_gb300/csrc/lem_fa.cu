@@ -219,11 +219,12 @@ __global__ void __launch_bounds__(256)
     __shared__ uint8_t s_ext[kTile * kTile];
     __shared__ uint8_t s_done[kTile * kTile];
     __shared__ int16_t s_oslot[kTile * kTile];
+    __shared__ int16_t s_q[kTile * kTile];
     __shared__ int16_t s_olist[kTileEnt];
     __shared__ int32_t s_ocnt[kTileEnt];
     __shared__ int16_t s_ostart[kTileEnt];
     __shared__ int16_t s_ofill[kTileEnt];
-    __shared__ int s_no;
+    __shared__ int s_no, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = blockIdx.x;
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
@@ -274,12 +275,11 @@ __global__ void __launch_bounds__(256)
         s_la[l] = make_float2(wl, 0.f);
         s_done[l] = 0;
     }
+    if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
-    // accumulation from inside the tile: chains of last-arriving donors
-#pragma unroll 1
-    for (int q = 0; q < 4; ++q) {
-        int cur = src[q] ? (ly0 + 8 * q) * kTile + lx : -1;
-        for (int guard = 0; cur >= 0 && guard < kTile * kTile; ++guard) {
+    // accumulation from inside the tile, in dependency order
+    tile_wave(
+        [&](int cur) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
@@ -294,19 +294,9 @@ __global__ void __launch_bounds__(256)
             if (acc.x < 0.0f) acc = make_float2(0.f, 0.f);
             s_la[cur] = ff_add(s_la[cur], acc);
             s_done[cur] = 1;
-            __threadfence_block();
-            int nxt = -1;
-            if (s_kind[cur] == kKindIn) {
-                const int r = s_ptr[cur];
-                if (atomicSub(&s_pend[r], 1) == 1) {
-                    __threadfence_block();
-                    nxt = r;
-                }
-            }
-            cur = nxt;
-        }
-    }
-    __syncthreads();
+            return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
+        },
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
     // the end of every in-tile path: pointer jumping (paths are shorter than 2^10 cells)
     for (int it = 0; it < 10; ++it) {
 #pragma unroll
@@ -465,7 +455,8 @@ __global__ void __launch_bounds__(256)
     __shared__ float2 s_hval[kTH * kTH];
     __shared__ int32_t s_pend[kTile * kTile];
     __shared__ float2 s_val[kTile * kTile];
-    __shared__ int s_done, s_dem;
+    __shared__ int16_t s_q[kTile * kTile];
+    __shared__ int s_done, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = blockIdx.x;
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
@@ -525,11 +516,10 @@ __global__ void __launch_bounds__(256)
         src[q] = pend == 0 && !outlet[q];
         s_val[l] = make_float2(wl, 0.f);
     }
+    if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
-#pragma unroll 1
-    for (int q = 0; q < 4; ++q) {
-        int cur = src[q] ? (ly0 + 8 * q) * kTile + lx : -1;
-        for (int guard = 0; cur >= 0 && guard < kTile * kTile; ++guard) {
+    tile_wave(
+        [&](int cur) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
@@ -545,29 +535,19 @@ __global__ void __launch_bounds__(256)
             s_val[cur] = v;
             fa[(size_t)(ty0 + cy) * W + tx0 + cx] = v;
             ++done;
-            __threadfence_block();
-            int nxt = -1;
             const int d = bit_dir(s_code[hc]);
-            if (d >= 0) {
-                const int rlx = cx + dir_dx(d), rly = cy + dir_dy(d);
-                const int rh = hc + dir_dy(d) * kTH + dir_dx(d);
-                if (in_tile(rlx, rly) && s_cls[rh] == kCellIn) {
-                    const int r = rly * kTile + rlx;
-                    if (atomicSub(&s_pend[r], 1) == 1) {
-                        __threadfence_block();
-                        // an outlet keeps the coarse wave's value
-                        const bool r_out = [&] {
-                            const int dr = bit_dir(s_code[rh]);
-                            return dr >= 0 && s_cls[rh + dir_dy(dr) * kTH + dir_dx(dr)] == kCellIn &&
-                                   !in_tile(rlx + dir_dx(dr), rly + dir_dy(dr));
-                        }();
-                        if (!r_out) nxt = r;
-                    }
-                }
-            }
-            cur = nxt;
-        }
-    }
+            if (d < 0) return -1;
+            const int rlx = cx + dir_dx(d), rly = cy + dir_dy(d);
+            const int rh = hc + dir_dy(d) * kTH + dir_dx(d);
+            if (!in_tile(rlx, rly) || s_cls[rh] != kCellIn) return -1;
+            // an outlet keeps the coarse wave's value
+            const int dr = bit_dir(s_code[rh]);
+            if (dr >= 0 && s_cls[rh + dir_dy(dr) * kTH + dir_dx(dr)] == kCellIn &&
+                !in_tile(rlx + dir_dx(dr), rly + dir_dy(dr)))
+                return -1;
+            return rly * kTile + rlx;
+        },
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();

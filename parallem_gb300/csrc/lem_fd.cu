@@ -624,6 +624,7 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
         int32_t a = 0, b = 0;
         unsigned long long w = 0;
         int d = -1, nd = 0;
+        bool fa_ = false, fb_ = false;
         if (i < (size_t)cap) {
             const unsigned long long key = ekey[i];
             if (key != ~0ull) {
@@ -633,18 +634,8 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
                 w = ewt[i];
                 // labels are cell + 1 of one DEM; basin 0 is counted once per DEM it borders
                 d = dem_at(dc, (size_t)(a != 0 ? a : b) - 1);
-                const bool fa_ = atomicExch(seen + a, epoch) != epoch;
-                const bool fb_ = atomicExch(seen + b, epoch) != epoch;
-                if (fa_) {  // number the basin on its first edge
-                    const int32_t id = atomicAdd(&sc->n_basins, 1);
-                    bid[a] = id;
-                    blab[id] = a;
-                }
-                if (fb_) {
-                    const int32_t id = atomicAdd(&sc->n_basins, 1);
-                    bid[b] = id;
-                    blab[id] = b;
-                }
+                fa_ = atomicExch(seen + a, epoch) != epoch;
+                fb_ = atomicExch(seen + b, epoch) != epoch;
                 if (a != 0 && fa_) ++nd;
                 if (b != 0 && fb_) ++nd;
                 if ((a == 0 || b == 0) && *((volatile int32_t*)&dc.out[d].zero_seen) != epoch &&
@@ -652,6 +643,27 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
                     ++nd;
                 if (a != 0) raise[a] = ~0ull;
                 if (b != 0) raise[b] = ~0ull;
+            }
+        }
+        // number the basins first seen here: one atomic per warp
+        {
+            const unsigned lanes_below = (1u << (threadIdx.x & 31)) - 1;
+            const unsigned ma = __ballot_sync(0xffffffffu, fa_), mb = __ballot_sync(0xffffffffu, fb_);
+            const int tot = __popc(ma) + __popc(mb);
+            int base = 0;
+            if (tot) {
+                if ((threadIdx.x & 31) == 0) base = atomicAdd(&sc->n_basins, tot);
+                base = __shfl_sync(0xffffffffu, base, 0);
+            }
+            if (fa_) {
+                const int32_t id = base + __popc(ma & lanes_below);
+                bid[a] = id;
+                blab[id] = a;
+            }
+            if (fb_) {
+                const int32_t id = base + __popc(ma) + __popc(mb & lanes_below);
+                bid[b] = id;
+                blab[id] = b;
             }
         }
         // one atomic per DEM and warp for the label counts

@@ -464,7 +464,8 @@ __global__ void __launch_bounds__(256)
     __shared__ int32_t s_pcnt[kTileEnt];
     __shared__ int16_t s_pstart[kTileEnt];
     __shared__ int16_t s_pfill[kTileEnt];
-    __shared__ int s_no, s_nt, s_done, s_pool, s_dem;
+    __shared__ int16_t s_q[kTile * kTile];
+    __shared__ int s_no, s_nt, s_done, s_pool, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = blockIdx.x;
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
@@ -523,10 +524,10 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
     // settle what depends on this tile only; order the waiting cells
     int done = 0;
-#pragma unroll 1
-    for (int q = 0; q < 4; ++q) {
-        int cur = src[q] ? (ly0 + 8 * q) * kTile + lx : -1;
-        for (int guard = 0; cur >= 0 && guard < kTile * kTile; ++guard) {
+    if (threadIdx.x == 0) s_qn = 0;
+    __syncthreads();
+    tile_wave(
+        [&](int cur) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             bool taint = s_ext[cur] != 0;
             float from = 0.f;
@@ -559,19 +560,9 @@ __global__ void __launch_bounds__(256)
                 s_flag[cur] = kFDone | kFTaint;
                 s_topo[atomicAdd(&s_nt, 1)] = (int16_t)cur;
             }
-            __threadfence_block();
-            int nxt = -1;
-            if (s_kind[cur] == kKindIn) {
-                const int r = s_ptr[cur];
-                if (atomicSub(&s_pend[r], 1) == 1) {
-                    __threadfence_block();
-                    nxt = r;
-                }
-            }
-            cur = nxt;
-        }
-    }
-    __syncthreads();
+            return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
+        },
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
     for (int it = 0; it < 10; ++it) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -861,7 +852,8 @@ __global__ void __launch_bounds__(256)
     __shared__ int32_t s_pend[kTile * kTile];
     __shared__ float s_new[kTile * kTile];
     __shared__ uint8_t s_stat[kTile * kTile];
-    __shared__ int s_done, s_dem;
+    __shared__ int16_t s_q[kTile * kTile];
+    __shared__ int s_done, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = blockIdx.x;
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
@@ -923,16 +915,15 @@ __global__ void __launch_bounds__(256)
         s_new[l] = v;
         src[q] = pend == 0;
     }
+    if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
-#pragma unroll 1
-    for (int q = 0; q < 4; ++q) {
-        int cur = src[q] ? (ly0 + 8 * q) * kTile + lx : -1;
-        for (int guard = 0; cur >= 0 && guard < kTile * kTile; ++guard) {
+    tile_wave(
+        [&](int cur) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             const int d = bit_dir(s_code[hc]);
             const int rlx = cx + (d >= 0 ? dir_dx(d) : 0), rly = cy + (d >= 0 ? dir_dy(d) : 0);
             const bool rin = d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn;
-            if (rin && !in_tile(rlx, rly)) break;  // an outlet: the coarse wave stored it
+            if (rin && !in_tile(rlx, rly)) return -1;  // an outlet: the coarse wave stored it
             if (s_stat[cur] == 2) {
                 float from = 0.f;
 #pragma unroll
@@ -949,18 +940,9 @@ __global__ void __launch_bounds__(256)
                 sed_store((size_t)(ty0 + cy) * W + tx0 + cx, in.L, sn, depo, stone, fines, soilT);
                 ++done;
             }
-            __threadfence_block();
-            int nxt = -1;
-            if (rin) {
-                const int r = rly * kTile + rlx;
-                if (atomicSub(&s_pend[r], 1) == 1) {
-                    __threadfence_block();
-                    nxt = r;
-                }
-            }
-            cur = nxt;
-        }
-    }
+            return rin ? rly * kTile + rlx : -1;
+        },
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();

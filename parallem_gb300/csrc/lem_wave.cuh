@@ -190,6 +190,36 @@ __device__ __forceinline__ int ring_halo(int i) {
     return (i - 2 * kTH - kTile + 1) * kTH + kTH - 1;
 }
 
+// The in-tile dependency wave of one block, in rounds: a round takes every
+// queued cell (all its donors in the tile finished), computes it with
+// op(c), which returns the in-tile receiver it releases (or -1), and
+// queues that receiver when c was its last donor.  Cells are queued once, in
+// an order where every donor comes before its receiver.  Every lane works on a
+// cell while the round holds one per lane, which a walk along each chain
+// cannot do.
+template <class Op>
+__device__ __forceinline__ void tile_wave(const Op& op, int32_t* s_pend, int16_t* s_q, int* s_qn, int* s_end,
+                                          const bool (&src)[4], int lx, int ly0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (src[q]) s_q[atomicAdd(s_qn, 1)] = (int16_t)((ly0 + 8 * q) * kTile + lx);
+    int start = 0;
+    for (int guard = 0; guard <= kTile * kTile; ++guard) {
+        __syncthreads();
+        if (threadIdx.x == 0) *s_end = *s_qn;
+        __syncthreads();
+        const int end = *s_end;
+        if (start == end) break;
+        for (int i = start + threadIdx.x; i < end; i += blockDim.x) {
+            const int c = s_q[i];
+            const int r = op(c);
+            if (r >= 0 && atomicSub(&s_pend[r], 1) == 1) s_q[atomicAdd(s_qn, 1)] = (int16_t)r;
+        }
+        start = end;
+    }
+    __syncthreads();
+}
+
 // Receivers of cell (x, y) by its direction code: in-grid, in-catchment cells.
 __device__ __forceinline__ int code_receivers(const uint8_t* __restrict__ fd, const uint8_t* __restrict__ mask,
                                               int32_t cur, int x, int y, int W, int H, int32_t* r) {
