@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
     // accumulation from inside the tile, in dependency order
     tile_wave(
-        [&](int cur) {
+        [&](int cur, int rnd) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(256)
     if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
     tile_wave(
-        [&](int cur) {
+        [&](int cur, int rnd) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             float2 acc = make_float2(0.f, 0.f);
 #pragma unroll

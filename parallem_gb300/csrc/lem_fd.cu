@@ -634,8 +634,9 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
                 w = ewt[i];
                 // labels are cell + 1 of one DEM; basin 0 is counted once per DEM it borders
                 d = dem_at(dc, (size_t)(a != 0 ? a : b) - 1);
-                fa_ = atomicExch(seen + a, epoch) != epoch;
-                fb_ = atomicExch(seen + b, epoch) != epoch;
+                // most labels are on many edges (basin 0 on most): test before the atomic
+                fa_ = __ldcg(seen + a) != epoch && atomicExch(seen + a, epoch) != epoch;
+                fb_ = __ldcg(seen + b) != epoch && atomicExch(seen + b, epoch) != epoch;
                 if (a != 0 && fa_) ++nd;
                 if (b != 0 && fb_) ++nd;
                 if ((a == 0 || b == 0) && *((volatile int32_t*)&dc.out[d].zero_seen) != epoch &&

@@ -465,6 +465,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int16_t s_pstart[kTileEnt];
     __shared__ int16_t s_pfill[kTileEnt];
     __shared__ int16_t s_q[kTile * kTile];
+    __shared__ int16_t s_rnd[kTile * kTile];
     __shared__ int s_no, s_nt, s_done, s_pool, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = blockIdx.x;
@@ -527,7 +528,7 @@ __global__ void __launch_bounds__(256)
     if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
     tile_wave(
-        [&](int cur) {
+        [&](int cur, int rnd) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             bool taint = s_ext[cur] != 0;
             float from = 0.f;
@@ -558,6 +559,7 @@ __global__ void __launch_bounds__(256)
                 ++done;
             } else {
                 s_flag[cur] = kFDone | kFTaint;
+                s_rnd[cur] = (int16_t)rnd;  // a level for the coarse evaluation: inputs come from earlier rounds
                 s_topo[atomicAdd(&s_nt, 1)] = (int16_t)cur;
             }
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
@@ -737,7 +739,8 @@ __global__ void __launch_bounds__(256)
             p_map[pool + start + m] = H;
             ++m;
         }
-        p_abc[nbase + pos] = make_float4(s_A[l], s_B[l], C, __int_as_float(start | (m << 11) | (s_nz[l] << 15)));
+        p_abc[nbase + pos] =
+            make_float4(s_A[l], s_B[l], C, __int_as_float(start | (m << 11) | (s_nz[l] << 15) | ((int)s_rnd[l] << 16)));
     }
     const int j = threadIdx.x;
     bool ready = false;
@@ -758,7 +761,9 @@ __global__ void __launch_bounds__(256)
     if (threadIdx.x == 0 && s_done && s_dem >= 0) atomicAdd(&dc.out[s_dem].sed_done, s_done);
 }
 
-// One outlet of the coarse sediment wave: its program, then its own stores.
+// One outlet of the coarse sediment wave, a warp per outlet: its program
+// level by level (nodes of one tile-wave round depend only on earlier rounds,
+// and the program lists them by round), then its own stores by lane 0.
 struct SedCoarse {
     const uint8_t* fd;
     const int32_t* t_orng;
@@ -772,49 +777,65 @@ struct SedCoarse {
     float* stone;
     float* fines;
     float* soilT;
+    float* s_vals;  // kProgLocal values per warp of the block
     int W, TW;
-    __device__ __forceinline__ void cell(int32_t o, int x, int y) const {
+    __device__ __forceinline__ void cell_warp(int32_t o, int x, int y, int lane) const {
         const int rng = __ldg(t_orng + o);
         const int cnt = rng & 0xffff;
         if (cnt == 0) return;  // settled inside its tile
         const int t = (y / kTile) * TW + x / kTile;
         const size_t nbase = (size_t)t * kTile * kTile + (rng >> 16);
         const size_t pool = (size_t)t * kPool;
-        float vals[kProgLocal];
-        float sn = 0.f;
-        bool nz = false;
-        for (int i = 0; i < cnt; ++i) {
-            const float4 r = __ldg(p_abc + nbase + i);
-            const int meta = __float_as_int(r.w);
-            const int start = meta & 2047, nin = (meta >> 11) & 15;
-            nz = (meta >> 15) & 1;
-            float from = r.z;
-            for (int jr = 0; jr < nin; ++jr) {
-                const int32_t ref = __ldg(p_ref + pool + start + jr);
-                const float4 mp = __ldg(p_map + pool + start + jr);
-                float v;
-                if (ref >= 0)
-                    v = __ldcg(stone + ref);
-                else if (-ref - 1 < kProgLocal)
-                    v = vals[-ref - 1];
-                else
-                    v = __ldcg(p_val + nbase - ref - 1);
-                from = __fadd_rn(from, __fmul_rn(1.0f, map_apply(mp, v)));
+        float* vals = s_vals + (threadIdx.x >> 5) * kProgLocal;
+        for (int i = 0; i < cnt;) {
+            const int j = i + lane;
+            float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+            int meta = -1;
+            if (j < cnt) {
+                r = __ldg(p_abc + nbase + j);
+                meta = __float_as_int(r.w);
             }
-            sn = nz ? sed_mix(r.x, r.y, from) : r.x;
-            if (i < kProgLocal)
-                vals[i] = sn;
-            else
-                __stcg(p_val + nbase + i, sn);
+            const int lvl0 = __shfl_sync(0xffffffffu, meta >> 16, 0);
+            const bool act = j < cnt && (meta >> 16) == lvl0;
+            const int run = __popc(__ballot_sync(0xffffffffu, act));  // the run of this level (a prefix)
+            if (act) {
+                const int start = meta & 2047, nin = (meta >> 11) & 15;
+                const bool nz = (meta >> 15) & 1;
+                float from = r.z;
+                for (int jr = 0; jr < nin; ++jr) {
+                    const int32_t ref = __ldg(p_ref + pool + start + jr);
+                    const float4 mp = __ldg(p_map + pool + start + jr);
+                    float v;
+                    if (ref >= 0)
+                        v = __ldcg(stone + ref);
+                    else if (-ref - 1 < kProgLocal)
+                        v = vals[-ref - 1];
+                    else
+                        v = __ldcg(p_val + nbase - ref - 1);
+                    from = __fadd_rn(from, __fmul_rn(1.0f, map_apply(mp, v)));
+                }
+                const float sn = nz ? sed_mix(r.x, r.y, from) : r.x;
+                if (j < kProgLocal)
+                    vals[j] = sn;
+                else
+                    __stcg(p_val + nbase + j, sn);
+            }
+            __syncwarp();
+            i += run;
         }
-        // the outlet is the last node of its program
-        const float2 out = __ldg(t_out + o);
-        depo[o] = out.x;
-        if (nz) {
-            __stcg(stone + o, sn);
-            fines[o] = __fsub_rn(100.0f, sn);
+        if (lane == 0) {
+            // the outlet is the last node of its program
+            const int j = cnt - 1;
+            const float sn = j < kProgLocal ? vals[j] : __ldcg(p_val + nbase + j);
+            const int meta = __float_as_int(__ldg(p_abc + nbase + j).w);
+            const float2 out = __ldg(t_out + o);
+            depo[o] = out.x;
+            if ((meta >> 15) & 1) {
+                __stcg(stone + o, sn);
+                fines[o] = __fsub_rn(100.0f, sn);
+            }
+            soilT[o] = out.y;
         }
-        soilT[o] = out.y;
     }
     __device__ __forceinline__ int receivers(int32_t o, int x, int y, int32_t* r) const {
         const int d = bit_dir(__ldg(fd + o));
@@ -825,18 +846,18 @@ struct SedCoarse {
     }
 };
 
-__global__ void k_sedt_coarse(const uint8_t* __restrict__ fd, const int32_t* __restrict__ t_orng,
-                              const int32_t* __restrict__ t_dst, const float2* __restrict__ t_out,
-                              const float4* __restrict__ p_abc, const int32_t* __restrict__ p_ref,
-                              const float4* __restrict__ p_map, float* p_val,
-                              float* depo, float* stone, float* fines, float* soilT, int32_t* t_pend,
-                              int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc) {
+__global__ void __launch_bounds__(256)
+    k_sedt_coarse(const uint8_t* __restrict__ fd, const int32_t* __restrict__ t_orng,
+                  const int32_t* __restrict__ t_dst, const float2* __restrict__ t_out,
+                  const float4* __restrict__ p_abc, const int32_t* __restrict__ p_ref,
+                  const float4* __restrict__ p_map, float* p_val, float* depo, float* stone, float* fines,
+                  float* soilT, int32_t* t_pend, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc) {
     if (!sc->sed_tiled_ok) return;
+    __shared__ float s_vals[8 * kProgLocal];
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->counters[0] = sc->tile_src;
-    const SedCoarse op{fd, t_orng, t_dst, t_out, p_abc, p_ref, p_map, p_val, depo, stone, fines, soilT,
+    const SedCoarse op{fd, t_orng, t_dst, t_out, p_abc, p_ref, p_map, p_val, depo, stone, fines, soilT, s_vals,
                        k.W, (k.W + kTile - 1) / kTile};
-    int done = wave_walk(op, t_pend, list_a, list_b, k.W, k.H, sc);
-    (void)done;
+    wave_walk_warp(op, t_pend, list_a, list_b, k.W, k.H, sc);
 }
 
 __global__ void __launch_bounds__(256)
@@ -918,7 +939,7 @@ __global__ void __launch_bounds__(256)
     if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
     tile_wave(
-        [&](int cur) {
+        [&](int cur, int rnd) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             const int d = bit_dir(s_code[hc]);
             const int rlx = cx + (d >= 0 ? dir_dx(d) : 0), rly = cy + (d >= 0 ? dir_dy(d) : 0);

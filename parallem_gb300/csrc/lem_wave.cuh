@@ -192,7 +192,7 @@ __device__ __forceinline__ int ring_halo(int i) {
 
 // The in-tile dependency wave of one block, in rounds: a round takes every
 // queued cell (all its donors in the tile finished), computes it with
-// op(c), which returns the in-tile receiver it releases (or -1), and
+// op(c, round), which returns the in-tile receiver it releases (or -1), and
 // queues that receiver when c was its last donor.  Cells are queued once, in
 // an order where every donor comes before its receiver.  Every lane works on a
 // cell while the round holds one per lane, which a walk along each chain
@@ -212,12 +212,79 @@ __device__ __forceinline__ void tile_wave(const Op& op, int32_t* s_pend, int16_t
         if (start == end) break;
         for (int i = start + threadIdx.x; i < end; i += blockDim.x) {
             const int c = s_q[i];
-            const int r = op(c);
+            const int r = op(c, guard);
             if (r >= 0 && atomicSub(&s_pend[r], 1) == 1) s_q[atomicAdd(s_qn, 1)] = (int16_t)r;
         }
         start = end;
     }
     __syncthreads();
+}
+
+// The wave of wave_walk with a whole warp per node: lane 0 takes a ready node,
+// Op::cell_warp(c, x, y, lane) computes it with every lane, lane 0 releases its
+// receivers and the warp carries on with the first it made ready.  For nodes
+// whose own computation has parallel parts (the sediment programs).
+template <class Op>
+__device__ void wave_walk_warp(const Op& op, int32_t* pending, int32_t* list_a, int32_t* list_b, int W, int H,
+                               DevScalars* sc) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    const size_t N = (size_t)W * H;
+    const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int32_t* cnt = sc->counters;  // [0..2] list sizes by round % 3, [3..5] take heads by round % 3
+    if (gtid == 0) {
+        cnt[1] = cnt[2] = 0;
+        cnt[3] = cnt[4] = cnt[5] = 0;
+    }
+    grid.sync();
+    for (int round = 0;; ++round) {
+        const int32_t* in = (round & 1) ? list_b : list_a;
+        int32_t* out = (round & 1) ? list_a : list_b;
+        const int nin = *((volatile int32_t*)&cnt[round % 3]);
+        if (nin == 0) break;
+        if (round >= kWaveMaxRounds) {
+            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            break;
+        }
+        if (gtid == 0) {
+            cnt[(round + 2) % 3] = 0;
+            cnt[3 + (round + 1) % 3] = 0;
+        }
+        int32_t* head = &cnt[3 + round % 3];
+        for (size_t guard = 0; guard <= N; ++guard) {
+            int32_t cur = -1;
+            if (lane == 0) {
+                const int it = atomicAdd(head, 1);
+                if (it < nin) cur = __ldcg(in + it);
+            }
+            cur = __shfl_sync(0xffffffffu, cur, 0);
+            if (cur < 0) break;
+            for (size_t chain = 0; cur >= 0 && chain <= N; ++chain) {
+                const int x = cur % W, y = cur / W;
+                __syncwarp();
+                op.cell_warp(cur, x, y, lane);
+                __syncwarp();
+                int32_t next = -1;
+                if (lane == 0) {
+                    int32_t rcv[8];
+                    const int nr = op.receivers(cur, x, y, rcv);
+                    for (int j = 0; j < nr; ++j) {
+                        if (dec_acq_rel(pending + rcv[j]) == 1) {
+                            if (next < 0) {
+                                next = rcv[j];
+                            } else {
+                                const int p = atomicAdd(&cnt[(round + 1) % 3], 1);
+                                if (p < (int)N) out[p] = rcv[j];
+                            }
+                        }
+                    }
+                }
+                cur = __shfl_sync(0xffffffffu, next, 0);
+            }
+        }
+        grid.sync();
+    }
 }
 
 // Receivers of cell (x, y) by its direction code: in-grid, in-catchment cells.
