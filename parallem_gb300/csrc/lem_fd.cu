@@ -569,55 +569,126 @@ __device__ __forceinline__ uint64_t edge_hash(unsigned long long key, int logcap
     return (key * 0x9E3779B97F4A7C15ull) >> (64 - logcap);
 }
 
-// identify_watershed_boundary_write_backMFD (newflow.cu:787-877): the minimum
-// boundary height per unordered basin pair, in an open-addressing table.
-__global__ void k_flood_edges(const double* __restrict__ z, const uint8_t* __restrict__ mask,
-                              const int32_t* __restrict__ ws, unsigned long long* ekey, unsigned long long* ewt,
-                              int logcap, ModelConsts k, DevScalars* sc) {
+// Live capacity of the basin-pair table: 32 slots per label that can own a
+// basin (the sink cells, plus basin 0), at least 1024, at most the allocated
+// capacity.  Basins of 8-connected regions border a few others each, so the
+// table stays sparse for linear probing, and the table of a grid with few
+// sinks is small enough to stay in L2.
+__device__ __forceinline__ int edge_logcap(const DevScalars* sc, int logmax) {
+    const long long want = 32ll * ((long long)sc->n_sinks + 1);
+    int l = 10;
+    while (l < logmax && (1ll << l) < want) ++l;
+    return l;
+}
+
+__global__ void k_edge_clear(unsigned long long* ekey, unsigned long long* ewt, int logmax, DevScalars* sc) {
     if (sc->sinkcount_pass1 == 0) return;
-    const int W = k.W, H = k.H;
-    const size_t N = (size_t)W * H;
+    const size_t cap = 1ull << edge_logcap(sc, logmax);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (size_t)gridDim.x * blockDim.x) {
+        ekey[i] = ~0ull;
+        ewt[i] = ~0ull;
+    }
+}
+
+__device__ __forceinline__ void edge_insert(unsigned long long* ekey, unsigned long long* ewt, int logcap,
+                                            unsigned long long key, unsigned long long w, DevScalars* sc) {
     const uint64_t capm = (1ull << logcap) - 1;
-    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
-        if (!mask[c]) continue;
-        const int x = (int)(c % W), y = (int)(c / W);
-        const int32_t a = ws[c];
-        const unsigned long long kz = dkey(z[c]);
+    uint64_t h = edge_hash(key, logcap);
+    for (int probes = 0;; ++probes) {
+        unsigned long long cur = ekey[h];
+        if (cur == ~0ull) cur = atomicCAS(ekey + h, ~0ull, key);
+        if (cur == ~0ull || cur == key) {
+            if (w < __ldcg(ewt + h)) atomicMin(ewt + h, w);
+            return;
+        }
+        h = (h + 1) & capm;
+        if (probes >= 4096) {
+            atomicOr(&sc->err, ErrFlags::kCapacity);
+            return;
+        }
+    }
+}
+
+constexpr int FE_BX = 32, FE_BY = 8;
+constexpr int kEdgeSlots = 128;  // block-local pair table (a 32x8 tile borders few basin pairs)
+
+// identify_watershed_boundary_write_backMFD (newflow.cu:787-877): the minimum
+// boundary height per unordered basin pair, in an open-addressing table.  A
+// cell pair with different labels is a boundary at the higher cell's height
+// (the reference visits it from the cell with zs[this] >= zs[idx]).  Labels and
+// height keys of a 32x8 tile and its halo sit in shared memory, so interior
+// cells cost eight shared-memory compares; the tile's pairs are first reduced
+// in a block-local table and then merged into the global one, one insert per
+// distinct pair and tile.
+__global__ void __launch_bounds__(FE_BX* FE_BY)
+    k_flood_edges(const double* __restrict__ z, const uint8_t* __restrict__ mask, const int32_t* __restrict__ ws,
+                  unsigned long long* ekey, unsigned long long* ewt, int logmax, ModelConsts k, DevScalars* sc) {
+    if (sc->sinkcount_pass1 == 0) return;
+    __shared__ int32_t sw[FE_BY + 2][FE_BX + 2];
+    __shared__ unsigned long long sk[FE_BY + 2][FE_BX + 2];
+    __shared__ unsigned long long tkey[kEdgeSlots], twt[kEdgeSlots];
+    const int W = k.W, H = k.H;
+    const int logcap = edge_logcap(sc, logmax);
+    const int x0 = blockIdx.x * FE_BX, y0 = blockIdx.y * FE_BY;
+    const int tid = threadIdx.y * FE_BX + threadIdx.x;
+    for (int t = tid; t < kEdgeSlots; t += FE_BX * FE_BY) {
+        tkey[t] = ~0ull;
+        twt[t] = ~0ull;
+    }
+    for (int t = tid; t < (FE_BX + 2) * (FE_BY + 2); t += FE_BX * FE_BY) {
+        const int ly = t / (FE_BX + 2), lx = t % (FE_BX + 2);
+        const int gx = x0 + lx - 1, gy = y0 + ly - 1;
+        int32_t lab = -1;  // outside the grid: no neighbour
+        unsigned long long key = 0;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            const size_t g = (size_t)gy * W + gx;
+            lab = ws[g];
+            key = dkey(z[g]);
+        }
+        sw[ly][lx] = lab;
+        sk[ly][lx] = key;
+    }
+    __syncthreads();
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
+    if (x < W && y < H && mask[(size_t)y * W + x]) {
+        const int32_t a = sw[ly][lx];
+        const unsigned long long kz = sk[ly][lx];
+#pragma unroll
         for (int d = 0; d < 8; ++d) {
-            const int nx = x + dir_dx(d), ny = y + dir_dy(d);
-            if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
-            const size_t nb = (size_t)ny * W + nx;
-            const int32_t b = ws[nb];
-            if (a == b) continue;
-            const unsigned long long kn = dkey(z[nb]);
+            const int32_t b = sw[ly + dir_dy(d)][lx + dir_dx(d)];
+            if (b < 0 || b == a) continue;
+            const unsigned long long kn = sk[ly + dir_dy(d)][lx + dir_dx(d)];
             if (kz == 0 || kn == 0 || kz < kn) continue;  // zs[this] >= zs[idx] is false for NaN
             const unsigned long long key = ((unsigned long long)(uint32_t)min(a, b) << 32) | (uint32_t)max(a, b);
-            uint64_t h = edge_hash(key, logcap);
-            int probes = 0;
-            for (;;) {
-                unsigned long long cur = ekey[h];
-                if (cur == ~0ull) cur = atomicCAS(ekey + h, ~0ull, key);
+            uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 57);
+            bool done = false;
+            for (int p = 0; p < kEdgeSlots; ++p) {
+                const unsigned long long cur = atomicCAS(&tkey[h], ~0ull, key);
                 if (cur == ~0ull || cur == key) {
-                    if (kz < __ldcg(ewt + h)) atomicMin(ewt + h, kz);
+                    atomicMin(&twt[h], kz);
+                    done = true;
                     break;
                 }
-                h = (h + 1) & capm;
-                if (++probes > 4096) {
-                    atomicOr(&sc->err, ErrFlags::kCapacity);
-                    break;
-                }
+                h = (h + 1) & (kEdgeSlots - 1);
             }
+            if (!done) edge_insert(ekey, ewt, logcap, key, kz, sc);
         }
+    }
+    __syncthreads();
+    for (int t = tid; t < kEdgeSlots; t += FE_BX * FE_BY) {
+        if (tkey[t] != ~0ull) edge_insert(ekey, ewt, logcap, tkey[t], twt[t], sc);
     }
 }
 
 // Compact the table into an edge list and count the labels on edges
 // (data->sinkcount, newflow.cu:1044-1045).  Labels on edges start unreached.
 __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, const unsigned long long* __restrict__ ewt,
-                                int64_t cap, int32_t* ea, int32_t* eb, unsigned long long* ew,
+                                int logmax, int32_t* ea, int32_t* eb, unsigned long long* ew,
                                 unsigned long long* raise, int32_t* seen, int32_t epoch, int32_t* bid,
                                 int32_t* blab, DevScalars* sc, DemCtx dc) {
     if (sc->sinkcount_pass1 == 0) return;
+    const size_t cap = 1ull << edge_logcap(sc, logmax);
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)cap; base += (size_t)gridDim.x * blockDim.x) {
         const size_t i = base + threadIdx.x;
         bool has = false;
@@ -984,14 +1055,16 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
         void* args[] = {(void*)&ws, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc};
         if ((r = coop("k_flood_jump", (const void*)k_flood_jump, s.max_coop_blocks, args, L)) != LEM_OK) return r;
     }
-    int logcap = 0;
-    while ((1ll << logcap) < s.ecap) ++logcap;
-    LEM_CUDA_TRY(cudaMemsetAsync(s.ekey, 0xff, sizeof(unsigned long long) * s.ecap, L.st));
-    LEM_CUDA_TRY(cudaMemsetAsync(s.ewt, 0xff, sizeof(unsigned long long) * s.ecap, L.st));
-    LEM_LAUNCH(L, k_flood_edges, flat_blocks(N, T, big), T, s.z, s.mask, s.ws, s.ekey, s.ewt, logcap, k, s.sc);
+    int logmax = 0;
+    while ((1ll << logmax) < s.ecap) ++logmax;
+    LEM_LAUNCH(L, k_edge_clear, flat_blocks((size_t)s.ecap, T, big), T, s.ekey, s.ewt, logmax, s.sc);
+    {
+        const dim3 eb(FE_BX, FE_BY), eg((k.W + FE_BX - 1) / FE_BX, (k.H + FE_BY - 1) / FE_BY);
+        LEM_LAUNCH(L, k_flood_edges, eg, eb, s.z, s.mask, s.ws, s.ekey, s.ewt, logmax, k, s.sc);
+    }
     static int32_t epoch = 0;
     ++epoch;
-    LEM_LAUNCH(L, k_flood_compact, flat_blocks((size_t)s.ecap, T, big), T, s.ekey, s.ewt, s.ecap, s.edge_a, s.edge_b,
+    LEM_LAUNCH(L, k_flood_compact, flat_blocks((size_t)s.ecap, T, big), T, s.ekey, s.ewt, logmax, s.edge_a, s.edge_b,
                s.edge_w, s.raise, s.label_seen, epoch, s.bid, s.blab, s.sc, s.dems);
     {
         const int32_t* ea = s.edge_a;
