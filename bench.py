@@ -250,11 +250,12 @@ class GridWork:
     """One large grid on one handle (the plain path)."""
 
     def __init__(self, lem, S, args, rank, total_steps):
-        self.sc = S.config_large(2 + rank, n=args.grid, steps=total_steps)
+        self.sc = S.config_large(2 + rank, n=args.grid, steps=max(total_steps, 100))  # the 100-step series
         st = S.initial_state(self.sc.dem, 30.0, self.sc.init_rain, self.sc.init_temp)
         self.cells = int((st["mask"] == 1).sum())
         self.g = lem.Model(self.sc.dem, 30.0, self.sc.init_rain, self.sc.init_temp)
         self.g.set_state(st)
+        self.g.graphs(not args.no_graphs)
         self.lem = lem
 
     def step(self, i):
@@ -292,7 +293,9 @@ class EnsembleWork:
     def __init__(self, lem, S, args, rank, total_steps):
         from parallem_gb300.packing import TilePacker
         self.lem = lem
-        self.ens = S.config_ensemble(4 + rank, count=args.dems, steps=max(total_steps, 8))
+        # 200-step climate series per DEM (the DEMs do not depend on the steps run)
+        assert total_steps <= 200, "the ensemble's climate series hold 200 steps"
+        self.ens = S.config_ensemble(4 + rank, count=args.dems, steps=200)
         order = sorted(range(len(self.ens)), key=lambda i: -self.ens[i].dem.size)
         W = args.canvas
         H = 1024
@@ -313,6 +316,7 @@ class EnsembleWork:
             self.ids[i] = k
             self.cells += int((st["mask"] == 1).sum())
         self.g = self.b  # timing, profiling and launch counts of the batch handle
+        self.b.graphs(not args.no_graphs)
 
     def step(self, i):
         for sc, k in zip(self.ens, self.ids):
@@ -446,6 +450,8 @@ def main():
     ap.add_argument("--canvas", type=int, default=8192, help="width of the ensemble's canvas")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path sample of the ensemble")
+    ap.add_argument("--no-graphs", action="store_true", help="step eagerly instead of one CUDA graph per step")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch schedule (no autotuning steps)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -462,39 +468,57 @@ def main():
         build.build()
     barrier(dist)
     lem.select_device(local)
-    total_steps = args.warmup + 2 * args.steps
+    tune_steps = 0 if args.no_tune else 4  # lem_autotune: one step per candidate schedule
+    total_steps = tune_steps + args.warmup + 3 * args.steps
     work = (EnsembleWork if args.workload == "ensemble" else GridWork)(lem, S, args, rank, total_steps)
     g = work.g
     cells = work.cells
 
-    # warm-up steps (untimed)
-    for i in range(args.warmup):
+    # autotuning steps, then warm-up steps (untimed)
+    if tune_steps:
+        g.autotune(1)
+        for i in range(tune_steps):
+            work.step(i)
+    for i in range(tune_steps, tune_steps + args.warmup):
         work.step(i)
     g.synchronize()
+    tuning = g.tuning()
     barrier(dist)
+    i0 = tune_steps + args.warmup  # step index of the first timed step
 
     # timed region 1: resident state, device events on the library's stream
+    # (each step one CUDA graph launch unless --no-graphs)
     launches0 = g.launches
-    g.profiling(True)
     with ClockSampler(local) as clk:
         g.record(0)
-        for i in range(args.warmup, args.warmup + args.steps):
+        for i in range(i0, i0 + args.steps):
             work.step(i)
         g.record(1)
         ms = g.elapsed_ms(0, 1)
-    prof = g.profile()
-    g.profiling(False)
     g.synchronize()
     launches = g.launches - launches0
     ms_max = reduce_max(dist, ms)
     cells_all = reduce_sum(dist, cells)
     value = cells_all * args.steps / (ms_max / 1e3)
 
-    # timed region 2: end to end through the C ABI with host buffers
+    # timed region 2: the same steps launched eagerly with a pair of events
+    # around every kernel (the per-kernel times and the roofline's duration)
+    barrier(dist)
+    g.profiling(True)
+    g.record(2)
+    for i in range(i0 + args.steps, i0 + 2 * args.steps):
+        work.step(i)
+    g.record(3)
+    eager_ms = g.elapsed_ms(2, 3)
+    prof = g.profile()
+    g.profiling(False)
+    g.synchronize()
+
+    # timed region 3: end to end through the C ABI with host buffers
     barrier(dist)
     h2d = d2h = 0
     t0 = time.perf_counter()
-    for j, i in enumerate(range(args.warmup + args.steps, args.warmup + 2 * args.steps)):
+    for j, i in enumerate(range(i0 + 2 * args.steps, i0 + 3 * args.steps)):
         a, b = work.e2e_step(i, j)
         h2d += a
         d2h += b
@@ -549,8 +573,13 @@ def main():
                      "step_level": {"bytes_per_cell_timestep": B_ALG,
                                     "achieved": B_ALG * cells / (step_ms / 1e3) / 1e9,
                                     "frac": B_ALG * cells / (step_ms / 1e3) / 1e9 / hbm}},
+        "graphs": not args.no_graphs,
+        "tuning": tuning,
         "kernels": {k: {"launches": v[0], "ms_per_step": v[1] / args.steps} for k, v in
                     sorted(prof.items(), key=lambda kv: -kv[1][1])},
+        "kernel_timing": {"source": f"{args.steps} eagerly launched steps after the timed region, "
+                                    "CUDA events around every kernel on the library's stream",
+                          "eager_ms_per_step": eager_ms / args.steps},
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
     }

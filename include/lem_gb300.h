@@ -242,6 +242,38 @@ lem_status lem_dem_get_totals(lem_handle* h, int32_t id, lem_totals* out);  /* s
 /* One timestep of every active DEM; flags as lem_step, for all DEMs. */
 lem_status lem_step_batch(lem_handle* h, uint32_t flags);
 
+/* CUDA-graph steps (off by default; no counterpart in the reference, which
+ * launches every kernel from the host).  When on, lem_step and lem_step_batch
+ * upload the per-DEM inputs and then launch the whole timestep as one graph,
+ * captured on first use and again whenever the launch configuration changes
+ * (a DEM joins or leaves, other step flags); results equal eager steps bit for
+ * bit.  While per-kernel profiling (lem_set_profiling) is on, steps launch
+ * eagerly.  The single-stage calls (lem_flow_direction ...) are always eager. */
+lem_status lem_set_graphs(lem_handle* h, int32_t on);
+
+/* Autotuner of the launch schedule (no counterpart in the reference).  Over
+ * the handle's next 4 * steps_per_candidate steps (lem_step or lem_step_batch;
+ * real steps of the model, launched eagerly), candidate schedules are run and
+ * every tunable kernel is timed with events; afterwards each kernel keeps its
+ * fastest value.  Tuned are the blocks of the cooperative kernels (1 to 4 per
+ * SM, at most the co-resident count) and, for the in-tile waves, the round
+ * size below which the rest of a wave runs on one warp.  Results are the same
+ * under every schedule.  LEM_ERR_STATE while profiling is on (and
+ * lem_set_profiling / lem_profile_read return it while tuning). */
+#define LEM_TUNE_COOP 8   /* k_plateau_relax, k_flood_merge, k_flood_jump, k_flood_spill,
+                             k_fat_coarse, k_fa_walk, k_sedt_coarse, k_sed_walk */
+#define LEM_TUNE_WAVES 4  /* k_fat_local, k_fat_final, k_sedt_local, k_sedt_final */
+typedef struct lem_tuning {
+    int32_t state;                          /* 0 default schedule, 1 tuning, 2 tuned            */
+    int32_t steps_left;                     /* tuning steps still to run                        */
+    int32_t coop_blocks[LEM_TUNE_COOP];     /* blocks each cooperative kernel launches with    */
+    int32_t narrow_below[LEM_TUNE_WAVES];   /* in-tile waves: smaller rounds run on one warp (0: never) */
+    double default_ms;                      /* ms per step of these kernels, default schedule  */
+    double tuned_ms;                        /*   and with the schedule kept (as measured)       */
+} lem_tuning;
+lem_status lem_autotune(lem_handle* h, int32_t steps_per_candidate);
+lem_status lem_get_tuning(lem_handle* h, lem_tuning* out);
+
 /* Restart snapshot of one DEM's resident state: the DEM, the DEM of the
  * initial climate grids, the mask, the persistent slopes (whose stale entries
  * the next steps read), the seven soil and vegetation fields, the outlet and

@@ -69,6 +69,28 @@ lem_status cuda_fail(cudaError_t e, const char* what, const char* file, int line
 
 using namespace lem;
 
+// The autotuner: over its next steps a handle runs candidate schedules (the
+// cooperative kernels' blocks per SM, the in-tile waves' narrow threshold),
+// times every tunable kernel with events, and then keeps for each kernel the
+// fastest value.  Results do not depend on the schedule: every loop runs to a
+// unique fixpoint, sums are pulled in a fixed order, and an in-tile round holds
+// the same cells on one warp or on many.
+constexpr int kTuneCands = 4;
+constexpr int kTuneBlocksPerSm[kTuneCands] = {1, 2, 3, 4};
+constexpr int kTuneNarrowVals = 3;
+constexpr int kTuneNarrow[kTuneNarrowVals] = {0, 32, 64};
+const char* const kCoopNames[kCoopKernels] = {"k_plateau_relax", "k_flood_merge", "k_flood_jump", "k_flood_spill",
+                                              "k_fat_coarse",    "k_fa_walk",     "k_sedt_coarse", "k_sed_walk"};
+const char* const kWaveNames[kTileWaves] = {"k_fat_local", "k_fat_final", "k_sedt_local", "k_sedt_final"};
+struct Tuner {
+    int state = 0;  // 0 default schedule, 1 tuning, 2 tuned
+    int cand = 0, step_in = 0, per = 1;
+    double coop_ms[kCoopKernels][kTuneCands] = {};     // device ms, summed over the candidate's steps
+    double wave_ms[kTileWaves][kTuneNarrowVals] = {};  // device ms, summed over the steps of each value
+    int wave_n[kTuneNarrowVals] = {};                  // steps measured per narrow value
+    double default_ms = 0, tuned_ms = 0;
+};
+
 // A DEM of the handle as the host tracks it: its region and its climate state.
 struct HostDem {
     bool active = false;
@@ -95,12 +117,20 @@ struct lem_handle {
     DemOut* dem_out = nullptr;
     uint16_t* dem_of = nullptr;
     int32_t* chunks = nullptr;
+    int32_t* live = nullptr;       // device list of the tiles holding a DEM region (batch grids)
+    bool live_dirty = true;        // a DEM joined or left since the list was uploaded
     DemOut* host_out = nullptr;    // pinned mirror of dem_out
     void* staging = nullptr;       // pinned host buffer for field conversions, grown on demand
     size_t staging_bytes = 0;
     DevScalars* host_sc = nullptr; // pinned mirror of the device scalars
     Profiler prof;
     bool profiling = false;
+    bool graphs = false;           // steps replay a captured CUDA graph (lem_set_graphs)
+    cudaGraphExec_t gexec = nullptr;
+    int32_t gkey[3] = {-1, -1, -1};  // chunks, visited tiles and step flags the graph was captured for
+    uint64_t glaunches = 0;        // kernel launches in one replay
+    int sms = 0;                   // SMs of the handle's device
+    Tuner tune;
     cudaEvent_t events[16] = {};
     Launch launch() { return Launch{st, &launches, profiling ? &prof : nullptr}; }
 };
@@ -219,6 +249,7 @@ __global__ void k_region(DevState s, uint16_t* of, int W, int x0, int y0, int w,
         s.ero[g] = s.inci[g] = s.geli[g] = s.depo[g] = s.dz[g] = s.wc[g] = s.wp[g] = 0.f;
         s.contrib[g] = 0;
         s.ws[g] = 0;
+        s.sp[g] = 0.f;
     }
 }
 
@@ -265,6 +296,24 @@ lem_status prepare(lem_handle* h) {
     LEM_CUDA_TRY(cudaMemcpyAsync(h->dem_in, in.data(), sizeof(DemIn) * n, cudaMemcpyHostToDevice, h->st));
     LEM_CUDA_TRY(cudaMemcpyAsync(h->chunks, chunk.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, h->st));
     h->s.n_chunks = chunk[n];
+    if (h->batch && h->live_dirty) {
+        // the tiles covered by some DEM region, in ascending order
+        const int tw = (h->k.W + kTile - 1) / kTile, th = (h->k.H + kTile - 1) / kTile;
+        std::vector<uint8_t> on((size_t)tw * th, 0);
+        for (const HostDem& r : h->dems) {
+            if (!r.active) continue;
+            for (int ty = r.y0 / kTile; ty < (r.y0 + r.h + kTile - 1) / kTile; ++ty)
+                for (int tx = r.x0 / kTile; tx < (r.x0 + r.w + kTile - 1) / kTile; ++tx) on[(size_t)ty * tw + tx] = 1;
+        }
+        std::vector<int32_t> live;
+        for (size_t t = 0; t < on.size(); ++t)
+            if (on[t]) live.push_back((int32_t)t);
+        LEM_CUDA_TRY(cudaMemcpyAsync(h->live, live.data(), sizeof(int32_t) * live.size(), cudaMemcpyHostToDevice,
+                                     h->st));
+        h->s.live = h->live;
+        h->s.n_live = (int32_t)live.size();
+        h->live_dirty = false;
+    }
     return LEM_OK;
 }
 
@@ -609,10 +658,13 @@ lem_status create_common(const lem_grid_desc* grid, const lem_params* params, in
     ALLOC(h->chunks, (size_t)max_dems + 1);
     if (batch) {
         ALLOC(h->dem_of, N);
+        ALLOC(h->live, (size_t)((grid->width + kTile - 1) / kTile) * ((grid->height + kTile - 1) / kTile));
     }
 #undef ALLOC
     s.chunk_start = h->chunks;
     s.dems = DemCtx{h->dem_of, h->dem_in, h->dem_out, max_dems};
+    s.live = nullptr;  // a single grid visits every tile; a batch lists its DEMs' tiles before each stage
+    s.n_live = (int32_t)(((grid->width + kTile - 1) / kTile) * ((grid->height + kTile - 1) / kTile));
     std::vector<float> tab;
     dreybrodt_table(tab);
     e = cudaMemcpyAsync(s.temp_tab, tab.data(), sizeof(float) * kTabN, cudaMemcpyHostToDevice, h->st);
@@ -649,7 +701,84 @@ lem_status create_common(const lem_grid_desc* grid, const lem_params* params, in
     for (int i = 0; i < fa_coop_kernel_count; ++i) blocks = std::min(blocks, coop_blocks_for(fa_coop_kernels[i], 256, 0));
     for (int i = 0; i < mod_coop_kernel_count; ++i) blocks = std::min(blocks, coop_blocks_for(mod_coop_kernels[i], 256, 0));
     s.max_coop_blocks = blocks;
+    for (int i = 0; i < kCoopKernels; ++i) s.coop_blocks[i] = blocks;
+    for (int i = 0; i < kTileWaves; ++i) h->k.narrow_below[i] = 0;
+    cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device);
     *out = h;
+    return LEM_OK;
+}
+
+// Per-kernel launches and device ms recorded since the last collection.
+lem_status profile_collect(lem_handle* h, std::vector<lem_kernel_stat>& agg) {
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    agg.clear();
+    for (const Profiler::Rec& r : h->prof.recs) {
+        float ms = 0.f;
+        LEM_CUDA_TRY(cudaEventElapsedTime(&ms, h->prof.pool[r.a], h->prof.pool[r.b]));
+        size_t j = 0;
+        while (j < agg.size() && std::strncmp(agg[j].name, r.name, sizeof(agg[j].name)) != 0) ++j;
+        if (j == agg.size()) {
+            lem_kernel_stat z{};
+            std::strncpy(z.name, r.name, sizeof(z.name) - 1);
+            agg.push_back(z);
+        }
+        agg[j].launches += 1;
+        agg[j].total_ms += ms;
+    }
+    h->prof.recs.clear();
+    h->prof.used = 0;
+    return LEM_OK;
+}
+
+// The schedule of the tuner's current candidate.
+void tune_apply(lem_handle* h) {
+    const Tuner& t = h->tune;
+    const int blocks = std::max(1, std::min(h->s.max_coop_blocks, kTuneBlocksPerSm[t.cand] * h->sms));
+    for (int i = 0; i < kCoopKernels; ++i) h->s.coop_blocks[i] = blocks;
+    for (int i = 0; i < kTileWaves; ++i) h->k.narrow_below[i] = kTuneNarrow[t.cand % kTuneNarrowVals];
+}
+
+// Books the kernel times of a tuning step; after the last candidate, keeps the
+// fastest schedule of every kernel.
+lem_status tune_record(lem_handle* h) {
+    Tuner& t = h->tune;
+    std::vector<lem_kernel_stat> agg;
+    lem_status r = profile_collect(h, agg);
+    if (r != LEM_OK) return r;
+    for (const lem_kernel_stat& st : agg) {
+        for (int i = 0; i < kCoopKernels; ++i)
+            if (!std::strcmp(st.name, kCoopNames[i])) t.coop_ms[i][t.cand] += st.total_ms;
+        for (int i = 0; i < kTileWaves; ++i)
+            if (!std::strcmp(st.name, kWaveNames[i])) t.wave_ms[i][t.cand % kTuneNarrowVals] += st.total_ms;
+    }
+    t.wave_n[t.cand % kTuneNarrowVals] += 1;
+    if (++t.step_in < t.per) return LEM_OK;
+    t.step_in = 0;
+    if (++t.cand < kTuneCands) return LEM_OK;
+    // the default schedule is every co-resident block (the largest candidate) and no narrow rounds
+    t.default_ms = t.tuned_ms = 0;
+    for (int i = 0; i < kCoopKernels; ++i) {
+        int best = kTuneCands - 1;
+        for (int c = 0; c < kTuneCands; ++c)
+            if (t.coop_ms[i][c] < t.coop_ms[i][best]) best = c;
+        h->s.coop_blocks[i] = std::max(1, std::min(h->s.max_coop_blocks, kTuneBlocksPerSm[best] * h->sms));
+        t.default_ms += t.coop_ms[i][kTuneCands - 1] / t.per;
+        t.tuned_ms += t.coop_ms[i][best] / t.per;
+    }
+    for (int i = 0; i < kTileWaves; ++i) {
+        int best = 0;
+        for (int v = 0; v < kTuneNarrowVals; ++v)
+            if (t.wave_ms[i][v] / t.wave_n[v] < t.wave_ms[i][best] / t.wave_n[best]) best = v;
+        h->k.narrow_below[i] = kTuneNarrow[best];
+        t.default_ms += t.wave_ms[i][0] / t.wave_n[0];
+        t.tuned_ms += t.wave_ms[i][best] / t.wave_n[best];
+    }
+    t.state = 2;
+    h->profiling = false;
+    if (h->gexec) {  // captured with other launch arguments
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
     return LEM_OK;
 }
 
@@ -664,6 +793,48 @@ lem_status run_stage(lem_handle* h, int stage, uint32_t flags) {
         return launch_flow_accumulation(h->s, h->k, f, L);
     }
     return launch_erosion(h->s, h->k, flags, L);
+}
+
+// A whole timestep as one graph launch.  The per-DEM inputs are uploaded first
+// (the kernels read them from device memory); the step's launches are captured
+// once per launch configuration (chunk count, visited tiles, step flags) and
+// replayed while it holds.  Every loop decision of a step is taken on the
+// device, so a replay runs exactly the kernels an eager step runs.
+lem_status graph_step(lem_handle* h, uint32_t flags) {
+    lem_status r = prepare(h);
+    if (r != LEM_OK) return r;
+    uint32_t f = flags & ~LEM_STEP_SET_OUTLET_FROM_FA;
+    if (any_flag(h, LEM_STEP_SET_OUTLET_FROM_FA)) f |= LEM_STEP_SET_OUTLET_FROM_FA;
+    const int32_t key[3] = {h->s.n_chunks, h->s.n_live, (int32_t)f};
+    if (!h->gexec || std::memcmp(key, h->gkey, sizeof key) != 0) {
+        if (h->gexec) {
+            cudaGraphExecDestroy(h->gexec);
+            h->gexec = nullptr;
+        }
+        LEM_CUDA_TRY(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+        uint64_t n = 0;
+        const Launch L{h->st, &n, nullptr};
+        r = launch_flow_direction(h->s, h->k, L);
+        if (r == LEM_OK) r = launch_flow_accumulation(h->s, h->k, f, L);
+        if (r == LEM_OK) r = launch_erosion(h->s, h->k, flags, L);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->st, &g);
+        if (r != LEM_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return r != LEM_OK ? r : cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&h->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            h->gexec = nullptr;
+            return cuda_fail(ei, "cudaGraphInstantiate", __FILE__, __LINE__);
+        }
+        std::memcpy(h->gkey, key, sizeof key);
+        h->glaunches = n;
+    }
+    LEM_CUDA_TRY(cudaGraphLaunch(h->gexec, h->st));
+    h->launches += h->glaunches;
+    return LEM_OK;
 }
 
 }  // namespace
@@ -687,6 +858,7 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
 lem_status lem_destroy(lem_handle* h) {
     if (!h) return LEM_ERR_INVALID;
     if (h->st) cudaStreamSynchronize(h->st);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
     for (cudaEvent_t e : h->prof.pool) cudaEventDestroy(e);
     for (cudaEvent_t e : h->events)
         if (e) cudaEventDestroy(e);
@@ -762,6 +934,21 @@ lem_status lem_step(lem_handle* h, const lem_climate* c, uint32_t flags) {
     lem_status r;
     if (!h) return LEM_ERR_INVALID;
     if (c && (r = lem_set_climate(h, c)) != LEM_OK) return r;
+    if (h->tune.state == 1) {
+        if (h->batch || !h->dem_set) return LEM_ERR_STATE;
+        tune_apply(h);
+        h->dems[0].next_flags = flags;
+        if ((r = run_stage(h, 0, 0)) == LEM_OK && (r = run_stage(h, 1, flags)) == LEM_OK) r = run_stage(h, 2, flags);
+        h->dems[0].next_flags = 0;
+        return r != LEM_OK ? r : tune_record(h);
+    }
+    if (h->graphs && !h->profiling) {
+        if (h->batch || !h->dem_set) return LEM_ERR_STATE;
+        h->dems[0].next_flags = flags;
+        r = graph_step(h, flags);
+        h->dems[0].next_flags = 0;
+        return r;
+    }
     if ((r = lem_flow_direction(h)) != LEM_OK) return r;
     if ((r = lem_flow_accumulation(h, flags)) != LEM_OK) return r;
     return lem_erosion(h, flags);
@@ -834,6 +1021,7 @@ lem_status lem_dem_add(lem_handle* h, int32_t x0, int32_t y0, int32_t width, int
     LEM_CUDA_TRY(cudaMemcpyAsync(&h->dem_out[slot], &zero, sizeof zero, cudaMemcpyHostToDevice, h->st));
     LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
     d.active = true;
+    h->live_dirty = true;
     *id = slot;
     return LEM_OK;
 }
@@ -850,6 +1038,7 @@ lem_status lem_dem_remove(lem_handle* h, int32_t id) {
     if ((r = region_op(h, h->dems[id], -1)) != LEM_OK) return r;
     LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
     h->dems[id] = HostDem{};
+    h->live_dirty = true;
     return LEM_OK;
 }
 
@@ -1021,11 +1210,55 @@ lem_status lem_snapshot_load(lem_handle* h, int32_t id, const void* host, size_t
 lem_status lem_step_batch(lem_handle* h, uint32_t flags) {
     if (!h || !h->batch) return LEM_ERR_INVALID;
     lem_status r;
-    if ((r = run_stage(h, 0, 0)) != LEM_OK) return r;
-    if ((r = run_stage(h, 1, flags)) != LEM_OK) return r;
-    r = run_stage(h, 2, flags);
+    if (h->tune.state == 1) {
+        tune_apply(h);
+        if ((r = run_stage(h, 0, 0)) == LEM_OK && (r = run_stage(h, 1, flags)) == LEM_OK) r = run_stage(h, 2, flags);
+        if (r == LEM_OK) r = tune_record(h);
+    } else if (h->graphs && !h->profiling) {
+        r = graph_step(h, flags);
+    } else {
+        if ((r = run_stage(h, 0, 0)) != LEM_OK) return r;
+        if ((r = run_stage(h, 1, flags)) != LEM_OK) return r;
+        r = run_stage(h, 2, flags);
+    }
     for (HostDem& d : h->dems) d.next_flags = 0;
     return r;
+}
+
+lem_status lem_autotune(lem_handle* h, int32_t steps_per_candidate) {
+    if (!h || steps_per_candidate < 1) return LEM_ERR_INVALID;
+    if (h->profiling || h->tune.state == 1) return LEM_ERR_STATE;
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    h->tune = Tuner{};
+    h->tune.state = 1;
+    h->tune.per = steps_per_candidate;
+    h->profiling = true;  // the tuning steps time every kernel
+    h->prof.recs.clear();
+    h->prof.used = 0;
+    return LEM_OK;
+}
+
+lem_status lem_get_tuning(lem_handle* h, lem_tuning* out) {
+    if (!h || !out) return LEM_ERR_INVALID;
+    std::memset(out, 0, sizeof *out);
+    out->state = h->tune.state;
+    out->steps_left = h->tune.state == 1 ? (kTuneCands - h->tune.cand) * h->tune.per - h->tune.step_in : 0;
+    for (int i = 0; i < kCoopKernels; ++i) out->coop_blocks[i] = h->s.coop_blocks[i];
+    for (int i = 0; i < kTileWaves; ++i) out->narrow_below[i] = h->k.narrow_below[i];
+    out->default_ms = h->tune.default_ms;
+    out->tuned_ms = h->tune.tuned_ms;
+    return LEM_OK;
+}
+
+lem_status lem_set_graphs(lem_handle* h, int32_t on) {
+    if (!h) return LEM_ERR_INVALID;
+    h->graphs = on != 0;
+    if (!h->graphs && h->gexec) {
+        LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    return LEM_OK;
 }
 
 void* lem_stream(lem_handle* h) { return h ? (void*)h->st : nullptr; }
@@ -1052,6 +1285,7 @@ lem_status lem_event_elapsed(lem_handle* h, int32_t from, int32_t to, float* ms)
 
 lem_status lem_set_profiling(lem_handle* h, int32_t on) {
     if (!h) return LEM_ERR_INVALID;
+    if (h->tune.state == 1) return LEM_ERR_STATE;
     LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
     h->profiling = on != 0;
     h->prof.recs.clear();
@@ -1061,23 +1295,10 @@ lem_status lem_set_profiling(lem_handle* h, int32_t on) {
 
 lem_status lem_profile_read(lem_handle* h, lem_kernel_stat* out, int32_t cap, int32_t* count) {
     if (!h || !count || (cap > 0 && !out)) return LEM_ERR_INVALID;
-    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
+    if (h->tune.state == 1) return LEM_ERR_STATE;
     std::vector<lem_kernel_stat> agg;
-    for (const Profiler::Rec& r : h->prof.recs) {
-        float ms = 0.f;
-        LEM_CUDA_TRY(cudaEventElapsedTime(&ms, h->prof.pool[r.a], h->prof.pool[r.b]));
-        size_t j = 0;
-        while (j < agg.size() && std::strncmp(agg[j].name, r.name, sizeof(agg[j].name)) != 0) ++j;
-        if (j == agg.size()) {
-            lem_kernel_stat z{};
-            std::strncpy(z.name, r.name, sizeof(z.name) - 1);
-            agg.push_back(z);
-        }
-        agg[j].launches += 1;
-        agg[j].total_ms += ms;
-    }
-    h->prof.recs.clear();
-    h->prof.used = 0;
+    lem_status r = profile_collect(h, agg);
+    if (r != LEM_OK) return r;
     *count = (int32_t)agg.size();
     for (int32_t i = 0; i < cap && i < (int32_t)agg.size(); ++i) out[i] = agg[i];
     return LEM_OK;

@@ -89,6 +89,7 @@ struct DevScalars {
     int32_t tiled_ok;                // 1: this step's accumulation may take the tiled path
     int32_t tile_src;                // tile outlets with no pending inflow (coarse sources)
     int32_t sed_tiled_ok;            // 1: this step's sediment routing may take the tiled path
+    int32_t epoch;                   // flow-direction stages run so far (first-seen marks of basin labels)
 };
 
 // The DEMs of a handle.  A single grid is one DEM covering the whole grid; a

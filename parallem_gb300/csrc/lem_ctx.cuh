@@ -32,7 +32,14 @@ struct ModelConsts {  // per-handle constants derived on the host in double
     float rescale_weather;  // 10000 * (10000 / cs^2)      eroincidep.cu:628
     float rescale_veg;      // 10000 / cs^2                Data.cpp:124
     float erod_const;       // 0.043*(struct-2) + 0.033*(perm-3)
+    int32_t narrow_below[4];  // in-tile waves (TileWave order): rounds with fewer queued cells run on one warp, 0: never
 };
+
+// The in-tile waves and the cooperative kernels whose schedule the autotuner
+// sets (the order of lem_tuning's arrays).
+enum TileWave { kTwFatLocal = 0, kTwFatFinal, kTwSedLocal, kTwSedFinal, kTileWaves };
+enum CoopKernel { kCkPlateau = 0, kCkMerge, kCkJump, kCkSpill, kCkFatCoarse, kCkFaWalk, kCkSedCoarse, kCkSedWalk,
+                  kCoopKernels };
 
 
 struct DevState {
@@ -93,9 +100,39 @@ struct DevState {
     DemCtx dems;                // the DEMs of the grid
     int32_t* chunk_start;       // streaming passes: first chunk of each DEM (n + 1 entries)
     int32_t n_chunks;
+    int32_t* live;              // batch grids: the tiles holding a DEM's region, ascending
+    int32_t n_live;             // tiles the canvas-wide kernels visit
     float* temp_tab;
     int32_t max_coop_blocks;    // co-resident blocks of the cooperative kernels
+    int32_t coop_blocks[kCoopKernels];  // blocks each cooperative kernel launches with (<= max_coop_blocks)
 };
+
+// The tiles a canvas-wide kernel visits: in a batch grid the 32x32 tiles that
+// hold a DEM's region (every other cell is nodata outside every DEM and keeps
+// the values its region was emptied with; no in-catchment cell has such a
+// neighbour), in a single grid every tile.  Position v of a visit is cell
+// v & 1023 of the (v >> 10)-th visited tile, row by row, so a warp covers one
+// 32-cell row of one tile and never two DEMs.
+static_assert(kTile == 32, "visit positions hold a 32x32 tile in 10 bits");
+struct TileSet {
+    const int32_t* id;  // visited tile ids; null: tiles 0 .. n-1
+    int n;
+    int tw;             // tiles per grid row
+    __device__ __forceinline__ int tile(int i) const { return id ? __ldg(id + i) : i; }
+    __host__ __device__ __forceinline__ size_t span() const { return (size_t)n << 10; }
+    // the cell at visit position v; false where an edge tile of a single grid
+    // extends past the grid
+    __device__ __forceinline__ bool cell(size_t v, int W, int H, int& x, int& y) const {
+        const int t = tile((int)(v >> 10));
+        const int o = (int)(v & 1023);
+        x = (t % tw) * kTile + (o & (kTile - 1));
+        y = (t / tw) * kTile + o / kTile;
+        return x < W && y < H;
+    }
+};
+inline TileSet tiles_of(const DevState& s, int W) {
+    return TileSet{s.live, s.n_live, (W + kTile - 1) / kTile};
+}
 
 // Streaming passes over the DEMs' regions run one block per chunk of kChunk
 // cells, every chunk inside one DEM, so block sums go to that DEM's totals.
@@ -147,6 +184,22 @@ struct Launch {
         ++*count;
     }
 };
+
+// A cooperative launch (grid-wide barriers) of 256-thread blocks, as a launch
+// attribute so that it can be captured into a CUDA graph.
+inline cudaError_t coop_launch(const void* fn, int blocks, void** args, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, args);
+}
 
 #define LEM_LAUNCH(L, kern, grid, block, ...)                  \
     do {                                                       \

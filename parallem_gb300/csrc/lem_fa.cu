@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(256)
     k_fat_local(const double* __restrict__ z, const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                 const float* __restrict__ w, float2* __restrict__ t_la, int32_t* __restrict__ t_dst,
                 int32_t* __restrict__ t_pend, int32_t* __restrict__ t_orng, int32_t* __restrict__ t_ent,
-                int32_t* srcs, ModelConsts k, DevScalars* sc) {
+                int32_t* srcs, ModelConsts k, DevScalars* sc, TileSet ts) {
     if (!sc->tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int16_t s_ofill[kTileEnt];
     __shared__ int s_no, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
-    const int t = blockIdx.x;
+    const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
     tile_load(z, mask, fd, W, H, tx0, ty0, s_code, s_cls);
     __syncthreads();
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(256)
             s_done[cur] = 1;
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
         },
-        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0, k.narrow_below[kTwFatLocal]);
     // the end of every in-tile path: pointer jumping (paths are shorter than 2^10 cells)
     for (int it = 0; it < 10; ++it) {
 #pragma unroll
@@ -447,7 +447,7 @@ __global__ void k_fat_coarse(const uint8_t* __restrict__ mask, const uint8_t* __
 __global__ void __launch_bounds__(256)
     k_fat_final(const double* __restrict__ z, const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                 const float* __restrict__ w, const int32_t* __restrict__ t_pend, float2* fa, ModelConsts k,
-                DevScalars* sc, DemCtx dc) {
+                DevScalars* sc, DemCtx dc, TileSet ts) {
     if (!sc->tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int16_t s_q[kTile * kTile];
     __shared__ int s_done, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
-    const int t = blockIdx.x;
+    const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
     tile_load(z, mask, fd, W, H, tx0, ty0, s_code, s_cls);
     // donors in other tiles: outlets of their tiles, final after the coarse wave
@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(256)
                 return -1;
             return rly * kTile + rlx;
         },
-        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0, k.narrow_below[kTwFatFinal]);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();
@@ -620,9 +620,10 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, uin
     LEM_LAUNCH(L, k_fa_prep, s.n_chunks, T, s.z, s.mask, s.fd, s.stone, s.totB, s.soilM, s.w, s.fa, s.pending,
                contrib, s.list_a, s.chunk_start, k, s.dems, s.sc);
     if (tiled) {
-        const int tiles = ((k.W + kTile - 1) / kTile) * ((k.H + kTile - 1) / kTile);
+        const TileSet ts = tiles_of(s, k.W);
+        const int tiles = ts.n;
         LEM_LAUNCH(L, k_fat_local, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_la, s.t_dst, s.t_pend, s.t_orng, s.t_ent,
-                   s.list_b, k, s.sc);
+                   s.list_b, k, s.sc, ts);
         const uint8_t* mask = s.mask;
         const uint8_t* fd = s.fd;
         const float2* tla = s.t_la;
@@ -638,10 +639,9 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, uin
         void* args[] = {(void*)&mask, (void*)&fd, (void*)&tla, (void*)&torng, (void*)&tent, (void*)&tdst,
                         (void*)&fa, (void*)&tpend, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc};
         L.pre("k_fat_coarse");
-        LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fat_coarse, dim3(s.max_coop_blocks), dim3(256),
-                                                 args, 0, L.st));
+        LEM_CUDA_TRY(coop_launch((const void*)k_fat_coarse, s.coop_blocks[kCkFatCoarse], args, L.st));
         L.post();
-        LEM_LAUNCH(L, k_fat_final, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_pend, s.fa, k, s.sc, s.dems);
+        LEM_LAUNCH(L, k_fat_final, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_pend, s.fa, k, s.sc, s.dems, ts);
     }
     {
         const uint8_t* mask = s.mask;
@@ -659,8 +659,7 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, uin
                         (void*)&contrib, (void*)&la, (void*)&lb, (void*)&kk,   (void*)&sc,  (void*)&dc,
                         (void*)&gate};
         L.pre("k_fa_walk");
-        LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fa_walk, dim3(s.max_coop_blocks), dim3(256), args,
-                                                 0, L.st));
+        LEM_CUDA_TRY(coop_launch((const void*)k_fa_walk, s.coop_blocks[kCkFaWalk], args, L.st));
         L.post();
     }
     if (flags & LEM_STEP_SET_OUTLET_FROM_FA) {  // some DEM moves its outlet this step
@@ -797,7 +796,7 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
         DemCtx dc{nullptr, nullptr, dem, 1};
         void* args[] = {(void*)&m, (void*)&c, (void*)&ww, (void*)&prop, (void*)&fa, (void*)&pending,
                         (void*)&contrib, (void*)&la, (void*)&lb, (void*)&k, (void*)&sc, (void*)&dc, (void*)&gate};
-        LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_fa_walk, dim3(nd.blocks), dim3(256), args, 0, st));
+        LEM_CUDA_TRY(coop_launch((const void*)k_fa_walk, nd.blocks, args, st));
     }
     k_na_out<<<blocks, T, 0, st>>>(fa, d_fa, N);
     LEM_CUDA_TRY(cudaGetLastError());

@@ -65,13 +65,14 @@ __device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t* l
 __global__ void __launch_bounds__(FD_BX* FD_BY)
     k_flowdirs(const double* __restrict__ z, const uint8_t* __restrict__ mask, float* __restrict__ slopes,
                uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, ModelConsts k, DevScalars* sc, DemCtx dc,
-               int pass) {
+               TileSet ts, int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
     __shared__ unsigned long long skey[FD_BY + 2][FD_BX + 2];
     __shared__ float shi[FD_BY + 2][FD_BX + 2];
     __shared__ float slo[FD_BY + 2][FD_BX + 2];
     const int W = k.W, H = k.H;
-    const int x0 = blockIdx.x * FD_BX, y0 = blockIdx.y * FD_BY;
+    const int t = ts.tile(blockIdx.x);
+    const int x0 = (t % ts.tw) * kTile, y0 = (t / ts.tw) * kTile + blockIdx.y * FD_BY;
     const int tid = threadIdx.y * FD_BX + threadIdx.x;
     for (int t = tid; t < (FD_BX + 2) * (FD_BY + 2); t += FD_BX * FD_BY) {
         int ly = t / (FD_BX + 2), lx = t % (FD_BX + 2);
@@ -212,13 +213,15 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
 // downslope direction; their distance starts at 2e7, every other cell at 0.
 __global__ void k_plateau_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
                                const uint8_t* __restrict__ mfd, float* __restrict__ sp, int32_t* cand, ModelConsts k,
-                               DevScalars* sc, int pass) {
+                               DevScalars* sc, TileSet ts, int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
     const size_t N = (size_t)k.W * k.H;
-    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += (size_t)gridDim.x * blockDim.x) {
-        const size_t c = base + threadIdx.x;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < ts.span(); base += (size_t)gridDim.x * blockDim.x) {
+        int x, y;
+        const bool in = ts.cell(base + threadIdx.x, k.W, k.H, x, y);
+        const size_t c = (size_t)y * k.W + x;
         bool is_c = false;
-        if (c < N) {
+        if (in) {
             float v = 0.f;
             if (mask[c] && sfd[c] == 0 && mfd[c] == 0) {
                 v = kFar;
@@ -414,15 +417,16 @@ __global__ void k_plateau_final(const double* __restrict__ z, const float* __res
 // other cells point at their SFD receiver, masked and edge cells are basin 0.
 __global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
                              uint8_t* __restrict__ sfd1, int32_t* ws, int32_t* sinks, unsigned long long* raise,
-                             int32_t* bid, ModelConsts k, DevScalars* sc, DemCtx dc) {
+                             int32_t* bid, ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts) {
     const int W = k.W, H = k.H;
     const size_t N = (size_t)W * H;
     int nsink = 0;
-    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += (size_t)gridDim.x * blockDim.x) {
-        const size_t c = base + threadIdx.x;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < ts.span(); base += (size_t)gridDim.x * blockDim.x) {
+        int x, y;
+        const bool in = ts.cell(base + threadIdx.x, W, H, x, y);
+        const size_t c = (size_t)y * W + x;
         bool sink = false;
-        if (c < N) {
-            const int x = (int)(c % W), y = (int)(c / W);
+        if (in) {
             int32_t v = 0;
             sfd1[c] = sfd[c];
             if (mask[c]) {
@@ -506,7 +510,8 @@ __global__ void k_flood_merge(const double* __restrict__ z, int32_t* ws, const i
 
 // identify_watershedMFD loop (newflow.cu:469-487): pointer jumping until every
 // cell holds the label of the sink (or basin 0) its SFD path ends in.
-__global__ void k_flood_jump(int32_t* ws, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc) {
+__global__ void k_flood_jump(int32_t* ws, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc,
+                             TileSet ts) {
     if (sc->sinkcount_pass1 == 0) return;
     cg::grid_group grid = cg::this_grid();
     const size_t N = (size_t)k.W * k.H;
@@ -519,11 +524,13 @@ __global__ void k_flood_jump(int32_t* ws, int32_t* list_a, int32_t* list_b, Mode
         cnt[2] = 0;
     }
     grid.sync();
-    // round 0 over every cell
-    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += gstride) {
-        const size_t c = base + threadIdx.x;
+    // round 0 over every visited cell
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < ts.span(); base += gstride) {
+        int x, y;
+        const bool in = ts.cell(base + threadIdx.x, k.W, k.H, x, y);
+        const size_t c = (size_t)y * k.W + x;
         bool keep = false;
-        if (c < N) {
+        if (in) {
             int32_t v = __ldcg(ws + c);
             if (v < 0) {
                 v = __ldcg(ws + (-(size_t)v - 1));
@@ -622,14 +629,16 @@ constexpr int kEdgeSlots = 128;  // block-local pair table (a 32x8 tile borders 
 // distinct pair and tile.
 __global__ void __launch_bounds__(FE_BX* FE_BY)
     k_flood_edges(const double* __restrict__ z, const uint8_t* __restrict__ mask, const int32_t* __restrict__ ws,
-                  unsigned long long* ekey, unsigned long long* ewt, int logmax, ModelConsts k, DevScalars* sc) {
+                  unsigned long long* ekey, unsigned long long* ewt, int logmax, ModelConsts k, DevScalars* sc,
+                  TileSet ts) {
     if (sc->sinkcount_pass1 == 0) return;
     __shared__ int32_t sw[FE_BY + 2][FE_BX + 2];
     __shared__ unsigned long long sk[FE_BY + 2][FE_BX + 2];
     __shared__ unsigned long long tkey[kEdgeSlots], twt[kEdgeSlots];
     const int W = k.W, H = k.H;
     const int logcap = edge_logcap(sc, logmax);
-    const int x0 = blockIdx.x * FE_BX, y0 = blockIdx.y * FE_BY;
+    const int tl = ts.tile(blockIdx.x);
+    const int x0 = (tl % ts.tw) * kTile, y0 = (tl / ts.tw) * kTile + blockIdx.y * FE_BY;
     const int tid = threadIdx.y * FE_BX + threadIdx.x;
     for (int t = tid; t < kEdgeSlots; t += FE_BX * FE_BY) {
         tkey[t] = ~0ull;
@@ -685,9 +694,10 @@ __global__ void __launch_bounds__(FE_BX* FE_BY)
 // (data->sinkcount, newflow.cu:1044-1045).  Labels on edges start unreached.
 __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, const unsigned long long* __restrict__ ewt,
                                 int logmax, int32_t* ea, int32_t* eb, unsigned long long* ew,
-                                unsigned long long* raise, int32_t* seen, int32_t epoch, int32_t* bid,
-                                int32_t* blab, DevScalars* sc, DemCtx dc) {
+                                unsigned long long* raise, int32_t* seen, int32_t* bid, int32_t* blab,
+                                DevScalars* sc, DemCtx dc) {
     if (sc->sinkcount_pass1 == 0) return;
+    const int32_t epoch = sc->epoch;
     const size_t cap = 1ull << edge_logcap(sc, logmax);
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)cap; base += (size_t)gridDim.x * blockDim.x) {
         const size_t i = base + threadIdx.x;
@@ -907,10 +917,13 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
 // raise_watershedMFD (newflow.cu:879-894) into the scratch DEM of pass 2.
 __global__ void k_flood_raise(const double* __restrict__ z, const uint8_t* __restrict__ mask,
                               const int32_t* __restrict__ ws, const unsigned long long* __restrict__ raise,
-                              double* __restrict__ zf, ModelConsts k, DevScalars* sc, DemCtx dc) {
+                              double* __restrict__ zf, ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts) {
     if (sc->sinkcount_pass1 == 0) return;
-    const size_t N = (size_t)k.W * k.H;
-    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+    for (size_t v0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v0 < ts.span();
+         v0 += (size_t)gridDim.x * blockDim.x) {
+        int x, y;
+        if (!ts.cell(v0, k.W, k.H, x, y)) continue;
+        const size_t c = (size_t)y * k.W + x;
         double v = z[c];
         // a DEM without sinks keeps its DEM: its second pass repeats the first
         if (mask[c] && dc.out[dem_at(dc, c)].sinkcount_pass1 != 0) {
@@ -925,9 +938,12 @@ __global__ void k_flood_raise(const double* __restrict__ z, const uint8_t* __res
 // Epilogue of cuFlowDirection (routeflow.cu:934-953) and the host outlet check
 // of routeflow.cu:738-741, which the reference applies after its device copy.
 __global__ void k_fd_epilogue(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
-                              const uint8_t* __restrict__ mfd, uint8_t* __restrict__ fd, ModelConsts k) {
-    const size_t N = (size_t)k.W * k.H;
-    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+                              const uint8_t* __restrict__ mfd, uint8_t* __restrict__ fd, ModelConsts k, TileSet ts) {
+    for (size_t v0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v0 < ts.span();
+         v0 += (size_t)gridDim.x * blockDim.x) {
+        int x, y;
+        if (!ts.cell(v0, k.W, k.H, x, y)) continue;
+        const size_t c = (size_t)y * k.W + x;
         uint8_t v = sfd[c];
         if (k.flow_type != 0 && mask[c] && mfd[c] != 0) v = mfd[c];
         fd[c] = v;
@@ -954,6 +970,7 @@ __global__ void k_fd_outlets(uint8_t* __restrict__ fd, double* z, DemCtx dc) {
 __global__ void k_fd_reset(DevScalars* sc, DemCtx dc) {
     const int d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d == 0) {
+        sc->epoch += 1;
         sc->sinkcount_pass1 = 0;
         sc->flood_sweeps = sc->label_rounds = sc->spill_rounds = 0;
         sc->plateau_sweeps = 0;
@@ -986,7 +1003,7 @@ int coop_blocks_for(const void* kernel, int threads, size_t smem) {
 
 static lem_status coop(const char* name, const void* fn, int blocks, void** args, const Launch& L) {
     L.pre(name);
-    LEM_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(256), args, 0, L.st));
+    LEM_CUDA_TRY(coop_launch(fn, blocks, args, L.st));
     L.post();
     return LEM_OK;
 }
@@ -1001,14 +1018,16 @@ static int flat_blocks(size_t n, int threads, int cap_blocks) {
 // One pass of FlowDirs + plateau routing.  Pass 1 reads the stage's DEM and
 // updates the persistent slopes; pass 2 reads the raised DEM.
 static lem_status direction_pass(const DevState& s, const ModelConsts& k, const Launch& L, int pass) {
-    const size_t N = (size_t)k.W * k.H;
     const int T = 256, big = 152 * 32;
-    const dim3 fdb(FD_BX, FD_BY), fdg((k.W + FD_BX - 1) / FD_BX, (k.H + FD_BY - 1) / FD_BY);
+    const TileSet ts = tiles_of(s, k.W);
+    const size_t span = ts.span();
+    const dim3 fdb(FD_BX, FD_BY), fdg(ts.n, kTile / FD_BY);
     const double* zz = pass == 1 ? s.z : s.zf;
     float* slopes = pass == 1 ? s.slopes : nullptr;
     if (pass == 2) LEM_LAUNCH(L, k_cand_reset, 1, 1, s.sc);
-    LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, k, s.sc, s.dems, pass);
-    LEM_LAUNCH(L, k_plateau_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, pass);
+    LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, k, s.sc, s.dems, ts, pass);
+    LEM_LAUNCH(L, k_plateau_init, flat_blocks(span, T, big), T, s.mask, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, ts,
+               pass);
     {
         // candidates in list_a; frontiers in list_b and `pending` (an int32 grid unused in this stage)
         float* sp = s.sp;
@@ -1020,23 +1039,24 @@ static lem_status direction_pass(const DevState& s, const ModelConsts& k, const 
         DevScalars* sc = s.sc;
         void* args[] = {(void*)&zz, (void*)&sp, (void*)&cand, (void*)&la, (void*)&lb, (void*)&mark, (void*)&kk,
                         (void*)&sc, (void*)&pass};
-        lem_status r = coop("k_plateau_relax", (const void*)k_plateau_relax, s.max_coop_blocks, args, L);
+        lem_status r = coop("k_plateau_relax", (const void*)k_plateau_relax, s.coop_blocks[kCkPlateau], args, L);
         if (r != LEM_OK) return r;
     }
-    LEM_LAUNCH(L, k_plateau_final, flat_blocks(N, T, big), T, zz, s.sp, s.list_a, s.sfd, s.mfd, slopes, k, s.sc,
+    LEM_LAUNCH(L, k_plateau_final, flat_blocks(span, T, big), T, zz, s.sp, s.list_a, s.sfd, s.mfd, slopes, k, s.sc,
                pass);
     return LEM_OK;
 }
 
 lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const Launch& L) {
-    const size_t N = (size_t)k.W * k.H;
     const int T = 256, big = 152 * 32;
+    const TileSet ts = tiles_of(s, k.W);
+    const size_t span = ts.span();
     lem_status r;
     LEM_LAUNCH(L, k_fd_reset, (s.dems.n + 127) / 128, 128, s.sc, s.dems);
     if ((r = direction_pass(s, k, L, 1)) != LEM_OK) return r;
     // sink flooding on the pass-1 codes
-    LEM_LAUNCH(L, k_flood_init, flat_blocks(N, T, big), T, s.mask, s.sfd, s.sfd1, s.ws, s.list_b, s.raise, s.bid, k,
-               s.sc, s.dems);
+    LEM_LAUNCH(L, k_flood_init, flat_blocks(span, T, big), T, s.mask, s.sfd, s.sfd1, s.ws, s.list_b, s.raise, s.bid,
+               k, s.sc, s.dems, ts);
     {
         const double* zz = s.z;
         int32_t* ws = s.ws;
@@ -1044,7 +1064,7 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
         void* args[] = {(void*)&zz, (void*)&ws, (void*)&sinks, (void*)&kk, (void*)&sc};
-        if ((r = coop("k_flood_merge", (const void*)k_flood_merge, s.max_coop_blocks, args, L)) != LEM_OK) return r;
+        if ((r = coop("k_flood_merge", (const void*)k_flood_merge, s.coop_blocks[kCkMerge], args, L)) != LEM_OK) return r;
     }
     {
         int32_t* ws = s.ws;
@@ -1052,20 +1072,19 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
         int32_t* lb = s.pending;
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
-        void* args[] = {(void*)&ws, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc};
-        if ((r = coop("k_flood_jump", (const void*)k_flood_jump, s.max_coop_blocks, args, L)) != LEM_OK) return r;
+        TileSet tt = ts;
+        void* args[] = {(void*)&ws, (void*)&la, (void*)&lb, (void*)&kk, (void*)&sc, (void*)&tt};
+        if ((r = coop("k_flood_jump", (const void*)k_flood_jump, s.coop_blocks[kCkJump], args, L)) != LEM_OK) return r;
     }
     int logmax = 0;
     while ((1ll << logmax) < s.ecap) ++logmax;
     LEM_LAUNCH(L, k_edge_clear, flat_blocks((size_t)s.ecap, T, big), T, s.ekey, s.ewt, logmax, s.sc);
     {
-        const dim3 eb(FE_BX, FE_BY), eg((k.W + FE_BX - 1) / FE_BX, (k.H + FE_BY - 1) / FE_BY);
-        LEM_LAUNCH(L, k_flood_edges, eg, eb, s.z, s.mask, s.ws, s.ekey, s.ewt, logmax, k, s.sc);
+        const dim3 eb(FE_BX, FE_BY), eg(ts.n, kTile / FE_BY);
+        LEM_LAUNCH(L, k_flood_edges, eg, eb, s.z, s.mask, s.ws, s.ekey, s.ewt, logmax, k, s.sc, ts);
     }
-    static int32_t epoch = 0;
-    ++epoch;
     LEM_LAUNCH(L, k_flood_compact, flat_blocks((size_t)s.ecap, T, big), T, s.ekey, s.ewt, logmax, s.edge_a, s.edge_b,
-               s.edge_w, s.raise, s.label_seen, epoch, s.bid, s.blab, s.sc, s.dems);
+               s.edge_w, s.raise, s.label_seen, s.bid, s.blab, s.sc, s.dems);
     {
         const int32_t* ea = s.edge_a;
         const int32_t* eb = s.edge_b;
@@ -1083,11 +1102,12 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
         void* args[] = {(void*)&ea,   (void*)&eb,    (void*)&ew,    (void*)&raise, (void*)&comp, (void*)&cdist,
                         (void*)&cmaxw, (void*)&bidp, (void*)&blab,  (void*)&stamp, (void*)&bdist, (void*)&euv,
                         (void*)&sc};
-        if ((r = coop("k_flood_spill", (const void*)k_flood_spill, s.max_coop_blocks, args, L)) != LEM_OK) return r;
+        if ((r = coop("k_flood_spill", (const void*)k_flood_spill, s.coop_blocks[kCkSpill], args, L)) != LEM_OK) return r;
     }
-    LEM_LAUNCH(L, k_flood_raise, flat_blocks(N, T, big), T, s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc, s.dems);
+    LEM_LAUNCH(L, k_flood_raise, flat_blocks(span, T, big), T, s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc, s.dems,
+               ts);
     if ((r = direction_pass(s, k, L, 2)) != LEM_OK) return r;
-    LEM_LAUNCH(L, k_fd_epilogue, flat_blocks(N, T, big), T, s.mask, s.sfd, s.mfd, s.fd, k);
+    LEM_LAUNCH(L, k_fd_epilogue, flat_blocks(span, T, big), T, s.mask, s.sfd, s.mfd, s.fd, k, ts);
     LEM_LAUNCH(L, k_fd_outlets, (s.dems.n + 127) / 128, 128, s.fd, s.z, s.dems);
     LEM_CUDA_TRY(cudaGetLastError());
     return LEM_OK;

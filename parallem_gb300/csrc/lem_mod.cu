@@ -194,14 +194,15 @@ __global__ void __launch_bounds__(256)
 // tiled path.
 __global__ void k_sed_prep(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                            float* __restrict__ depo, int32_t* __restrict__ pending, int32_t* ready, ModelConsts k,
-                           DevScalars* sc) {
+                           DevScalars* sc, TileSet ts) {
     const int W = k.W, H = k.H;
     const size_t N = (size_t)W * H;
-    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += (size_t)gridDim.x * blockDim.x) {
-        const size_t i = base + threadIdx.x;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < ts.span(); base += (size_t)gridDim.x * blockDim.x) {
+        int x, y;
+        const bool in = ts.cell(base + threadIdx.x, W, H, x, y);
+        const size_t i = (size_t)y * W + x;
         bool src = false;
-        if (i < N) {
-            const int x = (int)(i % W), y = (int)(i / W);
+        if (in) {
             int32_t pend = kBlocked;
             if (mask[i]) {
                 depo[i] = 0.00001f;
@@ -441,7 +442,7 @@ __global__ void __launch_bounds__(256)
                  float* fines, float* soilT, int32_t* __restrict__ t_dst, int32_t* __restrict__ t_pend,
                  int32_t* __restrict__ t_orng, float2* __restrict__ t_out, float4* __restrict__ p_abc,
                  int32_t* __restrict__ p_ref, float4* __restrict__ p_map, uint8_t* __restrict__ t_stat,
-                 int32_t* srcs, ModelConsts k, DevScalars* sc, DemCtx dc) {
+                 int32_t* srcs, ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts) {
     if (!sc->sed_tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -468,7 +469,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int16_t s_rnd[kTile * kTile];
     __shared__ int s_no, s_nt, s_done, s_pool, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
-    const int t = blockIdx.x;
+    const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
     sed_tile_load(mask, fd, W, H, tx0, ty0, s_code, s_cls);
     if (threadIdx.x < kTileEnt) {
@@ -564,7 +565,7 @@ __global__ void __launch_bounds__(256)
             }
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
         },
-        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0, k.narrow_below[kTwSedLocal]);
     for (int it = 0; it < 10; ++it) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -864,7 +865,7 @@ __global__ void __launch_bounds__(256)
     k_sedt_final(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd, const float* __restrict__ ero,
                  const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
                  float* fines, float* soilT, const int32_t* __restrict__ t_pend, const uint8_t* __restrict__ t_stat,
-                 ModelConsts k, DevScalars* sc, DemCtx dc) {
+                 ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts) {
     if (!sc->sed_tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -876,7 +877,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int16_t s_q[kTile * kTile];
     __shared__ int s_done, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
-    const int t = blockIdx.x;
+    const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
     sed_tile_load(mask, fd, W, H, tx0, ty0, s_code, s_cls);
     if (threadIdx.x < kRing) {
@@ -963,7 +964,7 @@ __global__ void __launch_bounds__(256)
             }
             return rin ? rly * kTile + rlx : -1;
         },
-        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0, k.narrow_below[kTwSedFinal]);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();
@@ -1161,12 +1162,17 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flag
     LEM_LAUNCH(L, k_mod_reset, (s.dems.n + 127) / 128, 128, s.sc, s.dems, tiled);
     LEM_LAUNCH(L, k_erosion, s.n_chunks, T, s.z, s.z_init, s.mask, s.slopes, s.fa, s.fines, s.nut, s.soilT, s.stone,
                s.totB, s.slopeptr, s.ero, s.inci, s.geli, s.chunk_start, k, s.dems);
-    LEM_LAUNCH(L, k_sed_prep, blocks, T, s.mask, s.fd, s.depo, s.pending, s.list_a, k, s.sc);
+    const TileSet ts = tiles_of(s, k.W);
+    {
+        const size_t vb = (ts.span() + T - 1) / T;
+        LEM_LAUNCH(L, k_sed_prep, (int)(vb > 152 * 32 ? 152 * 32 : vb), T, s.mask, s.fd, s.depo, s.pending, s.list_a,
+                   k, s.sc, ts);
+    }
     if (tiled) {
-        const int tiles = ((k.W + kTile - 1) / kTile) * ((k.H + kTile - 1) / kTile);
+        const int tiles = ts.n;
         LEM_LAUNCH(L, k_sedt_local, tiles, 256, s.mask, s.fd, s.ero, s.inci, s.geli, s.depo, s.stone, s.fines,
                    s.soilT, s.t_dst, s.t_pend, s.t_orng, s.t_la, s.p_abc, s.p_ref, s.p_map, s.t_stat, s.list_b, k,
-                   s.sc, s.dems);
+                   s.sc, s.dems, ts);
         const uint8_t* fd = s.fd;
         const int32_t* torng = s.t_orng;
         const int32_t* tdst = s.t_dst;
@@ -1188,11 +1194,10 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flag
                         (void*)&pmap,  (void*)&pval,  (void*)&depo,  (void*)&stone, (void*)&fines, (void*)&soilT, (void*)&tpend,
                         (void*)&la,    (void*)&lb,    (void*)&kk,    (void*)&sc};
         L.pre("k_sedt_coarse");
-        LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sedt_coarse, dim3(s.max_coop_blocks), dim3(256),
-                                                 args, 0, L.st));
+        LEM_CUDA_TRY(coop_launch((const void*)k_sedt_coarse, s.coop_blocks[kCkSedCoarse], args, L.st));
         L.post();
         LEM_LAUNCH(L, k_sedt_final, tiles, 256, s.mask, s.fd, s.ero, s.inci, s.geli, s.depo, s.stone, s.fines,
-                   s.soilT, s.t_pend, s.t_stat, k, s.sc, s.dems);
+                   s.soilT, s.t_pend, s.t_stat, k, s.sc, s.dems, ts);
     }
     {
         const uint8_t* mask = s.mask;
@@ -1216,8 +1221,7 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flag
                         (void*)&pending, (void*)&la, (void*)&lb,    (void*)&kk,      (void*)&sc, (void*)&dc,
                         (void*)&gate};
         L.pre("k_sed_walk");
-        LEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sed_walk, dim3(s.max_coop_blocks), dim3(256), args,
-                                                 0, L.st));
+        LEM_CUDA_TRY(coop_launch((const void*)k_sed_walk, s.coop_blocks[kCkSedWalk], args, L.st));
         L.post();
     }
     const bool diag = (flags & LEM_STEP_KEEP_DIAGNOSTICS) != 0;

@@ -72,6 +72,25 @@ class Totals(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("state", C.c_int32), ("steps_left", C.c_int32), ("coop_blocks", C.c_int32 * 8),
+                ("narrow_below", C.c_int32 * 4), ("default_ms", C.c_double), ("tuned_ms", C.c_double)]
+
+
+COOP_KERNELS = ("k_plateau_relax", "k_flood_merge", "k_flood_jump", "k_flood_spill", "k_fat_coarse", "k_fa_walk",
+                "k_sedt_coarse", "k_sed_walk")
+WAVE_KERNELS = ("k_fat_local", "k_fat_final", "k_sedt_local", "k_sedt_final")
+
+
+def _tuning(h) -> dict:
+    t = Tuning()
+    _check(load().lem_get_tuning(h, C.byref(t)), "lem_get_tuning")
+    return {"state": ("default", "tuning", "tuned")[t.state], "steps_left": t.steps_left,
+            "coop_blocks": dict(zip(COOP_KERNELS, list(t.coop_blocks))),
+            "narrow_below": dict(zip(WAVE_KERNELS, list(t.narrow_below))),
+            "default_ms": t.default_ms, "tuned_ms": t.tuned_ms}
+
+
 class KernelStat(C.Structure):
     _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint32), ("total_ms", C.c_double)]
 
@@ -112,6 +131,9 @@ SIGNATURES = {
     "lem_dem_set_step_flags": (C.c_int, [_H, C.c_int32, C.c_uint32]),
     "lem_dem_get_totals": (C.c_int, [_H, C.c_int32, C.POINTER(Totals)]),
     "lem_step_batch": (C.c_int, [_H, C.c_uint32]),
+    "lem_set_graphs": (C.c_int, [_H, C.c_int32]),
+    "lem_autotune": (C.c_int, [_H, C.c_int32]),
+    "lem_get_tuning": (C.c_int, [_H, C.c_void_p]),
     "lem_snapshot_bytes": (C.c_size_t, [_H, C.c_int32]),
     "lem_snapshot_save": (C.c_int, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
     "lem_snapshot_load": (C.c_int, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
@@ -266,6 +288,17 @@ class Model:
     def profiling(self, on: bool):
         _check(load().lem_set_profiling(self.h, int(bool(on))), "lem_set_profiling")
 
+    def graphs(self, on: bool):
+        """Steps launch as one captured CUDA graph (lem_set_graphs)."""
+        _check(load().lem_set_graphs(self.h, int(bool(on))), "lem_set_graphs")
+
+    def autotune(self, steps_per_candidate: int = 1):
+        """The next 4 * steps_per_candidate steps tune the launch schedule (lem_autotune)."""
+        _check(load().lem_autotune(self.h, int(steps_per_candidate)), "lem_autotune")
+
+    def tuning(self) -> dict:
+        return _tuning(self.h)
+
     def profile(self) -> dict:
         """{kernel name: (launches, total device ms)} since the previous read."""
         arr = (KernelStat * 64)()
@@ -404,6 +437,17 @@ class Batch:
 
     def profiling(self, on: bool):
         _check(load().lem_set_profiling(self.h, int(bool(on))), "lem_set_profiling")
+
+    def graphs(self, on: bool):
+        """Steps launch as one captured CUDA graph (lem_set_graphs)."""
+        _check(load().lem_set_graphs(self.h, int(bool(on))), "lem_set_graphs")
+
+    def autotune(self, steps_per_candidate: int = 1):
+        """The next 4 * steps_per_candidate steps tune the launch schedule (lem_autotune)."""
+        _check(load().lem_autotune(self.h, int(steps_per_candidate)), "lem_autotune")
+
+    def tuning(self) -> dict:
+        return _tuning(self.h)
 
     def profile(self) -> dict:
         arr = (KernelStat * 64)()

@@ -64,8 +64,9 @@ def make_request(rid: int, rng: np.random.Generator, arrival: float, side_lo: in
 
 class Server:
     def __init__(self, canvas_w: int, canvas_h: int, budget_bytes: float = 150e9, max_dems: int = 1024,
-                 params=None):
+                 params=None, graphs: bool = True):
         self.b = L.Batch(canvas_w, canvas_h, 30.0, max_dems=max_dems, params=params)
+        self.b.graphs(graphs)  # each step one graph launch, captured again when requests join or leave
         self.budget = budget_bytes
         self.canvas_bytes = canvas_w * canvas_h * BYTES_PER_CELL
         self.active = {}      # batch id -> [request, steps done]
