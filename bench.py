@@ -53,7 +53,7 @@ STAGE_BYTES = {
 # (its share of its stage).  Routing (plateaus, flooding) and the coarse waves
 # touch a data-dependent subset of cells and have no per-cell figure.
 KERNEL_BYTES = {
-    "k_flowdirs": 19,                 # FlowDirs, two launches per step: 38 / 2
+    "k_flowdirs": 23,                 # FlowDirs, two launches per step: 38 / 2, + W plateau distance (routing)
     "k_fa_prep": 20,                  # runoff
     "k_fa_walk": 11, "k_fat_final": 9, "k_fat_local": 5,  # accumulation: R code, w (+ W fa)
     "k_erosion": 72,

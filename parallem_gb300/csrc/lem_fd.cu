@@ -64,8 +64,8 @@ __device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t* l
 // sink/flat counters and lowest elevation; pass 2 writes codes only.
 __global__ void __launch_bounds__(FD_BX* FD_BY)
     k_flowdirs(const double* __restrict__ z, const uint8_t* __restrict__ mask, float* __restrict__ slopes,
-               uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, ModelConsts k, DevScalars* sc, DemCtx dc,
-               TileSet ts, int pass) {
+               uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, float* __restrict__ sp, int32_t* plateau,
+               ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts, int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
     __shared__ unsigned long long skey[FD_BY + 2][FD_BX + 2];
     __shared__ float shi[FD_BY + 2][FD_BX + 2];
@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
     const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
     int is_sink = 0, is_flat = 0;
+    bool is_cand = false, has_equal = false;
     unsigned long long low = ~0ull;
     if (x < W && y < H) {
         const size_t self = (size_t)y * W + x;
@@ -131,6 +132,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
                     }
                 }
             }
+            has_equal = flat > 0;
             if (cand) {
                 // certify the steepest direction against the exact fp64 quotients
                 const float zs_mag = fabsf(hs);
@@ -194,7 +196,16 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
         }
         sfd[self] = cs;
         mfd[self] = cm;
+        // the plateau candidates (newflow.cu:234-350): masked-in cells with no
+        // downslope direction start at distance 2e7, every other cell at 0
+        is_cand = mask[self] && cs == 0 && cm == 0;
+        sp[self] = is_cand ? kFar : 0.f;
     }
+    // Only a candidate with an equal-height neighbour can be routed: the others
+    // (single-cell pits, NaN cells) keep 2e7 and no direction, and stay off
+    // the list the relaxation and the final directions work through.
+    warp_append(is_cand && has_equal, (int32_t)((size_t)y * W + x), plateau, &sc->n_cand, (int)((size_t)W * H),
+                &sc->err);
     if (pass == 1) {
         const int s1 = warp_sum(is_sink), f1 = warp_sum(is_flat);
         low = warp_min_u64(low);
@@ -209,30 +220,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
 }
 
 // --------------------------------------------------------------------------
-// Plateau routing (newflow.cu:234-350).  Candidates are masked-in cells with no
-// downslope direction; their distance starts at 2e7, every other cell at 0.
-__global__ void k_plateau_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
-                               const uint8_t* __restrict__ mfd, float* __restrict__ sp, int32_t* cand, ModelConsts k,
-                               DevScalars* sc, TileSet ts, int pass) {
-    if (pass == 2 && sc->sinkcount_pass1 == 0) return;
-    const size_t N = (size_t)k.W * k.H;
-    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < ts.span(); base += (size_t)gridDim.x * blockDim.x) {
-        int x, y;
-        const bool in = ts.cell(base + threadIdx.x, k.W, k.H, x, y);
-        const size_t c = (size_t)y * k.W + x;
-        bool is_c = false;
-        if (in) {
-            float v = 0.f;
-            if (mask[c] && sfd[c] == 0 && mfd[c] == 0) {
-                v = kFar;
-                is_c = true;
-            }
-            sp[c] = v;
-        }
-        warp_append(is_c, (int32_t)c, cand, &sc->n_cand, (int)N, &sc->err);
-    }
-}
-
+// Plateau routing (newflow.cu:234-350); k_flowdirs lists the candidates.
 constexpr int kPT = 32;            // plateau tile edge (cells)
 constexpr int kPH = kPT + 2;       // tile with its one-cell halo
 constexpr int kTileSweeps = 2048;  // sweeps of one tile visit before it is re-queued
@@ -1025,9 +1013,7 @@ static lem_status direction_pass(const DevState& s, const ModelConsts& k, const 
     const double* zz = pass == 1 ? s.z : s.zf;
     float* slopes = pass == 1 ? s.slopes : nullptr;
     if (pass == 2) LEM_LAUNCH(L, k_cand_reset, 1, 1, s.sc);
-    LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, k, s.sc, s.dems, ts, pass);
-    LEM_LAUNCH(L, k_plateau_init, flat_blocks(span, T, big), T, s.mask, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, ts,
-               pass);
+    LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, s.dems, ts, pass);
     {
         // candidates in list_a; frontiers in list_b and `pending` (an int32 grid unused in this stage)
         float* sp = s.sp;

@@ -72,8 +72,9 @@ __global__ void __launch_bounds__(256)
               const float* __restrict__ slopes, const float2* __restrict__ fa, const float* __restrict__ fines,
               const float* __restrict__ nut, const float* __restrict__ soilT, const float* __restrict__ stone,
               const float* __restrict__ totB, float* __restrict__ slopeptr, float* __restrict__ ero,
-              float* __restrict__ inci, float* __restrict__ geli, const int32_t* __restrict__ chunk_start,
-              ModelConsts k, DemCtx dc) {
+              float* __restrict__ inci, float* __restrict__ geli, float* __restrict__ depo,
+              const uint8_t* __restrict__ fd, const int32_t* __restrict__ chunk_start, ModelConsts k, DemCtx dc,
+              DevScalars* sc) {
     __shared__ double red[8];
     __shared__ unsigned long long redk[8];
     const Chunk ch = chunk_of(chunk_start, dc.n, dc.in);
@@ -85,6 +86,7 @@ __global__ void __launch_bounds__(256)
     if (ch.first == 0 && threadIdx.x == 0) o.base_level = z[outlet] - 0.00012;  // updates.cu:151
     float se = 0.f, si = 0.f, sg = 0.f;
     unsigned long long famax = 0;
+    bool multi = false;
     for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
         int x, y;
         const size_t i = region_cell(c, ri, W, &x, &y);
@@ -95,6 +97,14 @@ __global__ void __launch_bounds__(256)
             ero[i] = inci[i] = geli[i] = 0.0f;
             slopeptr[i] = 0.0f;
             continue;
+        }
+        // sedmfdaccum set-up (mfd_accum.cu:389-396): depo = 1e-5 in the catchment.
+        // A multi-direction code among the routed cells (not row 0 / column 0,
+        // mfd_accum.cu:42) sends the step's sediment routing to the walk.
+        depo[i] = 0.00001f;
+        if (x != 0 && y != 0) {
+            const uint8_t code = fd[i];
+            multi |= (code & (code - 1)) != 0;
         }
         // aveslope (eroincidep.cu:8-37): mean of the positive entries
         const float4 a = reinterpret_cast<const float4*>(slopes)[2 * i];
@@ -179,22 +189,24 @@ __global__ void __launch_bounds__(256)
     const double ti = block_sum_d(si, red);
     const double tg = block_sum_d(sg, red);
     const unsigned long long fm = block_max_u64(famax, redk);
+    const bool any_multi = __syncthreads_or(multi) != 0;
     if (threadIdx.x == 0) {
         atomicAdd(&o.tot_e, te);
         atomicAdd(&o.tot_i, ti);
         atomicAdd(&o.tot_g, tg);
         atomicMax(&o.fa_max_key, fm);
+        if (any_multi) sc->sed_tiled_ok = 0;
     }
 }
 
-// sedmfdaccum set-up (mfd_accum.cu:389-396): depo = 1e-5 in the catchment;
-// cells in row 0 or column 0 are never processed (:42) and masked cells never
-// complete, so a donor of either kind blocks its receiver for good.  A step
-// with a multi-direction code among these cells takes the walk instead of the
-// tiled path.
+// In-degrees and sources of the global sediment wave, for the steps that take
+// it (MFD, or a multi-direction code found by k_erosion): cells in row 0 or
+// column 0 are never processed (mfd_accum.cu:42) and masked cells never
+// complete, so a donor of either kind blocks its receiver for good.
 __global__ void k_sed_prep(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                            float* __restrict__ depo, int32_t* __restrict__ pending, int32_t* ready, ModelConsts k,
                            DevScalars* sc, TileSet ts) {
+    if (sc->sed_tiled_ok) return;  // the tiled path routes this step
     const int W = k.W, H = k.H;
     const size_t N = (size_t)W * H;
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < ts.span(); base += (size_t)gridDim.x * blockDim.x) {
@@ -205,10 +217,7 @@ __global__ void k_sed_prep(const uint8_t* __restrict__ mask, const uint8_t* __re
         if (in) {
             int32_t pend = kBlocked;
             if (mask[i]) {
-                depo[i] = 0.00001f;
                 if (x != 0 && y != 0) {
-                    const uint8_t code = fd[i];
-                    if (code & (code - 1)) sc->sed_tiled_ok = 0;
                     pend = 0;
 #pragma unroll
                     for (int d = 0; d < 8; ++d) {
@@ -1161,7 +1170,7 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flag
     const int tiled = (k.flow_type == 0 && !prop) ? 1 : 0;
     LEM_LAUNCH(L, k_mod_reset, (s.dems.n + 127) / 128, 128, s.sc, s.dems, tiled);
     LEM_LAUNCH(L, k_erosion, s.n_chunks, T, s.z, s.z_init, s.mask, s.slopes, s.fa, s.fines, s.nut, s.soilT, s.stone,
-               s.totB, s.slopeptr, s.ero, s.inci, s.geli, s.chunk_start, k, s.dems);
+               s.totB, s.slopeptr, s.ero, s.inci, s.geli, s.depo, s.fd, s.chunk_start, k, s.dems, s.sc);
     const TileSet ts = tiles_of(s, k.W);
     {
         const size_t vb = (ts.span() + T - 1) / T;
