@@ -468,7 +468,7 @@ def main():
         build.build()
     barrier(dist)
     lem.select_device(local)
-    tune_steps = 0 if args.no_tune else 4  # lem_autotune: one step per candidate schedule
+    tune_steps = 0 if args.no_tune else 13  # lem_autotune(3): one unmeasured step, then 3 x 4 candidate steps
     total_steps = tune_steps + args.warmup + 3 * args.steps
     work = (EnsembleWork if args.workload == "ensemble" else GridWork)(lem, S, args, rank, total_steps)
     g = work.g
@@ -476,7 +476,7 @@ def main():
 
     # autotuning steps, then warm-up steps (untimed)
     if tune_steps:
-        g.autotune(1)
+        g.autotune(3)
         for i in range(tune_steps):
             work.step(i)
     for i in range(tune_steps, tune_steps + args.warmup):

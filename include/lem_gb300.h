@@ -251,27 +251,25 @@ lem_status lem_step_batch(lem_handle* h, uint32_t flags);
  * eagerly.  The single-stage calls (lem_flow_direction ...) are always eager. */
 lem_status lem_set_graphs(lem_handle* h, int32_t on);
 
-/* Autotuner of the launch schedule (no counterpart in the reference).  Over
- * the handle's next 4 * steps_per_candidate steps (lem_step or lem_step_batch;
- * real steps of the model, launched eagerly), candidate schedules are run and
- * every tunable kernel is timed with events; afterwards each kernel keeps its
- * fastest value.  Tuned are the blocks of the cooperative kernels (1 to 4 per
- * SM, at most the co-resident count) and, for the in-tile waves, the round
- * size below which the rest of a wave runs on one warp.  Results are the same
- * under every schedule.  LEM_ERR_STATE while profiling is on (and
- * lem_set_profiling / lem_profile_read return it while tuning). */
+/* Autotuner of the launch schedule (no counterpart in the reference).  The
+ * handle's next 1 + 4 * cycles steps (lem_step or lem_step_batch; real steps
+ * of the model, launched eagerly) run the cooperative kernels with 1, 2, 3 and
+ * 4 blocks per SM in turn (at most the co-resident count; the default is every
+ * co-resident block) and time them with events; afterwards each keeps the
+ * block count with the lowest mean time if it beats the default by more than
+ * 3 %.  Results are the same under every block count.  LEM_ERR_STATE while
+ * profiling is on (and lem_set_profiling and lem_profile_read return it while
+ * tuning). */
 #define LEM_TUNE_COOP 8   /* k_plateau_relax, k_flood_merge, k_flood_jump, k_flood_spill,
                              k_fat_coarse, k_fa_walk, k_sedt_coarse, k_sed_walk */
-#define LEM_TUNE_WAVES 4  /* k_fat_local, k_fat_final, k_sedt_local, k_sedt_final */
 typedef struct lem_tuning {
     int32_t state;                          /* 0 default schedule, 1 tuning, 2 tuned            */
     int32_t steps_left;                     /* tuning steps still to run                        */
     int32_t coop_blocks[LEM_TUNE_COOP];     /* blocks each cooperative kernel launches with    */
-    int32_t narrow_below[LEM_TUNE_WAVES];   /* in-tile waves: smaller rounds run on one warp (0: never) */
     double default_ms;                      /* ms per step of these kernels, default schedule  */
     double tuned_ms;                        /*   and with the schedule kept (as measured)       */
 } lem_tuning;
-lem_status lem_autotune(lem_handle* h, int32_t steps_per_candidate);
+lem_status lem_autotune(lem_handle* h, int32_t cycles);
 lem_status lem_get_tuning(lem_handle* h, lem_tuning* out);
 
 /* Restart snapshot of one DEM's resident state: the DEM, the DEM of the

@@ -69,25 +69,26 @@ lem_status cuda_fail(cudaError_t e, const char* what, const char* file, int line
 
 using namespace lem;
 
-// The autotuner: over its next steps a handle runs candidate schedules (the
-// cooperative kernels' blocks per SM, the in-tile waves' narrow threshold),
-// times every tunable kernel with events, and then keeps for each kernel the
-// fastest value.  Results do not depend on the schedule: every loop runs to a
-// unique fixpoint, sums are pulled in a fixed order, and an in-tile round holds
-// the same cells on one warp or on many.
+// The autotuner: over its next steps a handle runs every cooperative kernel
+// with 1, 2, 3 and 4 blocks per SM in turn (step s of the tuning runs
+// candidate s % 4, so the drift of the model state between steps falls on all
+// candidates alike; the first step, under the default schedule, is not
+// measured), times each with events, and keeps for each kernel the block count
+// with the lowest mean time when it beats the default (every co-resident
+// block) by more than the step-to-step noise.  Results do not depend on the
+// block count: every loop runs to a unique fixpoint and sums are pulled in a
+// fixed order.
 constexpr int kTuneCands = 4;
 constexpr int kTuneBlocksPerSm[kTuneCands] = {1, 2, 3, 4};
-constexpr int kTuneNarrowVals = 3;
-constexpr int kTuneNarrow[kTuneNarrowVals] = {0, 32, 64};
+constexpr double kTuneMargin = 0.97;  // a candidate replaces the default only below 97 % of its time
 const char* const kCoopNames[kCoopKernels] = {"k_plateau_relax", "k_flood_merge", "k_flood_jump", "k_flood_spill",
                                               "k_fat_coarse",    "k_fa_walk",     "k_sedt_coarse", "k_sed_walk"};
-const char* const kWaveNames[kTileWaves] = {"k_fat_local", "k_fat_final", "k_sedt_local", "k_sedt_final"};
 struct Tuner {
     int state = 0;  // 0 default schedule, 1 tuning, 2 tuned
-    int cand = 0, step_in = 0, per = 1;
-    double coop_ms[kCoopKernels][kTuneCands] = {};     // device ms, summed over the candidate's steps
-    double wave_ms[kTileWaves][kTuneNarrowVals] = {};  // device ms, summed over the steps of each value
-    int wave_n[kTuneNarrowVals] = {};                  // steps measured per narrow value
+    int step = -1;  // tuning step (-1: the unmeasured first one)
+    int steps = 0;  // measured steps in all
+    double coop_ms[kCoopKernels][kTuneCands] = {};  // device ms, summed over the steps of each candidate
+    int coop_n[kTuneCands] = {};
     double default_ms = 0, tuned_ms = 0;
 };
 
@@ -702,7 +703,6 @@ lem_status create_common(const lem_grid_desc* grid, const lem_params* params, in
     for (int i = 0; i < mod_coop_kernel_count; ++i) blocks = std::min(blocks, coop_blocks_for(mod_coop_kernels[i], 256, 0));
     s.max_coop_blocks = blocks;
     for (int i = 0; i < kCoopKernels; ++i) s.coop_blocks[i] = blocks;
-    for (int i = 0; i < kTileWaves; ++i) h->k.narrow_below[i] = 0;
     cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device);
     *out = h;
     return LEM_OK;
@@ -730,48 +730,43 @@ lem_status profile_collect(lem_handle* h, std::vector<lem_kernel_stat>& agg) {
     return LEM_OK;
 }
 
-// The schedule of the tuner's current candidate.
-void tune_apply(lem_handle* h) {
-    const Tuner& t = h->tune;
-    const int blocks = std::max(1, std::min(h->s.max_coop_blocks, kTuneBlocksPerSm[t.cand] * h->sms));
-    for (int i = 0; i < kCoopKernels; ++i) h->s.coop_blocks[i] = blocks;
-    for (int i = 0; i < kTileWaves; ++i) h->k.narrow_below[i] = kTuneNarrow[t.cand % kTuneNarrowVals];
+int coop_blocks_of(const lem_handle* h, int cand) {
+    return std::max(1, std::min(h->s.max_coop_blocks, kTuneBlocksPerSm[cand] * h->sms));
 }
 
-// Books the kernel times of a tuning step; after the last candidate, keeps the
-// fastest schedule of every kernel.
+// The schedule of the tuner's current step.
+void tune_apply(lem_handle* h) {
+    const Tuner& t = h->tune;
+    const int c = t.step < 0 ? kTuneCands - 1 : t.step % kTuneCands;
+    for (int i = 0; i < kCoopKernels; ++i) h->s.coop_blocks[i] = coop_blocks_of(h, c);
+}
+
+// Books the kernel times of a tuning step; after the last one, keeps for every
+// cooperative kernel its fastest block count (the default unless another is
+// clearly faster).
 lem_status tune_record(lem_handle* h) {
     Tuner& t = h->tune;
     std::vector<lem_kernel_stat> agg;
     lem_status r = profile_collect(h, agg);
     if (r != LEM_OK) return r;
-    for (const lem_kernel_stat& st : agg) {
-        for (int i = 0; i < kCoopKernels; ++i)
-            if (!std::strcmp(st.name, kCoopNames[i])) t.coop_ms[i][t.cand] += st.total_ms;
-        for (int i = 0; i < kTileWaves; ++i)
-            if (!std::strcmp(st.name, kWaveNames[i])) t.wave_ms[i][t.cand % kTuneNarrowVals] += st.total_ms;
+    if (t.step >= 0) {
+        const int c = t.step % kTuneCands;
+        for (const lem_kernel_stat& st : agg)
+            for (int i = 0; i < kCoopKernels; ++i)
+                if (!std::strcmp(st.name, kCoopNames[i])) t.coop_ms[i][c] += st.total_ms;
+        t.coop_n[c] += 1;
     }
-    t.wave_n[t.cand % kTuneNarrowVals] += 1;
-    if (++t.step_in < t.per) return LEM_OK;
-    t.step_in = 0;
-    if (++t.cand < kTuneCands) return LEM_OK;
-    // the default schedule is every co-resident block (the largest candidate) and no narrow rounds
+    if (++t.step < t.steps) return LEM_OK;
+    const int def = kTuneCands - 1;  // the default: every co-resident block (the largest candidate)
     t.default_ms = t.tuned_ms = 0;
     for (int i = 0; i < kCoopKernels; ++i) {
-        int best = kTuneCands - 1;
+        int best = def;
         for (int c = 0; c < kTuneCands; ++c)
-            if (t.coop_ms[i][c] < t.coop_ms[i][best]) best = c;
-        h->s.coop_blocks[i] = std::max(1, std::min(h->s.max_coop_blocks, kTuneBlocksPerSm[best] * h->sms));
-        t.default_ms += t.coop_ms[i][kTuneCands - 1] / t.per;
-        t.tuned_ms += t.coop_ms[i][best] / t.per;
-    }
-    for (int i = 0; i < kTileWaves; ++i) {
-        int best = 0;
-        for (int v = 0; v < kTuneNarrowVals; ++v)
-            if (t.wave_ms[i][v] / t.wave_n[v] < t.wave_ms[i][best] / t.wave_n[best]) best = v;
-        h->k.narrow_below[i] = kTuneNarrow[best];
-        t.default_ms += t.wave_ms[i][0] / t.wave_n[0];
-        t.tuned_ms += t.wave_ms[i][best] / t.wave_n[best];
+            if (t.coop_ms[i][c] / t.coop_n[c] < t.coop_ms[i][best] / t.coop_n[best]) best = c;
+        if (t.coop_ms[i][best] / t.coop_n[best] > kTuneMargin * t.coop_ms[i][def] / t.coop_n[def]) best = def;
+        h->s.coop_blocks[i] = coop_blocks_of(h, best);
+        t.default_ms += t.coop_ms[i][def] / t.coop_n[def];
+        t.tuned_ms += t.coop_ms[i][best] / t.coop_n[best];
     }
     t.state = 2;
     h->profiling = false;
@@ -1225,13 +1220,13 @@ lem_status lem_step_batch(lem_handle* h, uint32_t flags) {
     return r;
 }
 
-lem_status lem_autotune(lem_handle* h, int32_t steps_per_candidate) {
-    if (!h || steps_per_candidate < 1) return LEM_ERR_INVALID;
+lem_status lem_autotune(lem_handle* h, int32_t cycles) {
+    if (!h || cycles < 1 || cycles > 1000) return LEM_ERR_INVALID;
     if (h->profiling || h->tune.state == 1) return LEM_ERR_STATE;
     LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
     h->tune = Tuner{};
     h->tune.state = 1;
-    h->tune.per = steps_per_candidate;
+    h->tune.steps = kTuneCands * cycles;
     h->profiling = true;  // the tuning steps time every kernel
     h->prof.recs.clear();
     h->prof.used = 0;
@@ -1242,9 +1237,8 @@ lem_status lem_get_tuning(lem_handle* h, lem_tuning* out) {
     if (!h || !out) return LEM_ERR_INVALID;
     std::memset(out, 0, sizeof *out);
     out->state = h->tune.state;
-    out->steps_left = h->tune.state == 1 ? (kTuneCands - h->tune.cand) * h->tune.per - h->tune.step_in : 0;
+    out->steps_left = h->tune.state == 1 ? h->tune.steps - h->tune.step : 0;
     for (int i = 0; i < kCoopKernels; ++i) out->coop_blocks[i] = h->s.coop_blocks[i];
-    for (int i = 0; i < kTileWaves; ++i) out->narrow_below[i] = h->k.narrow_below[i];
     out->default_ms = h->tune.default_ms;
     out->tuned_ms = h->tune.tuned_ms;
     return LEM_OK;

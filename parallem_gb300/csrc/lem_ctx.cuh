@@ -32,12 +32,10 @@ struct ModelConsts {  // per-handle constants derived on the host in double
     float rescale_weather;  // 10000 * (10000 / cs^2)      eroincidep.cu:628
     float rescale_veg;      // 10000 / cs^2                Data.cpp:124
     float erod_const;       // 0.043*(struct-2) + 0.033*(perm-3)
-    int32_t narrow_below[4];  // in-tile waves (TileWave order): rounds with fewer queued cells run on one warp, 0: never
 };
 
-// The in-tile waves and the cooperative kernels whose schedule the autotuner
-// sets (the order of lem_tuning's arrays).
-enum TileWave { kTwFatLocal = 0, kTwFatFinal, kTwSedLocal, kTwSedFinal, kTileWaves };
+// The cooperative kernels whose block count the autotuner sets (the order of
+// lem_tuning's array).
 enum CoopKernel { kCkPlateau = 0, kCkMerge, kCkJump, kCkSpill, kCkFatCoarse, kCkFaWalk, kCkSedCoarse, kCkSedWalk,
                   kCoopKernels };
 

@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(256)
             s_done[cur] = 1;
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
         },
-        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0, k.narrow_below[kTwFatLocal]);
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
     // the end of every in-tile path: pointer jumping (paths are shorter than 2^10 cells)
     for (int it = 0; it < 10; ++it) {
 #pragma unroll
@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(256)
                 return -1;
             return rly * kTile + rlx;
         },
-        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0, k.narrow_below[kTwFatFinal]);
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();

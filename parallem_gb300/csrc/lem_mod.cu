@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(256)
             }
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
         },
-        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0, k.narrow_below[kTwSedLocal]);
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
     for (int it = 0; it < 10; ++it) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -973,7 +973,7 @@ __global__ void __launch_bounds__(256)
             }
             return rin ? rly * kTile + rlx : -1;
         },
-        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0, k.narrow_below[kTwSedFinal]);
+        s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();

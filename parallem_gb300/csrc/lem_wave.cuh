@@ -196,43 +196,26 @@ __device__ __forceinline__ int ring_halo(int i) {
 // queues that receiver when c was its last donor.  Cells are queued once, in
 // an order where every donor comes before its receiver.  Every lane works on a
 // cell while the round holds one per lane, which a walk along each chain
-// cannot do.  Rounds run on every warp of the block between block barriers;
-// once a round holds fewer than narrow_below cells (0: never), the first warp
-// alone runs the rest of the wave between warp barriers (the long tail of
-// single chains) and the other warps wait once, at the end.  The rounds, and
-// the cells in each, are the same either way.
+// cannot do.
 template <class Op>
 __device__ __forceinline__ void tile_wave(const Op& op, int32_t* s_pend, int16_t* s_q, int* s_qn, int* s_end,
-                                          const bool (&src)[4], int lx, int ly0, int narrow_below) {
+                                          const bool (&src)[4], int lx, int ly0) {
 #pragma unroll
     for (int q = 0; q < 4; ++q)
         if (src[q]) s_q[atomicAdd(s_qn, 1)] = (int16_t)((ly0 + 8 * q) * kTile + lx);
-    int start = 0, round = 0;
-    for (; round <= kTile * kTile; ++round) {
+    int start = 0;
+    for (int round = 0; round <= kTile * kTile; ++round) {
         __syncthreads();
         if (threadIdx.x == 0) *s_end = *s_qn;
         __syncthreads();
         const int end = *s_end;
-        if (end == start || end - start < narrow_below) break;  // done, or a small round: the first warp goes on
+        if (start == end) break;
         for (int i = start + threadIdx.x; i < end; i += blockDim.x) {
             const int c = s_q[i];
             const int r = op(c, round);
             if (r >= 0 && atomicSub(&s_pend[r], 1) == 1) s_q[atomicAdd(s_qn, 1)] = (int16_t)r;
         }
         start = end;
-    }
-    if (threadIdx.x < 32) {
-        for (; round <= kTile * kTile; ++round) {
-            __syncwarp();
-            const int end = *((volatile int*)s_qn);
-            if (start == end) break;
-            for (int i = start + threadIdx.x; i < end; i += 32) {
-                const int c = s_q[i];
-                const int r = op(c, round);
-                if (r >= 0 && atomicSub(&s_pend[r], 1) == 1) s_q[atomicAdd(s_qn, 1)] = (int16_t)r;
-            }
-            start = end;
-        }
     }
     __syncthreads();
 }

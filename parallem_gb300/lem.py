@@ -74,12 +74,11 @@ class Totals(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("state", C.c_int32), ("steps_left", C.c_int32), ("coop_blocks", C.c_int32 * 8),
-                ("narrow_below", C.c_int32 * 4), ("default_ms", C.c_double), ("tuned_ms", C.c_double)]
+                ("default_ms", C.c_double), ("tuned_ms", C.c_double)]
 
 
 COOP_KERNELS = ("k_plateau_relax", "k_flood_merge", "k_flood_jump", "k_flood_spill", "k_fat_coarse", "k_fa_walk",
                 "k_sedt_coarse", "k_sed_walk")
-WAVE_KERNELS = ("k_fat_local", "k_fat_final", "k_sedt_local", "k_sedt_final")
 
 
 def _tuning(h) -> dict:
@@ -87,7 +86,6 @@ def _tuning(h) -> dict:
     _check(load().lem_get_tuning(h, C.byref(t)), "lem_get_tuning")
     return {"state": ("default", "tuning", "tuned")[t.state], "steps_left": t.steps_left,
             "coop_blocks": dict(zip(COOP_KERNELS, list(t.coop_blocks))),
-            "narrow_below": dict(zip(WAVE_KERNELS, list(t.narrow_below))),
             "default_ms": t.default_ms, "tuned_ms": t.tuned_ms}
 
 
@@ -292,9 +290,9 @@ class Model:
         """Steps launch as one captured CUDA graph (lem_set_graphs)."""
         _check(load().lem_set_graphs(self.h, int(bool(on))), "lem_set_graphs")
 
-    def autotune(self, steps_per_candidate: int = 1):
-        """The next 4 * steps_per_candidate steps tune the launch schedule (lem_autotune)."""
-        _check(load().lem_autotune(self.h, int(steps_per_candidate)), "lem_autotune")
+    def autotune(self, cycles: int = 1):
+        """The next 1 + 4 * cycles steps tune the launch schedule (lem_autotune)."""
+        _check(load().lem_autotune(self.h, int(cycles)), "lem_autotune")
 
     def tuning(self) -> dict:
         return _tuning(self.h)
@@ -442,9 +440,9 @@ class Batch:
         """Steps launch as one captured CUDA graph (lem_set_graphs)."""
         _check(load().lem_set_graphs(self.h, int(bool(on))), "lem_set_graphs")
 
-    def autotune(self, steps_per_candidate: int = 1):
-        """The next 4 * steps_per_candidate steps tune the launch schedule (lem_autotune)."""
-        _check(load().lem_autotune(self.h, int(steps_per_candidate)), "lem_autotune")
+    def autotune(self, cycles: int = 1):
+        """The next 1 + 4 * cycles steps tune the launch schedule (lem_autotune)."""
+        _check(load().lem_autotune(self.h, int(cycles)), "lem_autotune")
 
     def tuning(self) -> dict:
         return _tuning(self.h)

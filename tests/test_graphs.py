@@ -84,19 +84,19 @@ def test_batch_graph_equals_eager_across_joins(lem):
 
 def test_autotuned_schedule_gives_the_same_grids(lem):
     """Steps under every candidate schedule of the autotuner (cooperative blocks
-    per SM, one-warp tails of the in-tile waves) give the grids of the default
-    schedule, and the schedule kept afterwards is one of the candidates."""
+    per SM) give the grids of the default schedule, and the schedule kept
+    afterwards is one of the candidates."""
     def run(tune):
-        dem = S.make_dem(256, 0.75, 800.0, 0.04, 60, 6, 91)
+        dem = S.make_dem(160, 0.75, 800.0, 0.04, 30, 3, 91)
         st = S.initial_state(dem, 30.0, 900.0, 9.0)
         rng = np.random.default_rng(92)
         m = lem.Model(dem, 30.0, 900.0, 9.0)
         m.set_state(st)
         m.graphs(True)
         if tune:
-            m.autotune(1)
+            m.autotune(3)
             assert m.tuning()["state"] == "tuning"
-        for j in range(6):
+        for j in range(14):
             m.step(float(rng.lognormal(np.log(900), 0.3)), float(rng.normal(9, 2)), True, 0x1 if j == 0 else 0)
         m.synchronize()
         out = {f: m.get(f) for f in GRIDS}
@@ -109,6 +109,5 @@ def test_autotuned_schedule_gives_the_same_grids(lem):
     tuned, t1 = run(True)
     check_same(tuned, plain, "autotuned")
     assert t0["state"] == "default" and t1["state"] == "tuned" and t1["steps_left"] == 0
-    assert all(v in (0, 32, 64) for v in t1["narrow_below"].values())
     assert all(b > 0 for b in t1["coop_blocks"].values())
     assert t1["tuned_ms"] <= t1["default_ms"] + 1e-9
