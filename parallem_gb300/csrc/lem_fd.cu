@@ -57,6 +57,20 @@ __device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t* l
     }
 }
 
+// entry d (N, NE, ... NW) of a cell's 8 slopes held as two float4
+__device__ __forceinline__ void set_slope(float4& a, float4& b, int d, float v) {
+    switch (d) {
+        case 0: a.x = v; break;
+        case 1: a.y = v; break;
+        case 2: a.z = v; break;
+        case 3: a.w = v; break;
+        case 4: b.x = v; break;
+        case 5: b.y = v; break;
+        case 6: b.z = v; break;
+        default: b.w = v; break;
+    }
+}
+
 // --------------------------------------------------------------------------
 // FlowDirs (newflow.cu:49-174) on a 32x8 tile with a one-cell halo in shared
 // memory.  Pass 1 writes the downslope slopes into the persistent 8-per-cell
@@ -74,6 +88,18 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     const int t = ts.tile(blockIdx.x);
     const int x0 = (t % ts.tw) * kTile, y0 = (t / ts.tw) * kTile + blockIdx.y * FD_BY;
     const int tid = threadIdx.y * FD_BX + threadIdx.x;
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
+    const bool inb = x < W && y < H;
+    const size_t self = (size_t)y * W + x;
+    const uint8_t mk = inb ? mask[self] : 0;
+    // the cell's persistent slopes, read before the halo so that the two loads overlap
+    float4* const sp4 = (slopes && mk) ? reinterpret_cast<float4*>(slopes + 8 * self) : nullptr;
+    float4 sa = make_float4(0.f, 0.f, 0.f, 0.f), sb = sa;
+    if (sp4) {
+        sa = sp4[0];
+        sb = sp4[1];
+    }
     for (int t = tid; t < (FD_BX + 2) * (FD_BY + 2); t += FD_BX * FD_BY) {
         int ly = t / (FD_BX + 2), lx = t % (FD_BX + 2);
         int gx = x0 + lx - 1, gy = y0 + ly - 1;
@@ -90,40 +116,36 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     }
     __syncthreads();
 
-    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
-    const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
     int is_sink = 0, is_flat = 0;
     bool is_cand = false, has_equal = false;
     unsigned long long low = ~0ull;
-    if (x < W && y < H) {
-        const size_t self = (size_t)y * W + x;
+    if (inb) {
         uint8_t cs = kMaskedCode, cm = kMaskedCode;
-        if (mask[self]) {
+        if (mk) {
             cs = cm = 0;  // a NaN elevation compares false with every neighbour: no direction
         }
-        if (mask[self] && skey[ly][lx] != 0) {
+        if (mk && skey[ly][lx] != 0) {
             const unsigned long long ks = skey[ly][lx];
             const unsigned long long knd = key_nodata();
             const float hs = shi[ly][lx], ls = slo[ly][lx];
+            // the fp32 estimate of the slope towards d (from the head/tail split of z)
+            auto est = [&](int d) {
+                return ((hs - shi[ly + dir_dy(d)][lx + dir_dx(d)]) + (ls - slo[ly + dir_dy(d)][lx + dir_dx(d)])) *
+                       k.inv_len[d];
+            };
             low = ks;
             int up = 0, flat = 0;
             uint32_t aspect = 0, cand = 0;
-            float sv[8];
-            unsigned long long kn8[8];
             int bestd = -1;
             float best = -1.0f;
 #pragma unroll
             for (int d = 0; d < 8; ++d) {
-                sv[d] = 0.f;
                 const unsigned long long kn = skey[ly + dir_dy(d)][lx + dir_dx(d)];
-                kn8[d] = kn;
                 if (kn == 0) continue;
                 if (ks < kn) up += 1;
                 if (ks == kn) flat += 1;
                 if (ks > kn && kn != knd) {
-                    const float dd = (hs - shi[ly + dir_dy(d)][lx + dir_dx(d)]) + (ls - slo[ly + dir_dy(d)][lx + dir_dx(d)]);
-                    const float s = dd * k.inv_len[d];
-                    sv[d] = s;
+                    const float s = est(d);
                     cand |= 1u << d;
                     aspect |= dir_bit(d);
                     if (s > best) {
@@ -137,19 +159,23 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
                 // certify the steepest direction against the exact fp64 quotients
                 const float zs_mag = fabsf(hs);
                 bool certain = true;
-                const float err_b = best * 1.0e-6f + fmaxf(zs_mag, 1.0f) * 1.0e-12f * k.inv_len[bestd];
+                const float inv_b = (bestd & 1) ? k.inv_len[1] : k.inv_len[0];  // the length depends on d's parity
+                const float err_b = best * 1.0e-6f + fmaxf(zs_mag, 1.0f) * 1.0e-12f * inv_b;
+                const unsigned long long kb = skey[ly + dir_dy(bestd)][lx + dir_dx(bestd)];
 #pragma unroll
                 for (int d = 0; d < 8; ++d) {
                     if (!((cand >> d) & 1u)) continue;
+                    const float sd = est(d);
                     const float abs_d = fmaxf(zs_mag, 1.0f) * 1.0e-12f * k.inv_len[d];
                     // a drop close to the split error of z: the estimate is not
                     // within 1e-7 of the reference's slope (and may even round to 0,
                     // while the reference stores a positive slope that aveslope counts)
-                    if (sv[d] < 1.0e5f * abs_d) certain = false;
+                    if (sd < 1.0e5f * abs_d) certain = false;
                     if (d == bestd) continue;
-                    const float err_d = sv[d] * 1.0e-6f + abs_d;
-                    if (sv[d] + err_d < best - err_b) continue;
-                    if (((d ^ bestd) & 1) == 0 && kn8[d] == kn8[bestd] && d > bestd) continue;  // exact tie
+                    const float err_d = sd * 1.0e-6f + abs_d;
+                    if (sd + err_d < best - err_b) continue;
+                    if (((d ^ bestd) & 1) == 0 && skey[ly + dir_dy(d)][lx + dir_dx(d)] == kb && d > bestd)
+                        continue;  // exact tie
                     certain = false;
                 }
                 if (!certain) {
@@ -157,29 +183,24 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
                     const double zs = dkey_inv(ks);
                     double smax = 0.0;
                     bestd = -1;
+#pragma unroll
                     for (int d = 0; d < 8; ++d) {
                         if (!((cand >> d) & 1u)) continue;
-                        const double st = (zs - dkey_inv(kn8[d])) / k.len[d];
-                        sv[d] = (float)st;
+                        const double st = (zs - dkey_inv(skey[ly + dir_dy(d)][lx + dir_dx(d)])) / k.len[d];
+                        set_slope(sa, sb, d, (float)st);
                         if (st > smax) {
                             smax = st;
                             bestd = d;
                         }
                     }
+                } else {
+#pragma unroll
+                    for (int d = 0; d < 8; ++d)
+                        if ((cand >> d) & 1u) set_slope(sa, sb, d, est(d));
                 }
-                if (slopes) {
-                    float4* p = reinterpret_cast<float4*>(slopes + 8 * self);
-                    float4 a = p[0], b = p[1];
-                    if (cand & 0x01u) a.x = sv[0];
-                    if (cand & 0x02u) a.y = sv[1];
-                    if (cand & 0x04u) a.z = sv[2];
-                    if (cand & 0x08u) a.w = sv[3];
-                    if (cand & 0x10u) b.x = sv[4];
-                    if (cand & 0x20u) b.y = sv[5];
-                    if (cand & 0x40u) b.z = sv[6];
-                    if (cand & 0x80u) b.w = sv[7];
-                    p[0] = a;
-                    p[1] = b;
+                if (sp4) {
+                    sp4[0] = sa;
+                    sp4[1] = sb;
                 }
             }
             uint32_t asfd = bestd >= 0 ? dir_bit(bestd) : 0u;
@@ -198,7 +219,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
         mfd[self] = cm;
         // the plateau candidates (newflow.cu:234-350): masked-in cells with no
         // downslope direction start at distance 2e7, every other cell at 0
-        is_cand = mask[self] && cs == 0 && cm == 0;
+        is_cand = mk && cs == 0 && cm == 0;
         sp[self] = is_cand ? kFar : 0.f;
     }
     // Only a candidate with an equal-height neighbour can be routed: the others
@@ -209,7 +230,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     if (pass == 1) {
         const int s1 = warp_sum(is_sink), f1 = warp_sum(is_flat);
         low = warp_min_u64(low);
-        const int d = warp_dem(dc, (size_t)y * W + x, x < W && y < H && mask[(size_t)y * W + x]);
+        const int d = warp_dem(dc, self, mk != 0);
         if ((threadIdx.x & 31) == 0 && d >= 0) {
             DemOut& o = dc.out[d];
             if (s1) atomicAdd(&o.sink_counter, s1);

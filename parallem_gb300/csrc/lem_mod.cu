@@ -870,7 +870,9 @@ __global__ void __launch_bounds__(256)
     wave_walk_warp(op, t_pend, list_a, list_b, k.W, k.H, sc);
 }
 
-__global__ void __launch_bounds__(256)
+constexpr uint8_t kStatNz = 4;  // k_sedt_final: flag in a waiting cell's status
+
+__global__ void __launch_bounds__(256, 6)
     k_sedt_final(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd, const float* __restrict__ ero,
                  const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
                  float* fines, float* soilT, const int32_t* __restrict__ t_pend, const uint8_t* __restrict__ t_stat,
@@ -882,7 +884,11 @@ __global__ void __launch_bounds__(256)
     __shared__ float s_hval[kTH * kTH];
     __shared__ int32_t s_pend[kTile * kTile];
     __shared__ float s_new[kTile * kTile];
-    __shared__ uint8_t s_stat[kTile * kTile];
+    __shared__ uint8_t s_stat[kTile * kTile];  // 1 settled, 2 waiting; kStatNz: the sediment column is not empty
+    __shared__ float s_A[kTile * kTile];       // a waiting cell's deposition and stone-mix coefficients,
+    __shared__ float s_B[kTile * kTile];       //   computed before the wave so that its rounds read no
+    __shared__ float s_dep[kTile * kTile];     //   global memory
+    __shared__ float s_stn[kTile * kTile];
     __shared__ int16_t s_q[kTile * kTile];
     __shared__ int s_done, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
@@ -940,6 +946,14 @@ __global__ void __launch_bounds__(256)
             st = t_stat[g];
             v = __ldcg(stone + g);
             atomicMax(&s_dem, dem_at(dc, g));  // one DEM per tile
+            if (st == 2 && !outlet[q]) {
+                const SedInit in = sed_init(s_code, s_cls, lx, ly, tx0, ty0, W, ero, inci, geli, soilT, stone, k);
+                s_A[l] = in.L.A;
+                s_B[l] = in.L.B;
+                s_dep[l] = in.L.dep;
+                s_stn[l] = in.L.stn;
+                if (in.L.nz) st |= kStatNz;
+            }
         }
         s_pend[l] = pend;
         s_stat[l] = st;
@@ -955,7 +969,8 @@ __global__ void __launch_bounds__(256)
             const int rlx = cx + (d >= 0 ? dir_dx(d) : 0), rly = cy + (d >= 0 ? dir_dy(d) : 0);
             const bool rin = d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn;
             if (rin && !in_tile(rlx, rly)) return -1;  // an outlet: the coarse wave stored it
-            if (s_stat[cur] == 2) {
+            const uint8_t stc = s_stat[cur];
+            if ((stc & 3) == 2) {
                 float from = 0.f;
 #pragma unroll
                 for (int kk = 0; kk < 8; ++kk) {
@@ -965,10 +980,15 @@ __global__ void __launch_bounds__(256)
                     if (!donates(s_code[nh], dd) || s_cls[nh] != kCellIn) continue;
                     from = __fadd_rn(from, __fmul_rn(1.0f, in_tile(nlx, nly) ? s_new[nly * kTile + nlx] : s_hval[nh]));
                 }
-                const SedInit in = sed_init(s_code, s_cls, cx, cy, tx0, ty0, W, ero, inci, geli, soilT, stone, k);
-                const float sn = in.L.nz ? sed_mix(in.L.A, in.L.B, from) : s_new[cur];
+                SedLocal L;
+                L.A = s_A[cur];
+                L.B = s_B[cur];
+                L.dep = s_dep[cur];
+                L.stn = s_stn[cur];
+                L.nz = (stc & kStatNz) != 0;
+                const float sn = L.nz ? sed_mix(L.A, L.B, from) : s_new[cur];
                 s_new[cur] = sn;
-                sed_store((size_t)(ty0 + cy) * W + tx0 + cx, in.L, sn, depo, stone, fines, soilT);
+                sed_store((size_t)(ty0 + cy) * W + tx0 + cx, L, sn, depo, stone, fines, soilT);
                 ++done;
             }
             return rin ? rly * kTile + rlx : -1;
