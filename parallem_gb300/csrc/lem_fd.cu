@@ -291,7 +291,8 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
         warp_append(fresh, t, list_a, &cnt[0], ncap, &sc->err);
     }
     grid.sync();
-    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;  // rows ly0 + 8q of the tile
+    // a thread owns 4 consecutive rows of one column: 4 * wy + q
+    const int lx = threadIdx.x & 31, wy = threadIdx.x >> 5;
     int round = 0;
     for (;; ++round) {
         const int32_t* in = (round & 1) ? list_b : list_a;
@@ -307,44 +308,78 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
         for (int ti = blockIdx.x; ti < nin; ti += gridDim.x) {
             const int32_t t = __ldcg(in + ti);
             const int tx0 = (t % TW) * kPT, ty0 = (t / TW) * kPT;
-            for (int j = threadIdx.x; j < kPH * kPH; j += blockDim.x) {
+            // the halo in one batch of independent loads per thread
+            constexpr int kLoads = (kPH * kPH + 255) / 256;
+            unsigned long long kk[kLoads];
+            float vv[kLoads];
+#pragma unroll
+            for (int i = 0; i < kLoads; ++i) {
+                const int j = threadIdx.x + 256 * i;
                 const int gx = tx0 - 1 + j % kPH, gy = ty0 - 1 + j / kPH;
-                unsigned long long kk = 0;  // outside the grid: equal to no cell
-                float v = 0.f;
-                if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+                kk[i] = 0;  // outside the grid: equal to no cell
+                vv[i] = 0.f;
+                if (j < kPH * kPH && gx >= 0 && gx < W && gy >= 0 && gy < H) {
                     const size_t g = (size_t)gy * W + gx;
-                    kk = dkey(z[g]);
-                    v = __ldcg(sp + g);
+                    kk[i] = dkey(z[g]);
+                    vv[i] = __ldcg(sp + g);
                 }
-                s_key[j] = kk;
-                s_v[j] = v;
+            }
+#pragma unroll
+            for (int i = 0; i < kLoads; ++i) {
+                const int j = threadIdx.x + 256 * i;
+                if (j < kPH * kPH) {
+                    s_key[j] = kk[i];
+                    s_v[j] = vv[i];
+                }
             }
             if (threadIdx.x < 9) s_act[threadIdx.x] = 0;
             __syncthreads();
+            // per cell: its start value and the directions of its equal-height
+            // neighbours (none for a cell that is not a candidate or is NaN)
             float v0[4];
+            uint32_t eq[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) v0[q] = s_v[(ly0 + 8 * q + 1) * kPH + lx + 1];
+            for (int q = 0; q < 4; ++q) {
+                const int sidx = (4 * wy + q + 1) * kPH + lx + 1;
+                v0[q] = s_v[sidx];
+                const unsigned long long kc = s_key[sidx];
+                uint32_t m = 0;
+                if (v0[q] > 0.f && kc != 0) {  // a NaN cell (key 0) equals no neighbour
+#pragma unroll
+                    for (int d = 0; d < 8; ++d)
+                        if (s_key[sidx + dir_dy(d) * kPH + dir_dx(d)] == kc) m |= 1u << d;
+                }
+                eq[q] = m;
+            }
+            const bool any_eq = (eq[0] | eq[1] | eq[2] | eq[3]) != 0;
+            // Gauss-Seidel sweeps, down and up the thread's rows in turn
+            auto relax = [&](int q) {
+                if (!eq[q]) return false;
+                const int sidx = (4 * wy + q + 1) * kPH + lx + 1;
+                const float cv = s_v[sidx];
+                float best = cv;
+#pragma unroll
+                for (int d = 0; d < 8; ++d) {
+                    if (!((eq[q] >> d) & 1u)) continue;
+                    const float nv = s_v[sidx + dir_dy(d) * kPH + dir_dx(d)] + ((d & 1) ? 1.41f : 1.0f);
+                    if (nv < best) best = nv;
+                }
+                if (best < cv) {
+                    s_v[sidx] = best;
+                    return true;
+                }
+                return false;
+            };
             int sweep = 0;
             for (; sweep < kTileSweeps; ++sweep) {
                 bool ch = false;
+                if (any_eq) {
+                    if (sweep & 1) {
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int sidx = (ly0 + 8 * q + 1) * kPH + lx + 1;
-                    const float cv = s_v[sidx];
-                    const unsigned long long kc = s_key[sidx];
-                    if (cv > 0.f && kc != 0) {  // a NaN cell (key 0) equals no neighbour
-                        float best = cv;
+                        for (int q = 3; q >= 0; --q) ch |= relax(q);
+                    } else {
 #pragma unroll
-                        for (int d = 0; d < 8; ++d) {
-                            const int sn = sidx + dir_dy(d) * kPH + dir_dx(d);
-                            if (s_key[sn] != kc) continue;
-                            const float nv = s_v[sn] + ((d & 1) ? 1.41f : 1.0f);
-                            if (nv < best) best = nv;
-                        }
-                        if (best < cv) {
-                            s_v[sidx] = best;
-                            ch = true;
-                        }
+                        for (int q = 0; q < 4; ++q) ch |= relax(q);
                     }
                 }
                 if (!__syncthreads_or(ch)) break;
@@ -352,7 +387,7 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
             if (sweep == kTileSweeps && threadIdx.x == 0) s_act[4] = 1;  // not settled: visit again
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const int ly = ly0 + 8 * q;
+                const int ly = 4 * wy + q;
                 const int gx = tx0 + lx, gy = ty0 + ly;
                 const float v = s_v[(ly + 1) * kPH + lx + 1];
                 if (gx < W && gy < H && v < v0[q]) {
