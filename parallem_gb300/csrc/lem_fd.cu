@@ -620,13 +620,14 @@ __device__ __forceinline__ uint64_t edge_hash(unsigned long long key, int logcap
     return (key * 0x9E3779B97F4A7C15ull) >> (64 - logcap);
 }
 
-// Live capacity of the basin-pair table: 32 slots per label that can own a
-// basin (the sink cells, plus basin 0), at least 1024, at most the allocated
-// capacity.  Basins of 8-connected regions border a few others each, so the
-// table stays sparse for linear probing, and the table of a grid with few
-// sinks is small enough to stay in L2.
+// Live capacity of the basin-pair table: 8 slots per label that can own a
+// basin (the sink cells, plus basin 0), rounded up to a power of two, at
+// least 1024, at most the allocated capacity.  A basin borders about three
+// others on average (the basin graph is nearly planar), so the table is at
+// most about half full and linear probing stays short, and the table of a
+// grid with few sinks is small enough to stay in L2.
 __device__ __forceinline__ int edge_logcap(const DevScalars* sc, int logmax) {
-    const long long want = 32ll * ((long long)sc->n_sinks + 1);
+    const long long want = 8ll * ((long long)sc->n_sinks + 1);
     int l = 10;
     while (l < logmax && (1ll << l) < want) ++l;
     return l;
