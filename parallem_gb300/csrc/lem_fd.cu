@@ -459,46 +459,88 @@ __global__ void k_plateau_final(const double* __restrict__ z, const float* __res
 // Sink flooding (floodingDriver, routeflow.cu:202-676).
 // init_watershedMFD (newflow.cu:352-420): sink cells get a unique id (cell+1),
 // other cells point at their SFD receiver, masked and edge cells are basin 0.
-__global__ void k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd,
-                             uint8_t* __restrict__ sfd1, int32_t* ws, int32_t* sinks, unsigned long long* raise,
-                             int32_t* bid, ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts) {
+// The in-tile part of the labelling is done here as well: every cell of a
+// 32x32 tile follows its path inside the tile (pointer jumping in shared
+// memory) and keeps a pointer to where the path ends or leaves the tile.  A
+// path ending at a sink points at the sink, whose id the equal-height merge
+// may still change; one ending at basin 0 takes 0.  The global pointer
+// jumping then crosses tiles only.
+__global__ void __launch_bounds__(256)
+    k_flood_init(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ sfd, uint8_t* __restrict__ sfd1,
+                 int32_t* ws, int32_t* sinks, unsigned long long* raise, int32_t* bid, ModelConsts k,
+                 DevScalars* sc, DemCtx dc, TileSet ts) {
+    __shared__ int16_t s_nxt[kTile * kTile];  // next in-tile cell of the path; the cell itself at the path's end
+    __shared__ int32_t s_end[kTile * kTile];  // at a path's end: what the cells draining to it take
     const int W = k.W, H = k.H;
     const size_t N = (size_t)W * H;
+    const int t = ts.tile(blockIdx.x);
+    const int tx0 = (t % ts.tw) * kTile, ty0 = (t / ts.tw) * kTile;
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     int nsink = 0;
-    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < ts.span(); base += (size_t)gridDim.x * blockDim.x) {
-        int x, y;
-        const bool in = ts.cell(base + threadIdx.x, W, H, x, y);
+    int32_t own[4];
+    bool term[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx;
+        const int x = tx0 + lx, y = ty0 + ly;
+        const bool in = x < W && y < H;
         const size_t c = (size_t)y * W + x;
-        bool sink = false;
+        int16_t nxt = (int16_t)l;
+        int32_t endv = 0, ownv = 0;
+        bool sink = false, tm = true;
         if (in) {
-            int32_t v = 0;
-            sfd1[c] = sfd[c];
+            const uint8_t s = sfd[c];
+            sfd1[c] = s;
             if (mask[c]) {
-                const uint8_t s = sfd[c];
                 sink = (s == 0);
-                if (x == W - 1 || y == 0 || y == H - 1) {
-                    v = 0;
-                } else if (s == 0) {
-                    v = (int32_t)c + 1;
-                    raise[c + 1] = dkey(0.0);
-                } else {
+                const bool edge = x == W - 1 || y == 0 || y == H - 1;
+                if (sink) {
+                    endv = -(int32_t)c - 1;  // the cells above point at the sink
+                    if (!edge) {
+                        ownv = (int32_t)c + 1;
+                        raise[c + 1] = dkey(0.0);
+                    }
+                } else if (!edge) {
                     const int d = bit_dir(s);
                     const int nx = x + dir_dx(d < 0 ? 0 : d), ny = y + dir_dy(d < 0 ? 0 : d);
-                    if (d >= 0 && nx >= 0 && nx < W && ny >= 0 && ny < H)
-                        v = -(int32_t)((size_t)ny * W + nx) - 1;
-                    else
-                        v = 0;
+                    if (d >= 0 && nx >= 0 && nx < W && ny >= 0 && ny < H) {
+                        const int rlx = nx - tx0, rly = ny - ty0;
+                        if (rlx >= 0 && rlx < kTile && rly >= 0 && rly < kTile) {
+                            nxt = (int16_t)(rly * kTile + rlx);
+                            tm = false;
+                        } else {
+                            endv = ownv = -(int32_t)((size_t)ny * W + nx) - 1;
+                        }
+                    }
                 }
             }
-            ws[c] = v;
         }
+        s_nxt[l] = nxt;
+        s_end[l] = endv;
+        own[q] = ownv;
+        term[q] = tm;
         const int ws_ = warp_sum(sink ? 1 : 0);
         const int d = warp_dem(dc, c, sink);
-        if ((threadIdx.x & 31) == 0 && ws_) {
+        if (lx == 0 && ws_) {
             nsink += ws_;
             atomicAdd(&dc.out[d].sinkcount_pass1, ws_);
         }
         warp_append(sink, (int32_t)c, sinks, &sc->n_sinks, (int)N, &sc->err);
+    }
+    __syncthreads();
+    for (int it = 0; it < 10; ++it) {  // in-tile paths are shorter than 2^10 cells
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int l = (ly0 + 8 * q) * kTile + lx;
+            s_nxt[l] = s_nxt[s_nxt[l]];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx;
+        const int x = tx0 + lx, y = ty0 + ly;
+        if (x < W && y < H) ws[(size_t)y * W + x] = term[q] ? own[q] : s_end[s_nxt[l]];
     }
     if (nsink) atomicAdd(&sc->sinkcount_pass1, nsink);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1098,8 +1140,8 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
     LEM_LAUNCH(L, k_fd_reset, (s.dems.n + 127) / 128, 128, s.sc, s.dems);
     if ((r = direction_pass(s, k, L, 1)) != LEM_OK) return r;
     // sink flooding on the pass-1 codes
-    LEM_LAUNCH(L, k_flood_init, flat_blocks(span, T, big), T, s.mask, s.sfd, s.sfd1, s.ws, s.list_b, s.raise, s.bid,
-               k, s.sc, s.dems, ts);
+    LEM_LAUNCH(L, k_flood_init, ts.n, 256, s.mask, s.sfd, s.sfd1, s.ws, s.list_b, s.raise, s.bid, k, s.sc, s.dems,
+               ts);
     {
         const double* zz = s.z;
         int32_t* ws = s.ws;
