@@ -157,7 +157,8 @@ __device__ __forceinline__ Chunk chunk_of(const int32_t* chunk_start, int n, con
 }
 // grid index of region-linear cell i of DEM region r
 __device__ __forceinline__ size_t region_cell(const DemIn& r, int64_t i, int W, int* x, int* y) {
-    const int ry = (int)(i / r.w), rx = (int)(i - (int64_t)ry * r.w);
+    const uint32_t u = (uint32_t)i, rw = (uint32_t)r.w;  // a region holds fewer than 2^31 cells: 32-bit division
+    const int ry = (int)(u / rw), rx = (int)(u - (uint32_t)ry * rw);
     *x = r.x0 + rx;
     *y = r.y0 + ry;
     return (size_t)(*y) * W + *x;

@@ -25,18 +25,53 @@ namespace {
 // calcrunoffweight (runoffweight.cu:21-58) plus the in-degrees of the wave.
 // A donor outside the catchment is complete from the start when its DEM is
 // nodata (correctmfdflow's okgrid, mfd_simple.cu:279-285) and never otherwise.
-__global__ void k_fa_prep(const double* __restrict__ z, const uint8_t* __restrict__ mask,
-                          const uint8_t* __restrict__ fd, const float* __restrict__ stone,
-                          const float* __restrict__ totB, float* __restrict__ soilM, float* __restrict__ w,
-                          float2* __restrict__ fa, int32_t* __restrict__ pending, int32_t* __restrict__ contrib,
-                          int32_t* ready, const int32_t* __restrict__ chunk_start, ModelConsts k, DemCtx dc,
-                          DevScalars* sc) {
-    const int W = k.W, H = k.H;
-    const size_t N = (size_t)W * H;
+__global__ void k_fa_prep(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
+                          const float* __restrict__ stone, const float* __restrict__ totB, float* __restrict__ soilM,
+                          float* __restrict__ w, float2* __restrict__ fa, const int32_t* __restrict__ chunk_start,
+                          ModelConsts k, DemCtx dc, DevScalars* sc) {
+    const int W = k.W;
     const Chunk ch = chunk_of(chunk_start, dc.n, dc.in);
     const DemIn& r = dc.in[ch.d];
     const float rain0 = (float)r.rain, rinc = (float)r.rain_inc;
     int nact = 0;
+    bool untiled = false;
+    for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
+        int x, y;
+        const size_t i = region_cell(r, ri, W, &x, &y);
+        if (mask[i]) {
+            ++nact;
+            const float coeff = (1.0f - 0.0085f * stone[i]) * expf(-0.0025f * totB[i] / 76.5f) *
+                                tanhf(0.6f + soilM[i] / 0.2f);
+            const float myppt = (rain0 + (float)(y - r.y0) * rinc) / 1000.0f;
+            const float wi = myppt * coeff;
+            float sm = soilM[i] + myppt * (1.0f - coeff);
+            if (sm > 0.5f) sm = 0.5f;
+            soilM[i] = sm;
+            w[i] = wi;
+            fa[i] = make_float2(wi, 0.0f);
+            const uint8_t code = fd[i];
+            untiled |= wi < 0.0f || (code & (code - 1));
+        } else {
+            w[i] = -9999.0f;
+            fa[i] = make_float2(0.0f, 0.0f);
+        }
+    }
+    if (__syncthreads_or(untiled) && threadIdx.x == 0) sc->tiled_ok = 0;
+    nact = wsum(nact);
+    if ((threadIdx.x & 31) == 0 && nact) atomicAdd(&dc.out[ch.d].n_active, nact);
+}
+
+// In-degrees and sources of the global accumulation wave, for the steps that
+// take it (MFD, contributing area, or a step k_fa_prep sent off the tiled path).
+__global__ void k_fa_pend(const double* __restrict__ z, const uint8_t* __restrict__ mask,
+                          const uint8_t* __restrict__ fd, int32_t* __restrict__ pending, int32_t* __restrict__ contrib,
+                          int32_t* ready, const int32_t* __restrict__ chunk_start, ModelConsts k, DemCtx dc,
+                          DevScalars* sc, int gate) {
+    if (gate && sc->tiled_ok) return;  // the tiled path accumulates this step
+    const int W = k.W, H = k.H;
+    const size_t N = (size_t)W * H;
+    const Chunk ch = chunk_of(chunk_start, dc.n, dc.in);
+    const DemIn& r = dc.in[ch.d];
     for (int64_t base = ch.first; base < ch.end; base += blockDim.x) {
         const int64_t ri = base + threadIdx.x;
         bool src = false;
@@ -45,18 +80,6 @@ __global__ void k_fa_prep(const double* __restrict__ z, const uint8_t* __restric
             int x, y;
             i = region_cell(r, ri, W, &x, &y);
             if (mask[i]) {
-                ++nact;
-                const float coeff = (1.0f - 0.0085f * stone[i]) * expf(-0.0025f * totB[i] / 76.5f) *
-                                    tanhf(0.6f + soilM[i] / 0.2f);
-                const float myppt = (rain0 + (float)(y - r.y0) * rinc) / 1000.0f;
-                const float wi = myppt * coeff;
-                float sm = soilM[i] + myppt * (1.0f - coeff);
-                if (sm > 0.5f) sm = 0.5f;
-                soilM[i] = sm;
-                w[i] = wi;
-                fa[i] = make_float2(wi, 0.0f);
-                const uint8_t code = fd[i];
-                if (wi < 0.0f || (code & (code - 1))) sc->tiled_ok = 0;
                 if (contrib) contrib[i] = 1;
                 int32_t pend = 0;
 #pragma unroll
@@ -73,16 +96,12 @@ __global__ void k_fa_prep(const double* __restrict__ z, const uint8_t* __restric
                 pending[i] = pend;
                 src = (pend == 0);
             } else {
-                w[i] = -9999.0f;
-                fa[i] = make_float2(0.0f, 0.0f);
                 if (contrib) contrib[i] = 0;
                 pending[i] = kBlocked;
             }
         }
         wave_append(src, (int32_t)i, ready, &sc->counters[0], (int)N, &sc->err);
     }
-    nact = wsum(nact);
-    if ((threadIdx.x & 31) == 0 && nact) atomicAdd(&dc.out[ch.d].n_active, nact);
 }
 
 // calcprops (runoffweight.cu:141-354): slope-proportional partition, forcing a
@@ -617,8 +636,10 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, uin
         LEM_LAUNCH(L, k_calcprops, blocks, T, s.mask, s.fd, s.slopes, s.prop, N);
         prop = s.prop;
     }
-    LEM_LAUNCH(L, k_fa_prep, s.n_chunks, T, s.z, s.mask, s.fd, s.stone, s.totB, s.soilM, s.w, s.fa, s.pending,
-               contrib, s.list_a, s.chunk_start, k, s.dems, s.sc);
+    LEM_LAUNCH(L, k_fa_prep, s.n_chunks, T, s.mask, s.fd, s.stone, s.totB, s.soilM, s.w, s.fa, s.chunk_start, k,
+               s.dems, s.sc);
+    LEM_LAUNCH(L, k_fa_pend, s.n_chunks, T, s.z, s.mask, s.fd, s.pending, contrib, s.list_a, s.chunk_start, k, s.dems,
+               s.sc, tiled);
     if (tiled) {
         const TileSet ts = tiles_of(s, k.W);
         const int tiles = ts.n;
