@@ -529,12 +529,17 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
     for (int it = 0; it < 10; ++it) {  // in-tile paths are shorter than 2^10 cells
+        bool ch = false;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int l = (ly0 + 8 * q) * kTile + lx;
-            s_nxt[l] = s_nxt[s_nxt[l]];
+            const int16_t nx = s_nxt[s_nxt[l]];
+            if (nx != s_nxt[l]) {
+                s_nxt[l] = nx;
+                ch = true;
+            }
         }
-        __syncthreads();
+        if (!__syncthreads_or(ch)) break;  // every pointer is at its path's end
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {

@@ -575,13 +575,18 @@ __global__ void __launch_bounds__(256)
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
         },
         s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
-    for (int it = 0; it < 10; ++it) {
+    for (int it = 0; it < 10; ++it) {  // in-tile paths are shorter than 2^10 cells
+        bool ch = false;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int l = (ly0 + 8 * q) * kTile + lx;
-            s_ptr[l] = s_ptr[s_ptr[l]];
+            const int16_t nx = s_ptr[s_ptr[l]];
+            if (nx != s_ptr[l]) {
+                s_ptr[l] = nx;
+                ch = true;
+            }
         }
-        __syncthreads();
+        if (!__syncthreads_or(ch)) break;  // every pointer is at its path's end
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
