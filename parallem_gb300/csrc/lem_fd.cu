@@ -557,36 +557,61 @@ __global__ void __launch_bounds__(256)
 // init_watershed_sinkMFD loop (newflow.cu:430-460): equal-height sink cells
 // adopt the largest neighbouring id until nothing changes.
 __global__ void k_flood_merge(const double* __restrict__ z, int32_t* ws, const int32_t* __restrict__ sinks,
-                              ModelConsts k, DevScalars* sc) {
+                              int32_t* merging, ModelConsts k, DevScalars* sc) {
     if (sc->sinkcount_pass1 == 0) return;
     cg::grid_group grid = cg::this_grid();
     const int W = k.W, H = k.H;
     const int n = sc->n_sinks;
     const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gtid == 0) sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
+    const size_t gstride = (size_t)gridDim.x * blockDim.x;
+    int32_t* nmerge = &sc->counters[6];
+    if (gtid == 0) {
+        sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
+        *nmerge = 0;
+    }
     grid.sync();
+    // one sink: adopt the largest id of its equal-height neighbours; false for
+    // a sink with none (a strict pit), which no later round needs to visit
+    auto relax = [&](int32_t c, int& changed) {
+        const int x = c % W, y = c / W;
+        const unsigned long long kc = dkey(z[c]);
+        const int32_t mine = __ldcg(ws + c);
+        int32_t best = mine;
+        bool eq = false;
+        for (int d = 0; kc != 0 && d < 8; ++d) {
+            const int nx = x + dir_dx(d), ny = y + dir_dy(d);
+            if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+            const size_t nb = (size_t)ny * W + nx;
+            if (dkey(z[nb]) != kc) continue;
+            eq = true;
+            const int32_t o = __ldcg(ws + nb);
+            if (o > best) best = o;
+        }
+        if (best > mine) {
+            atomicMax(ws + c, best);
+            changed = 1;
+        }
+        return eq;
+    };
     int round = 0;
     for (;; ++round) {
         if (gtid == 0) sc->flag[(round + 1) % 3] = 0;  // next round's flag; this round's is read after the sync
         int changed = 0;
-        for (size_t i = gtid; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
-            const int32_t c = sinks[i];
-            const int x = c % W, y = c / W;
-            const unsigned long long kc = dkey(z[c]);
-            const int32_t mine = __ldcg(ws + c);
-            int32_t best = mine;
-            for (int d = 0; kc != 0 && d < 8; ++d) {
-                const int nx = x + dir_dx(d), ny = y + dir_dy(d);
-                if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
-                const size_t nb = (size_t)ny * W + nx;
-                if (dkey(z[nb]) != kc) continue;
-                const int32_t o = __ldcg(ws + nb);
-                if (o > best) best = o;
+        if (round == 0) {
+            // every sink once; the ones with an equal-height neighbour are listed
+            for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)n; base += gstride) {
+                const size_t i = base + threadIdx.x;
+                bool eq = false;
+                int32_t c = 0;
+                if (i < (size_t)n) {
+                    c = sinks[i];
+                    eq = relax(c, changed);
+                }
+                warp_append(eq, c, merging, nmerge, (int)((size_t)W * H), &sc->err);
             }
-            if (best > mine) {
-                atomicMax(ws + c, best);
-                changed = 1;
-            }
+        } else {
+            const int m = *((volatile int32_t*)nmerge);
+            for (size_t i = gtid; i < (size_t)m; i += gstride) relax(__ldcg(merging + i), changed);
         }
         if (changed) sc->flag[round % 3] = 1;
         grid.sync();
@@ -869,6 +894,8 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
 // endpoint lowered in the previous round or earlier in this one (a stamp per
 // basin), so improvements run along several edges in one sweep while settled
 // parts of the graph cost only the stamp test.
+constexpr int kSpillBatch = 4;  // edges a thread tests per batch of loads in a spill round
+
 __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __restrict__ eb,
                               const unsigned long long* __restrict__ ew, unsigned long long* raise, int32_t* comp,
                               unsigned long long* cdist, unsigned long long* cmaxw, const int32_t* __restrict__ bid,
@@ -895,20 +922,38 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
     for (;; ++round) {
         if (gtid == 0) sc->flag[(round + 1) % 3] = 0;  // next round's flag; this round's is read after the sync
         int changed = 0;
-        for (size_t i = gtid; i < (size_t)n; i += gstride) {
-            const int2 uv = __ldcg(reinterpret_cast<const int2*>(euv) + i);
-            const int32_t su = __ldcg(stamp + uv.x), sv = __ldcg(stamp + uv.y);
-            if (su < round - 1 && sv < round - 1) continue;
-            const unsigned long long w = ew[i];
-            const unsigned long long du = __ldcg(bdist + uv.x), dv = __ldcg(bdist + uv.y);
-            const unsigned long long cu = w > dv ? w : dv, cv = w > du ? w : du;
-            if (cu < du && atomicMin(bdist + uv.x, cu) > cu) {
-                stamp[uv.x] = round;
-                changed = 1;
+        // kSpillBatch edges per thread at a time, their loads issued together
+        for (size_t i0 = gtid; i0 < (size_t)n; i0 += gstride * kSpillBatch) {
+            int2 uv[kSpillBatch];
+            bool live[kSpillBatch];
+#pragma unroll
+            for (int b = 0; b < kSpillBatch; ++b) {
+                const size_t i = i0 + (size_t)b * gstride;
+                uv[b] = i < (size_t)n ? __ldcg(reinterpret_cast<const int2*>(euv) + i) : make_int2(-1, -1);
             }
-            if (cv < dv && atomicMin(bdist + uv.y, cv) > cv) {
-                stamp[uv.y] = round;
-                changed = 1;
+#pragma unroll
+            for (int b = 0; b < kSpillBatch; ++b) {
+                live[b] = false;
+                if (uv[b].x >= 0) {
+                    const int32_t su = __ldcg(stamp + uv[b].x), sv = __ldcg(stamp + uv[b].y);
+                    live[b] = su >= round - 1 || sv >= round - 1;
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < kSpillBatch; ++b) {
+                if (!live[b]) continue;
+                const size_t i = i0 + (size_t)b * gstride;
+                const unsigned long long w = ew[i];
+                const unsigned long long du = __ldcg(bdist + uv[b].x), dv = __ldcg(bdist + uv[b].y);
+                const unsigned long long cu = w > dv ? w : dv, cv = w > du ? w : du;
+                if (cu < du && atomicMin(bdist + uv[b].x, cu) > cu) {
+                    stamp[uv[b].x] = round;
+                    changed = 1;
+                }
+                if (cv < dv && atomicMin(bdist + uv[b].y, cv) > cv) {
+                    stamp[uv[b].y] = round;
+                    changed = 1;
+                }
             }
         }
         if (changed) sc->flag[round % 3] = 1;
@@ -1151,9 +1196,10 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
         const double* zz = s.z;
         int32_t* ws = s.ws;
         const int32_t* sinks = s.list_b;
+        int32_t* merging = s.list_a;  // free until the pointer jumping
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
-        void* args[] = {(void*)&zz, (void*)&ws, (void*)&sinks, (void*)&kk, (void*)&sc};
+        void* args[] = {(void*)&zz, (void*)&ws, (void*)&sinks, (void*)&merging, (void*)&kk, (void*)&sc};
         if ((r = coop("k_flood_merge", (const void*)k_flood_merge, s.coop_blocks[kCkMerge], args, L)) != LEM_OK) return r;
     }
     {
