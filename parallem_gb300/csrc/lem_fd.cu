@@ -894,8 +894,6 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
 // endpoint lowered in the previous round or earlier in this one (a stamp per
 // basin), so improvements run along several edges in one sweep while settled
 // parts of the graph cost only the stamp test.
-constexpr int kSpillBatch = 4;  // edges a thread tests per batch of loads in a spill round
-
 __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __restrict__ eb,
                               const unsigned long long* __restrict__ ew, unsigned long long* raise, int32_t* comp,
                               unsigned long long* cdist, unsigned long long* cmaxw, const int32_t* __restrict__ bid,
@@ -922,38 +920,20 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
     for (;; ++round) {
         if (gtid == 0) sc->flag[(round + 1) % 3] = 0;  // next round's flag; this round's is read after the sync
         int changed = 0;
-        // kSpillBatch edges per thread at a time, their loads issued together
-        for (size_t i0 = gtid; i0 < (size_t)n; i0 += gstride * kSpillBatch) {
-            int2 uv[kSpillBatch];
-            bool live[kSpillBatch];
-#pragma unroll
-            for (int b = 0; b < kSpillBatch; ++b) {
-                const size_t i = i0 + (size_t)b * gstride;
-                uv[b] = i < (size_t)n ? __ldcg(reinterpret_cast<const int2*>(euv) + i) : make_int2(-1, -1);
+        for (size_t i = gtid; i < (size_t)n; i += gstride) {
+            const int2 uv = __ldcg(reinterpret_cast<const int2*>(euv) + i);
+            const int32_t su = __ldcg(stamp + uv.x), sv = __ldcg(stamp + uv.y);
+            if (su < round - 1 && sv < round - 1) continue;
+            const unsigned long long w = ew[i];
+            const unsigned long long du = __ldcg(bdist + uv.x), dv = __ldcg(bdist + uv.y);
+            const unsigned long long cu = w > dv ? w : dv, cv = w > du ? w : du;
+            if (cu < du && atomicMin(bdist + uv.x, cu) > cu) {
+                stamp[uv.x] = round;
+                changed = 1;
             }
-#pragma unroll
-            for (int b = 0; b < kSpillBatch; ++b) {
-                live[b] = false;
-                if (uv[b].x >= 0) {
-                    const int32_t su = __ldcg(stamp + uv[b].x), sv = __ldcg(stamp + uv[b].y);
-                    live[b] = su >= round - 1 || sv >= round - 1;
-                }
-            }
-#pragma unroll
-            for (int b = 0; b < kSpillBatch; ++b) {
-                if (!live[b]) continue;
-                const size_t i = i0 + (size_t)b * gstride;
-                const unsigned long long w = ew[i];
-                const unsigned long long du = __ldcg(bdist + uv[b].x), dv = __ldcg(bdist + uv[b].y);
-                const unsigned long long cu = w > dv ? w : dv, cv = w > du ? w : du;
-                if (cu < du && atomicMin(bdist + uv[b].x, cu) > cu) {
-                    stamp[uv[b].x] = round;
-                    changed = 1;
-                }
-                if (cv < dv && atomicMin(bdist + uv[b].y, cv) > cv) {
-                    stamp[uv[b].y] = round;
-                    changed = 1;
-                }
+            if (cv < dv && atomicMin(bdist + uv.y, cv) > cv) {
+                stamp[uv.y] = round;
+                changed = 1;
             }
         }
         if (changed) sc->flag[round % 3] = 1;
