@@ -244,6 +244,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int16_t s_ostart[kTileEnt];
     __shared__ int16_t s_ofill[kTileEnt];
     __shared__ int s_no, s_qn, s_qend;
+    __shared__ int s_wcnt[9];  // per-warp counts of the outlet list and the source append
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
@@ -340,21 +341,7 @@ __global__ void __launch_bounds__(256)
         }
     }
     // outlets in cell order (they lie on the border: at most 124)
-    if (threadIdx.x < 32) {
-        const unsigned below = (1u << lx) - 1u;
-        int no = 0;
-        for (int base = 0; base < kTile * kTile; base += 32) {
-            const int l = base + lx;
-            const bool io = s_kind[l] == kKindOutlet;
-            const unsigned mo = __ballot_sync(0xffffffffu, io);
-            if (io) {
-                s_olist[no + __popc(mo & below)] = (int16_t)l;
-                s_oslot[l] = (int16_t)(no + __popc(mo & below));
-            }
-            no += __popc(mo);
-        }
-        if (lx == 0) s_no = no;
-    }
+    list_outlets(s_kind, s_olist, s_oslot, &s_no, s_wcnt);
     if (threadIdx.x < kTileEnt) s_ocnt[threadIdx.x] = 0;
     __syncthreads();
     // inflows: ring cells of the halo that flow into the tile, grouped by the
@@ -420,7 +407,7 @@ __global__ void __launch_bounds__(256)
         t_la[og] = s_la[o];
         ready = (opend == 0);
     }
-    wave_append(ready, og, srcs, &sc->tile_src, W * H, &sc->err);
+    block_append(ready, og, srcs, &sc->tile_src, W * H, &sc->err, s_wcnt);
 }
 
 // One outlet of the coarse wave.

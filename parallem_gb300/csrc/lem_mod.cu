@@ -477,6 +477,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int16_t s_q[kTile * kTile];
     __shared__ int16_t s_rnd[kTile * kTile];
     __shared__ int s_no, s_nt, s_done, s_pool, s_dem, s_qn, s_qend;
+    __shared__ int s_wcnt[9];  // per-warp counts of the outlet list and the source append
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
@@ -598,21 +599,7 @@ __global__ void __launch_bounds__(256)
         }
         if (tx0 + lx < W && ty0 + ly < H) t_stat[g] = (s_flag[l] & kFDone) ? ((s_flag[l] & kFTaint) ? 2 : 1) : 0;
     }
-    if (threadIdx.x < 32) {
-        const unsigned below = (1u << lx) - 1u;
-        int no = 0;
-        for (int base = 0; base < kTile * kTile; base += 32) {
-            const int l = base + lx;
-            const bool io = s_kind[l] == kKindOutlet;
-            const unsigned mo = __ballot_sync(0xffffffffu, io);
-            if (io) {
-                s_olist[no + __popc(mo & below)] = (int16_t)l;
-                s_oslot[l] = (int16_t)(no + __popc(mo & below));
-            }
-            no += __popc(mo);
-        }
-        if (lx == 0) s_no = no;
-    }
+    list_outlets(s_kind, s_olist, s_oslot, &s_no, s_wcnt);
     __syncthreads();
     // inflows per outlet (ring cells flowing into the tile)
     if (threadIdx.x < kRing) {
@@ -769,7 +756,7 @@ __global__ void __launch_bounds__(256)
         t_out[og] = make_float2(s_dep[o], s_stn[o]);
         ready = (opend == 0);
     }
-    wave_append(ready, og, srcs, &sc->tile_src, W * H, &sc->err);
+    block_append(ready, og, srcs, &sc->tile_src, W * H, &sc->err, s_wcnt);
     done = wsum(done);
     if ((threadIdx.x & 31) == 0 && done) atomicAdd(&s_done, done);
     __syncthreads();

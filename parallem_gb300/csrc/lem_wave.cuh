@@ -54,6 +54,35 @@ __device__ __forceinline__ void wave_append(bool pred, int32_t value, int32_t* l
     }
 }
 
+// Append with one atomic per block: every thread of the block calls it, and
+// s_cnt holds blockDim.x / 32 + 1 ints.  The tile kernels list their ready
+// outlets this way, so the blocks of a launch do not queue on one counter
+// warp by warp.
+__device__ __forceinline__ void block_append(bool pred, int32_t value, int32_t* list, int32_t* count, int cap,
+                                             uint32_t* err, int* s_cnt) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned ballot = __ballot_sync(0xffffffffu, pred);
+    if (lane == 0) s_cnt[wid] = __popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int w = 0; w < nw; ++w) {
+            const int c = s_cnt[w];
+            s_cnt[w] = tot;
+            tot += c;
+        }
+        s_cnt[nw] = tot ? atomicAdd(count, tot) : 0;
+    }
+    __syncthreads();
+    if (pred) {
+        const int pos = s_cnt[nw] + s_cnt[wid] + __popc(ballot & ((1u << lane) - 1));
+        if (pos < cap)
+            list[pos] = value;
+        else
+            atomicOr(err, ErrFlags::kCapacity);
+    }
+}
+
 // The neighbour in direction d of cell (x, y) donates to it when its code has
 // the bit of the opposite direction.
 __device__ __forceinline__ bool donates(uint8_t code_n, int d) { return (code_n & dir_bit((d + 4) & 7)) != 0; }
@@ -179,6 +208,38 @@ constexpr uint8_t kCellIn = 1;     // a cell the wave computes
 constexpr uint8_t kCellBlock = 2;  // a donor that never completes
 
 __device__ __forceinline__ bool in_tile(int lx, int ly) { return lx >= 0 && lx < kTile && ly >= 0 && ly < kTile; }
+
+// The outlets of a 32x32 tile (cells whose receiver lies in another tile) in
+// cell order, with each outlet's slot: warp w ballots rows 4w..4w+3, and a
+// prefix over the 8 warps' counts places them.  Called by all 256 threads;
+// s_wcnt holds 8 ints; the caller synchronises before reading the lists.
+__device__ __forceinline__ void list_outlets(const uint8_t* s_kind, int16_t* s_olist, int16_t* s_oslot, int* s_no,
+                                             int* s_wcnt) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned m[4];
+    int cnt = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        m[r] = __ballot_sync(0xffffffffu, s_kind[(4 * w + r) * kTile + lane] == kKindOutlet);
+        cnt += __popc(m[r]);
+    }
+    if (lane == 0) s_wcnt[w] = cnt;
+    __syncthreads();
+    int base = 0;
+    for (int i = 0; i < w; ++i) base += s_wcnt[i];
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int l = (4 * w + r) * kTile + lane;
+        if ((m[r] >> lane) & 1u) {
+            const int pos = base + __popc(m[r] & below);
+            s_olist[pos] = (int16_t)l;
+            s_oslot[l] = (int16_t)pos;
+        }
+        base += __popc(m[r]);
+    }
+    if (threadIdx.x == 255) *s_no = base;  // the last warp's end is the total
+}
 
 // The halo ring in a fixed order: top row, bottom row, left column, right column.
 constexpr int kRing = 4 * kTH - 4;
