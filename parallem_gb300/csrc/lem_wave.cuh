@@ -257,40 +257,26 @@ __device__ __forceinline__ int ring_halo(int i) {
 // queues that receiver when c was its last donor.  Cells are queued once, in
 // an order where every donor comes before its receiver.  Every lane works on a
 // cell while the round holds one per lane, which a walk along each chain
-// cannot do.  A round of at most one cell per thread ends with one barrier
-// that also counts the cells it queued (each thread queues at most one: a cell
-// releases at most one receiver); a larger round reads the queue's end
-// between two barriers.
+// cannot do.
 template <class Op>
 __device__ __forceinline__ void tile_wave(const Op& op, int32_t* s_pend, int16_t* s_q, int* s_qn, int* s_end,
                                           const bool (&src)[4], int lx, int ly0) {
 #pragma unroll
     for (int q = 0; q < 4; ++q)
         if (src[q]) s_q[atomicAdd(s_qn, 1)] = (int16_t)((ly0 + 8 * q) * kTile + lx);
-    __syncthreads();
-    if (threadIdx.x == 0) *s_end = *s_qn;
-    __syncthreads();
-    int start = 0, end = *s_end;
-    for (int round = 0; start < end && round <= kTile * kTile; ++round) {
-        const bool wide = end - start > (int)blockDim.x;  // the same in every thread
-        bool pushed = false;
+    int start = 0;
+    for (int round = 0; round <= kTile * kTile; ++round) {
+        __syncthreads();
+        if (threadIdx.x == 0) *s_end = *s_qn;
+        __syncthreads();
+        const int end = *s_end;
+        if (start == end) break;
         for (int i = start + threadIdx.x; i < end; i += blockDim.x) {
             const int c = s_q[i];
             const int r = op(c, round);
-            if (r >= 0 && atomicSub(&s_pend[r], 1) == 1) {
-                s_q[atomicAdd(s_qn, 1)] = (int16_t)r;
-                pushed = true;
-            }
+            if (r >= 0 && atomicSub(&s_pend[r], 1) == 1) s_q[atomicAdd(s_qn, 1)] = (int16_t)r;
         }
         start = end;
-        if (wide) {
-            __syncthreads();
-            if (threadIdx.x == 0) *s_end = *s_qn;
-            __syncthreads();
-            end = *s_end;
-        } else {
-            end += __syncthreads_count(pushed);
-        }
     }
     __syncthreads();
 }
