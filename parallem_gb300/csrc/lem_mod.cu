@@ -543,7 +543,6 @@ __global__ void __launch_bounds__(256)
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             bool taint = s_ext[cur] != 0;
             float from = 0.f;
-            int lvl = 0;  // one above every waiting in-tile donor
 #pragma unroll
             for (int kk = 0; kk < 8; ++kk) {
                 const int d = scan_dir(kk);
@@ -552,12 +551,10 @@ __global__ void __launch_bounds__(256)
                 const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
                 if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
                 const int n = nly * kTile + nlx;
-                if (s_flag[n] & kFTaint) {
+                if (s_flag[n] & kFTaint)
                     taint = true;
-                    lvl = max(lvl, (int)s_rnd[n] + 1);
-                } else {
+                else
                     from = __fadd_rn(from, __fmul_rn(1.0f, s_new[n]));
-                }
             }
             if (!taint) {
                 SedLocal L;
@@ -573,7 +570,7 @@ __global__ void __launch_bounds__(256)
                 ++done;
             } else {
                 s_flag[cur] = kFDone | kFTaint;
-                s_rnd[cur] = (int16_t)lvl;  // its level for the coarse evaluation: inputs have lower levels
+                s_rnd[cur] = (int16_t)rnd;  // its level for the coarse evaluation: inputs have lower levels
                 s_topo[atomicAdd(&s_nt, 1)] = (int16_t)cur;
             }
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;

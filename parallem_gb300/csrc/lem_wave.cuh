@@ -253,12 +253,14 @@ __device__ __forceinline__ int ring_halo(int i) {
 
 // The in-tile dependency wave of one block, in rounds: a round takes every
 // queued cell (all its donors in the tile finished), computes it with
-// op(c, round), which returns the in-tile receiver it releases (or -1), and
+// op(c, level), which returns the in-tile receiver it releases (or -1), and
 // when c was the receiver's last donor goes on with the receiver itself, up to
 // kChain cells in a row, before queueing the next one for the following round.
 // Cells are computed once, each after all its donors.  Every lane works on a
 // chain while the round holds one per lane, and the chains cut the rounds
-// (and their barriers) about kChain-fold.
+// (and their barriers) about kChain-fold.  level = kChain * round + the cell's
+// place in its chain: a cell's level exceeds every in-tile donor's, and cells
+// of one level never depend on one another.
 constexpr int kChain = 4;
 template <class Op>
 __device__ __forceinline__ void tile_wave(const Op& op, int32_t* s_pend, int16_t* s_q, int* s_qn, int* s_end,
@@ -276,7 +278,7 @@ __device__ __forceinline__ void tile_wave(const Op& op, int32_t* s_pend, int16_t
         for (int i = start + threadIdx.x; i < end; i += blockDim.x) {
             int c = s_q[i];
             for (int step = 0;; ++step) {
-                const int r = op(c, round);
+                const int r = op(c, kChain * round + step);
                 if (r < 0) break;
                 __threadfence_block();  // c's results before its release
                 if (atomicSub(&s_pend[r], 1) != 1) break;
