@@ -798,8 +798,10 @@ struct SedCoarse {
                 meta = __float_as_int(r.w);
             }
             const int lvl0 = __shfl_sync(0xffffffffu, meta >> 16, 0);
-            const bool act = j < cnt && (meta >> 16) == lvl0;
-            const int run = __popc(__ballot_sync(0xffffffffu, act));  // the run of this level (a prefix)
+            // the run: the nodes from i on that share i's level (independent of one another)
+            const unsigned same = __ballot_sync(0xffffffffu, j < cnt && (meta >> 16) == lvl0);
+            const int run = same == 0xffffffffu ? 32 : __ffs(~same) - 1;
+            const bool act = lane < run;
             if (act) {
                 const int start = meta & 2047, nin = (meta >> 11) & 15;
                 const bool nz = (meta >> 15) & 1;
