@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(256)
                 ++done;
             } else {
                 s_flag[cur] = kFDone | kFTaint;
-                s_rnd[cur] = (int16_t)rnd;  // its level for the coarse evaluation: inputs have lower levels
+                s_rnd[cur] = (int16_t)rnd;  // a level for the coarse evaluation: inputs come from earlier rounds
                 s_topo[atomicAdd(&s_nt, 1)] = (int16_t)cur;
             }
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
@@ -764,8 +764,8 @@ __global__ void __launch_bounds__(256)
 }
 
 // One outlet of the coarse sediment wave, a warp per outlet: its program
-// in runs of nodes of one level (nodes of one in-tile wave level depend only
-// on nodes listed before them), then its own stores by lane 0.
+// level by level (nodes of one tile-wave round depend only on earlier rounds,
+// and the program lists them by round), then its own stores by lane 0.
 struct SedCoarse {
     const uint8_t* fd;
     const int32_t* t_orng;

@@ -253,15 +253,11 @@ __device__ __forceinline__ int ring_halo(int i) {
 
 // The in-tile dependency wave of one block, in rounds: a round takes every
 // queued cell (all its donors in the tile finished), computes it with
-// op(c, level), which returns the in-tile receiver it releases (or -1), and
-// when c was the receiver's last donor goes on with the receiver itself, up to
-// kChain cells in a row, before queueing the next one for the following round.
-// Cells are computed once, each after all its donors.  Every lane works on a
-// chain while the round holds one per lane, and the chains cut the rounds
-// (and their barriers) about kChain-fold.  level = kChain * round + the cell's
-// place in its chain: a cell's level exceeds every in-tile donor's, and cells
-// of one level never depend on one another.
-constexpr int kChain = 4;
+// op(c, round), which returns the in-tile receiver it releases (or -1), and
+// queues that receiver when c was its last donor.  Cells are queued once, in
+// an order where every donor comes before its receiver.  Every lane works on a
+// cell while the round holds one per lane, which a walk along each chain
+// cannot do.
 template <class Op>
 __device__ __forceinline__ void tile_wave(const Op& op, int32_t* s_pend, int16_t* s_q, int* s_qn, int* s_end,
                                           const bool (&src)[4], int lx, int ly0) {
@@ -276,19 +272,9 @@ __device__ __forceinline__ void tile_wave(const Op& op, int32_t* s_pend, int16_t
         const int end = *s_end;
         if (start == end) break;
         for (int i = start + threadIdx.x; i < end; i += blockDim.x) {
-            int c = s_q[i];
-            for (int step = 0;; ++step) {
-                const int r = op(c, kChain * round + step);
-                if (r < 0) break;
-                __threadfence_block();  // c's results before its release
-                if (atomicSub(&s_pend[r], 1) != 1) break;
-                if (step + 1 == kChain) {
-                    s_q[atomicAdd(s_qn, 1)] = (int16_t)r;
-                    break;
-                }
-                __threadfence_block();  // the other donors' results before r is computed
-                c = r;
-            }
+            const int c = s_q[i];
+            const int r = op(c, round);
+            if (r >= 0 && atomicSub(&s_pend[r], 1) == 1) s_q[atomicAdd(s_qn, 1)] = (int16_t)r;
         }
         start = end;
     }
