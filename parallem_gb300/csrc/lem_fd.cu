@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
             int up = 0, flat = 0;
             uint32_t aspect = 0, cand = 0;
             int bestd = -1;
-            float best = -1.0f;
+            float best = -1.0f, second = -1.0f, smin = 3.0e38f;
 #pragma unroll
             for (int d = 0; d < 8; ++d) {
                 const unsigned long long kn = skey[ly + dir_dy(d)][lx + dir_dx(d)];
@@ -148,9 +148,13 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
                     const float s = est(d);
                     cand |= 1u << d;
                     aspect |= dir_bit(d);
+                    smin = fminf(smin, s);
                     if (s > best) {
+                        second = best;
                         best = s;
                         bestd = d;
+                    } else if (s > second) {
+                        second = s;
                     }
                 }
             }
@@ -158,25 +162,34 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
             if (cand) {
                 // certify the steepest direction against the exact fp64 quotients
                 const float zs_mag = fabsf(hs);
-                bool certain = true;
                 const float inv_b = (bestd & 1) ? k.inv_len[1] : k.inv_len[0];  // the length depends on d's parity
                 const float err_b = best * 1.0e-6f + fmaxf(zs_mag, 1.0f) * 1.0e-12f * inv_b;
-                const unsigned long long kb = skey[ly + dir_dy(bestd)][lx + dir_dx(bestd)];
+                // Quick test with the largest per-direction error (the axial one):
+                // every drop far above the split error and the runner-up clearly
+                // below the best certify every direction, since the per-direction
+                // tests below are monotone in the estimate and in the error.
+                const float abs_max = fmaxf(zs_mag, 1.0f) * 1.0e-12f * fmaxf(k.inv_len[0], k.inv_len[1]);
+                bool certain = !(smin < 1.0e5f * abs_max) &&
+                               (second < 0.0f || second + (second * 1.0e-6f + abs_max) < best - err_b);
+                if (!certain) {  // the full test, direction by direction
+                    certain = true;
+                    const unsigned long long kb = skey[ly + dir_dy(bestd)][lx + dir_dx(bestd)];
 #pragma unroll
-                for (int d = 0; d < 8; ++d) {
-                    if (!((cand >> d) & 1u)) continue;
-                    const float sd = est(d);
-                    const float abs_d = fmaxf(zs_mag, 1.0f) * 1.0e-12f * k.inv_len[d];
-                    // a drop close to the split error of z: the estimate is not
-                    // within 1e-7 of the reference's slope (and may even round to 0,
-                    // while the reference stores a positive slope that aveslope counts)
-                    if (sd < 1.0e5f * abs_d) certain = false;
-                    if (d == bestd) continue;
-                    const float err_d = sd * 1.0e-6f + abs_d;
-                    if (sd + err_d < best - err_b) continue;
-                    if (((d ^ bestd) & 1) == 0 && skey[ly + dir_dy(d)][lx + dir_dx(d)] == kb && d > bestd)
-                        continue;  // exact tie
-                    certain = false;
+                    for (int d = 0; d < 8; ++d) {
+                        if (!((cand >> d) & 1u)) continue;
+                        const float sd = est(d);
+                        const float abs_d = fmaxf(zs_mag, 1.0f) * 1.0e-12f * k.inv_len[d];
+                        // a drop close to the split error of z: the estimate is not
+                        // within 1e-7 of the reference's slope (and may even round to 0,
+                        // while the reference stores a positive slope that aveslope counts)
+                        if (sd < 1.0e5f * abs_d) certain = false;
+                        if (d == bestd) continue;
+                        const float err_d = sd * 1.0e-6f + abs_d;
+                        if (sd + err_d < best - err_b) continue;
+                        if (((d ^ bestd) & 1) == 0 && skey[ly + dir_dy(d)][lx + dir_dx(d)] == kb && d > bestd)
+                            continue;  // exact tie
+                        certain = false;
+                    }
                 }
                 if (!certain) {
                     // the reference's arithmetic (newflow.cu:117,130-135)
