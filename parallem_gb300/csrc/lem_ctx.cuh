@@ -184,6 +184,35 @@ struct Launch {
     }
 };
 
+// Append with one atomic per block: every thread of the block calls it, and
+// s_cnt holds blockDim.x / 32 + 1 ints.  Kernels whose every block appends to
+// one list (sinks, plateau candidates, ready tile outlets) use it, so the
+// blocks of a launch do not queue on one counter warp by warp.
+__device__ __forceinline__ void block_append(bool pred, int32_t value, int32_t* list, int32_t* count, int cap,
+                                             uint32_t* err, int* s_cnt) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned ballot = __ballot_sync(0xffffffffu, pred);
+    if (lane == 0) s_cnt[wid] = __popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int w = 0; w < nw; ++w) {
+            const int c = s_cnt[w];
+            s_cnt[w] = tot;
+            tot += c;
+        }
+        s_cnt[nw] = tot ? atomicAdd(count, tot) : 0;
+    }
+    __syncthreads();
+    if (pred) {
+        const int pos = s_cnt[nw] + s_cnt[wid] + __popc(ballot & ((1u << lane) - 1));
+        if (pos < cap)
+            list[pos] = value;
+        else
+            atomicOr(err, ErrFlags::kCapacity);
+    }
+}
+
 // A cooperative launch (grid-wide barriers) of 256-thread blocks, as a launch
 // attribute so that it can be captured into a CUDA graph.
 inline cudaError_t coop_launch(const void* fn, int blocks, void** args, cudaStream_t st) {

@@ -84,6 +84,9 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     __shared__ unsigned long long skey[FD_BY + 2][FD_BX + 2];
     __shared__ float shi[FD_BY + 2][FD_BX + 2];
     __shared__ float slo[FD_BY + 2][FD_BX + 2];
+    __shared__ int s_cnt[FD_BX * FD_BY / 32 + 1];
+    __shared__ int s_sinks, s_flats, s_dem;
+    __shared__ unsigned long long s_low;
     const int W = k.W, H = k.H;
     const int t = ts.tile(blockIdx.x);
     const int x0 = (t % ts.tw) * kTile, y0 = (t / ts.tw) * kTile + blockIdx.y * FD_BY;
@@ -238,17 +241,30 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     // Only a candidate with an equal-height neighbour can be routed: the others
     // (single-cell pits, NaN cells) keep 2e7 and no direction, and stay off
     // the list the relaxation and the final directions work through.
-    warp_append(is_cand && has_equal, (int32_t)((size_t)y * W + x), plateau, &sc->n_cand, (int)((size_t)W * H),
-                &sc->err);
+    block_append(is_cand && has_equal, (int32_t)self, plateau, &sc->n_cand, (int)((size_t)W * H), &sc->err, s_cnt);
     if (pass == 1) {
+        // the block's counters and lowest cell, one atomic each (a block lies in one DEM)
+        if (tid == 0) {
+            s_sinks = s_flats = 0;
+            s_low = ~0ull;
+            s_dem = -1;
+        }
+        __syncthreads();
         const int s1 = warp_sum(is_sink), f1 = warp_sum(is_flat);
         low = warp_min_u64(low);
         const int d = warp_dem(dc, self, mk != 0);
-        if ((threadIdx.x & 31) == 0 && d >= 0) {
-            DemOut& o = dc.out[d];
-            if (s1) atomicAdd(&o.sink_counter, s1);
-            if (f1) atomicAdd(&o.flat_counter, f1);
-            if (low != ~0ull) atomicMin(&o.lowest_key, low);
+        if ((tid & 31) == 0) {
+            if (s1) atomicAdd(&s_sinks, s1);
+            if (f1) atomicAdd(&s_flats, f1);
+            if (low != ~0ull) atomicMin(&s_low, low);
+            if (d >= 0) atomicMax(&s_dem, d);
+        }
+        __syncthreads();
+        if (tid == 0 && s_dem >= 0) {
+            DemOut& o = dc.out[s_dem];
+            if (s_sinks) atomicAdd(&o.sink_counter, s_sinks);
+            if (s_flats) atomicAdd(&o.flat_counter, s_flats);
+            if (s_low != ~0ull) atomicMin(&o.lowest_key, s_low);
         }
     }
 }
@@ -484,11 +500,18 @@ __global__ void __launch_bounds__(256)
                  DevScalars* sc, DemCtx dc, TileSet ts) {
     __shared__ int16_t s_nxt[kTile * kTile];  // next in-tile cell of the path; the cell itself at the path's end
     __shared__ int32_t s_end[kTile * kTile];  // at a path's end: what the cells draining to it take
+    __shared__ int s_cnt[9];
+    __shared__ int s_nsink, s_dem;
     const int W = k.W, H = k.H;
     const size_t N = (size_t)W * H;
     const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % ts.tw) * kTile, ty0 = (t / ts.tw) * kTile;
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        s_nsink = 0;
+        s_dem = -1;
+    }
+    __syncthreads();
     int nsink = 0;
     int32_t own[4];
     bool term[4];
@@ -532,14 +555,12 @@ __global__ void __launch_bounds__(256)
         s_end[l] = endv;
         own[q] = ownv;
         term[q] = tm;
-        const int ws_ = warp_sum(sink ? 1 : 0);
-        const int d = warp_dem(dc, c, sink);
-        if (lx == 0 && ws_) {
-            nsink += ws_;
-            atomicAdd(&dc.out[d].sinkcount_pass1, ws_);
-        }
-        warp_append(sink, (int32_t)c, sinks, &sc->n_sinks, (int)N, &sc->err);
+        nsink += sink ? 1 : 0;
+        if (sink) atomicMax(&s_dem, dem_at(dc, c));  // one DEM per tile
+        block_append(sink, (int32_t)c, sinks, &sc->n_sinks, (int)N, &sc->err, s_cnt);
     }
+    nsink = warp_sum(nsink);
+    if (lx == 0 && nsink) atomicAdd(&s_nsink, nsink);
     __syncthreads();
     for (int it = 0; it < 10; ++it) {  // in-tile paths are shorter than 2^10 cells
         bool ch = false;
@@ -560,7 +581,10 @@ __global__ void __launch_bounds__(256)
         const int x = tx0 + lx, y = ty0 + ly;
         if (x < W && y < H) ws[(size_t)y * W + x] = term[q] ? own[q] : s_end[s_nxt[l]];
     }
-    if (nsink) atomicAdd(&sc->sinkcount_pass1, nsink);
+    if (threadIdx.x == 0 && s_nsink) {  // s_nsink is complete after the jumping loop's barriers
+        atomicAdd(&dc.out[s_dem].sinkcount_pass1, s_nsink);
+        atomicAdd(&sc->sinkcount_pass1, s_nsink);
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         raise[0] = dkey(0.0);
         bid[0] = -1;  // numbered by the compaction once basin 0 is on an edge

@@ -54,35 +54,6 @@ __device__ __forceinline__ void wave_append(bool pred, int32_t value, int32_t* l
     }
 }
 
-// Append with one atomic per block: every thread of the block calls it, and
-// s_cnt holds blockDim.x / 32 + 1 ints.  The tile kernels list their ready
-// outlets this way, so the blocks of a launch do not queue on one counter
-// warp by warp.
-__device__ __forceinline__ void block_append(bool pred, int32_t value, int32_t* list, int32_t* count, int cap,
-                                             uint32_t* err, int* s_cnt) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const unsigned ballot = __ballot_sync(0xffffffffu, pred);
-    if (lane == 0) s_cnt[wid] = __popc(ballot);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int tot = 0;
-        for (int w = 0; w < nw; ++w) {
-            const int c = s_cnt[w];
-            s_cnt[w] = tot;
-            tot += c;
-        }
-        s_cnt[nw] = tot ? atomicAdd(count, tot) : 0;
-    }
-    __syncthreads();
-    if (pred) {
-        const int pos = s_cnt[nw] + s_cnt[wid] + __popc(ballot & ((1u << lane) - 1));
-        if (pos < cap)
-            list[pos] = value;
-        else
-            atomicOr(err, ErrFlags::kCapacity);
-    }
-}
-
 // The neighbour in direction d of cell (x, y) donates to it when its code has
 // the bit of the opposite direction.
 __device__ __forceinline__ bool donates(uint8_t code_n, int d) { return (code_n & dir_bit((d + 4) & 7)) != 0; }
