@@ -185,16 +185,17 @@ struct Launch {
 };
 
 // Append with one atomic per block: every thread of the block calls it, and
-// s_cnt holds blockDim.x / 32 + 1 ints.  Kernels whose every block appends to
+// s_cnt holds (threads of the block) / 32 + 1 ints.  Kernels whose every block appends to
 // one list (sinks, plateau candidates, ready tile outlets) use it, so the
 // blocks of a launch do not queue on one counter warp by warp.
 __device__ __forceinline__ void block_append(bool pred, int32_t value, int32_t* list, int32_t* count, int cap,
                                              uint32_t* err, int* s_cnt) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;  // warps are runs of 32 linear thread ids
+    const int lane = tid & 31, wid = tid >> 5, nw = (blockDim.x * blockDim.y) >> 5;
     const unsigned ballot = __ballot_sync(0xffffffffu, pred);
     if (lane == 0) s_cnt[wid] = __popc(ballot);
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         int tot = 0;
         for (int w = 0; w < nw; ++w) {
             const int c = s_cnt[w];

@@ -311,12 +311,16 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)n; base += gstride) {
         const size_t i = base + threadIdx.x;
         bool fresh = false;
-        int32_t t = 0;
+        int32_t t = -1;
         if (i < (size_t)n) {
             const int32_t c = cand[i];
             t = (c / W / kPT) * TW + (c % W) / kPT;
-            fresh = atomicExch(mark + t, rid0 + 1) != rid0 + 1;
         }
+        // candidates come in cell order: the lanes of a warp mostly share a
+        // tile, and one lane per tile tests and sets its mark
+        const unsigned peers = __match_any_sync(0xffffffffu, t);
+        if (t >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1)
+            fresh = __ldcg(mark + t) != rid0 + 1 && atomicExch(mark + t, rid0 + 1) != rid0 + 1;
         warp_append(fresh, t, list_a, &cnt[0], ncap, &sc->err);
     }
     grid.sync();
@@ -667,6 +671,7 @@ __global__ void k_flood_jump(int32_t* ws, int32_t* list_a, int32_t* list_b, Mode
                              TileSet ts) {
     if (sc->sinkcount_pass1 == 0) return;
     cg::grid_group grid = cg::this_grid();
+    __shared__ int s_cnt[9];
     const size_t N = (size_t)k.W * k.H;
     const size_t gstride = (size_t)gridDim.x * blockDim.x;
     const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -691,7 +696,7 @@ __global__ void k_flood_jump(int32_t* ws, int32_t* list_a, int32_t* list_b, Mode
                 keep = v < 0;
             }
         }
-        warp_append(keep, (int32_t)c, list_a, &cnt[0], (int)N, &sc->err);
+        block_append(keep, (int32_t)c, list_a, &cnt[0], (int)N, &sc->err, s_cnt);
     }
     grid.sync();
     int round = 0;
@@ -718,7 +723,7 @@ __global__ void k_flood_jump(int32_t* ws, int32_t* list_a, int32_t* list_b, Mode
                     keep = v < 0;
                 }
             }
-            warp_append(keep, c, out, &cnt[(round + 1) % 3], (int)N, &sc->err);
+            block_append(keep, c, out, &cnt[(round + 1) % 3], (int)N, &sc->err, s_cnt);
         }
         grid.sync();
     }
