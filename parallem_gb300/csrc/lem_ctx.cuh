@@ -185,11 +185,11 @@ struct Launch {
 };
 
 // Append with one atomic per block: every thread of the block calls it, and
-// s_cnt holds (threads of the block) / 32 + 1 ints.  Kernels whose every block appends to
+// s_cnt holds (threads of the block) / 32 + 1 ints.  block_reserve returns the
+// list position of a thread with pred set (-1 otherwise).  Kernels whose every block appends to
 // one list (sinks, plateau candidates, ready tile outlets) use it, so the
 // blocks of a launch do not queue on one counter warp by warp.
-__device__ __forceinline__ void block_append(bool pred, int32_t value, int32_t* list, int32_t* count, int cap,
-                                             uint32_t* err, int* s_cnt) {
+__device__ __forceinline__ int block_reserve(bool pred, int32_t* count, int* s_cnt) {
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;  // warps are runs of 32 linear thread ids
     const int lane = tid & 31, wid = tid >> 5, nw = (blockDim.x * blockDim.y) >> 5;
     const unsigned ballot = __ballot_sync(0xffffffffu, pred);
@@ -205,8 +205,12 @@ __device__ __forceinline__ void block_append(bool pred, int32_t value, int32_t* 
         s_cnt[nw] = tot ? atomicAdd(count, tot) : 0;
     }
     __syncthreads();
-    if (pred) {
-        const int pos = s_cnt[nw] + s_cnt[wid] + __popc(ballot & ((1u << lane) - 1));
+    return pred ? s_cnt[nw] + s_cnt[wid] + __popc(ballot & ((1u << lane) - 1)) : -1;
+}
+__device__ __forceinline__ void block_append(bool pred, int32_t value, int32_t* list, int32_t* count, int cap,
+                                             uint32_t* err, int* s_cnt) {
+    const int pos = block_reserve(pred, count, s_cnt);
+    if (pos >= 0) {
         if (pos < cap)
             list[pos] = value;
         else

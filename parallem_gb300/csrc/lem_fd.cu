@@ -856,6 +856,7 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
                                 unsigned long long* raise, int32_t* seen, int32_t* bid, int32_t* blab,
                                 DevScalars* sc, DemCtx dc) {
     if (sc->sinkcount_pass1 == 0) return;
+    __shared__ int s_cnt[9];
     const int32_t epoch = sc->epoch;
     const size_t cap = 1ull << edge_logcap(sc, logmax);
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)cap; base += (size_t)gridDim.x * blockDim.x) {
@@ -886,41 +887,27 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
                 if (b != 0) raise[b] = ~0ull;
             }
         }
-        // number the basins first seen here: one atomic per warp
-        {
-            const unsigned lanes_below = (1u << (threadIdx.x & 31)) - 1;
-            const unsigned ma = __ballot_sync(0xffffffffu, fa_), mb = __ballot_sync(0xffffffffu, fb_);
-            const int tot = __popc(ma) + __popc(mb);
-            int base = 0;
-            if (tot) {
-                if ((threadIdx.x & 31) == 0) base = atomicAdd(&sc->n_basins, tot);
-                base = __shfl_sync(0xffffffffu, base, 0);
-            }
-            if (fa_) {
-                const int32_t id = base + __popc(ma & lanes_below);
-                bid[a] = id;
-                blab[id] = a;
-            }
-            if (fb_) {
-                const int32_t id = base + __popc(ma) + __popc(mb & lanes_below);
-                bid[b] = id;
-                blab[id] = b;
-            }
+        // number the basins first seen here: one atomic per block
+        const int pa = block_reserve(fa_, &sc->n_basins, s_cnt);
+        if (pa >= 0) {
+            bid[a] = pa;
+            blab[pa] = a;
+        }
+        const int pb = block_reserve(fb_, &sc->n_basins, s_cnt);
+        if (pb >= 0) {
+            bid[b] = pb;
+            blab[pb] = b;
         }
         // one atomic per DEM and warp for the label counts
         const unsigned grp = __match_any_sync(0xffffffffu, nd ? d : -1);
         const int gsum = __reduce_add_sync(grp, nd);
         if (nd && (grp & ((1u << (threadIdx.x & 31)) - 1)) == 0) atomicAdd(&dc.out[d].sinkcount, gsum);
-        unsigned ballot = __ballot_sync(0xffffffffu, has);
-        if (!ballot) continue;
-        const int lane = threadIdx.x & 31, leader = __ffs(ballot) - 1;
-        int pos = 0;
-        if (lane == leader) pos = atomicAdd(&sc->n_edges, __popc(ballot));
-        pos = __shfl_sync(0xffffffffu, pos, leader) + __popc(ballot & ((1u << lane) - 1));
-        if (has) {
-            ea[pos] = a;
-            eb[pos] = b;
-            ew[pos] = w;
+        // the edge list: one atomic per block
+        const int pe = block_reserve(has, &sc->n_edges, s_cnt);
+        if (pe >= 0) {
+            ea[pe] = a;
+            eb[pe] = b;
+            ew[pe] = w;
         }
     }
 }
