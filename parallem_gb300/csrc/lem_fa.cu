@@ -25,6 +25,18 @@ namespace {
 // calcrunoffweight (runoffweight.cu:21-58) plus the in-degrees of the wave.
 // A donor outside the catchment is complete from the start when its DEM is
 // nodata (correctmfdflow's okgrid, mfd_simple.cu:279-285) and never otherwise.
+// Sum over a block of 256 threads (every thread calls it; the result is valid in thread 0).
+__device__ __forceinline__ int block_sum_i(int v) {
+    __shared__ int part[8];
+    v = wsum(v);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < 8; ++w) t += part[w];
+    return t;
+}
+
 __global__ void k_fa_prep(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                           const float* __restrict__ stone, const float* __restrict__ totB, float* __restrict__ soilM,
                           float* __restrict__ w, float2* __restrict__ fa, const int32_t* __restrict__ chunk_start,
@@ -57,8 +69,8 @@ __global__ void k_fa_prep(const uint8_t* __restrict__ mask, const uint8_t* __res
         }
     }
     if (__syncthreads_or(untiled) && threadIdx.x == 0) sc->tiled_ok = 0;
-    nact = wsum(nact);
-    if ((threadIdx.x & 31) == 0 && nact) atomicAdd(&dc.out[ch.d].n_active, nact);
+    const int tot = __syncthreads_count(nact > 0) ? block_sum_i(nact) : 0;  // one atomic per block
+    if (threadIdx.x == 0 && tot) atomicAdd(&dc.out[ch.d].n_active, tot);
 }
 
 // In-degrees and sources of the global accumulation wave, for the steps that
