@@ -70,16 +70,16 @@ lem_status cuda_fail(cudaError_t e, const char* what, const char* file, int line
 using namespace lem;
 
 // The autotuner: over its next steps a handle runs every cooperative kernel
-// with 1, 2, 3 and 4 blocks per SM in turn (step s of the tuning runs
-// candidate s % 4, so the drift of the model state between steps falls on all
-// candidates alike; the first step, under the default schedule, is not
-// measured), times each with events, and keeps for each kernel the block count
-// with the lowest mean time when it beats the default (every co-resident
-// block) by more than the step-to-step noise.  Results do not depend on the
-// block count: every loop runs to a unique fixpoint and sums are pulled in a
-// fixed order.
+// with 1, 2 and 4 blocks per SM and with all its co-resident blocks in turn
+// (step s of the tuning runs candidate s % 4, so the drift of the model state
+// between steps falls on all candidates alike; the first step, under the
+// default schedule, is not measured), times each with events, and keeps for
+// each kernel the block count with the lowest mean time when it beats the
+// default (every co-resident block) by more than the step-to-step noise.
+// Results do not depend on the block count: every loop runs to a unique
+// fixpoint and sums are pulled in a fixed order.
 constexpr int kTuneCands = 4;
-constexpr int kTuneBlocksPerSm[kTuneCands] = {1, 2, 3, 4};
+constexpr int kTuneBlocksPerSm[kTuneCands] = {1, 2, 4, 0};  // 0: every co-resident block
 constexpr double kTuneMargin = 0.97;  // a candidate replaces the default only below 97 % of its time
 const char* const kCoopNames[kCoopKernels] = {"k_plateau_relax", "k_flood_merge", "k_flood_jump", "k_flood_spill",
                                               "k_fat_coarse",    "k_fa_walk",     "k_sedt_coarse", "k_sed_walk"};
@@ -702,7 +702,15 @@ lem_status create_common(const lem_grid_desc* grid, const lem_params* params, in
     for (int i = 0; i < fa_coop_kernel_count; ++i) blocks = std::min(blocks, coop_blocks_for(fa_coop_kernels[i], 256, 0));
     for (int i = 0; i < mod_coop_kernel_count; ++i) blocks = std::min(blocks, coop_blocks_for(mod_coop_kernels[i], 256, 0));
     s.max_coop_blocks = blocks;
-    for (int i = 0; i < kCoopKernels; ++i) s.coop_blocks[i] = blocks;
+    // each cooperative kernel's own co-residency bounds its launches (the
+    // kernel arrays of the three files, in CoopKernel order)
+    const void* const coop_fn[kCoopKernels] = {fd_coop_kernels[0], fd_coop_kernels[1], fd_coop_kernels[2],
+                                               fd_coop_kernels[3], fa_coop_kernels[1], fa_coop_kernels[0],
+                                               mod_coop_kernels[1], mod_coop_kernels[0]};
+    for (int i = 0; i < kCoopKernels; ++i) {
+        s.coop_cap[i] = coop_blocks_for(coop_fn[i], 256, 0);
+        s.coop_blocks[i] = s.coop_cap[i];
+    }
     cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device);
     *out = h;
     return LEM_OK;
@@ -730,15 +738,16 @@ lem_status profile_collect(lem_handle* h, std::vector<lem_kernel_stat>& agg) {
     return LEM_OK;
 }
 
-int coop_blocks_of(const lem_handle* h, int cand) {
-    return std::max(1, std::min(h->s.max_coop_blocks, kTuneBlocksPerSm[cand] * h->sms));
+int coop_blocks_of(const lem_handle* h, int kernel, int cand) {
+    const int cap = h->s.coop_cap[kernel];
+    return kTuneBlocksPerSm[cand] == 0 ? cap : std::max(1, std::min(cap, kTuneBlocksPerSm[cand] * h->sms));
 }
 
 // The schedule of the tuner's current step.
 void tune_apply(lem_handle* h) {
     const Tuner& t = h->tune;
     const int c = t.step < 0 ? kTuneCands - 1 : t.step % kTuneCands;
-    for (int i = 0; i < kCoopKernels; ++i) h->s.coop_blocks[i] = coop_blocks_of(h, c);
+    for (int i = 0; i < kCoopKernels; ++i) h->s.coop_blocks[i] = coop_blocks_of(h, i, c);
 }
 
 // Books the kernel times of a tuning step; after the last one, keeps for every
@@ -764,7 +773,7 @@ lem_status tune_record(lem_handle* h) {
         for (int c = 0; c < kTuneCands; ++c)
             if (t.coop_ms[i][c] / t.coop_n[c] < t.coop_ms[i][best] / t.coop_n[best]) best = c;
         if (t.coop_ms[i][best] / t.coop_n[best] > kTuneMargin * t.coop_ms[i][def] / t.coop_n[def]) best = def;
-        h->s.coop_blocks[i] = coop_blocks_of(h, best);
+        h->s.coop_blocks[i] = coop_blocks_of(h, i, best);
         t.default_ms += t.coop_ms[i][def] / t.coop_n[def];
         t.tuned_ms += t.coop_ms[i][best] / t.coop_n[best];
     }

@@ -102,7 +102,8 @@ struct DevState {
     int32_t n_live;             // tiles the canvas-wide kernels visit
     float* temp_tab;
     int32_t max_coop_blocks;    // co-resident blocks of the cooperative kernels
-    int32_t coop_blocks[kCoopKernels];  // blocks each cooperative kernel launches with (<= max_coop_blocks)
+    int32_t coop_blocks[kCoopKernels];  // blocks each cooperative kernel launches with (<= its coop_cap)
+    int32_t coop_cap[kCoopKernels];     // co-resident blocks of each cooperative kernel
 };
 
 // The tiles a canvas-wide kernel visits: in a batch grid the 32x32 tiles that
