@@ -285,7 +285,7 @@ constexpr int kTileSweeps = 2048;  // sweeps of one tile visit before it is re-q
 // candidate.  The fixpoint is unique, so the visiting order does not change the
 // result.  Only candidates (sp > 0) ever change: every other cell is a source
 // at 0.
-__global__ void __launch_bounds__(256, 6) k_plateau_relax(const double* __restrict__ z, float* sp,
+__global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict__ z, float* sp,
                                                        const int32_t* __restrict__ cand, int32_t* list_a,
                                                        int32_t* list_b, int32_t* mark, ModelConsts k,
                                                        DevScalars* sc, int pass) {
