@@ -254,9 +254,10 @@ lem_status lem_set_graphs(lem_handle* h, int32_t on);
 /* Autotuner of the launch schedule (no counterpart in the reference).  The
  * handle's next 1 + 4 * cycles steps (lem_step or lem_step_batch; real steps
  * of the model, launched eagerly) run the cooperative kernels with 1, 2 and 4
- * blocks per SM and with all their co-resident blocks (the default) in turn,
- * and time them with events; afterwards each keeps the block count with the
- * lowest mean time if it beats the default by more than 3 %.  Results are the same under every block count.  LEM_ERR_STATE while
+ * blocks per SM and with all their co-resident blocks in turn, and time them
+ * with events; afterwards each keeps the block count with the lowest mean
+ * time if it beats the default by more than 3 %.  The default, also before
+ * any tuning, is the block count every cooperative kernel can hold at once.  Results are the same under every block count.  LEM_ERR_STATE while
  * profiling is on (and lem_set_profiling and lem_profile_read return it while
  * tuning). */
 #define LEM_TUNE_COOP 8   /* k_plateau_relax, k_flood_merge, k_flood_jump, k_flood_spill,

@@ -75,11 +75,13 @@ using namespace lem;
 // between steps falls on all candidates alike; the first step, under the
 // default schedule, is not measured), times each with events, and keeps for
 // each kernel the block count with the lowest mean time when it beats the
-// default (every co-resident block) by more than the step-to-step noise.
-// Results do not depend on the block count: every loop runs to a unique
-// fixpoint and sums are pulled in a fixed order.
+// default by more than the step-to-step noise.  The default is the block
+// count every cooperative kernel can hold at once (4 per SM here), candidate
+// kTuneDefault.  Results do not depend on the block count: every loop runs to
+// a unique fixpoint and sums are pulled in a fixed order.
 constexpr int kTuneCands = 4;
 constexpr int kTuneBlocksPerSm[kTuneCands] = {1, 2, 4, 0};  // 0: every co-resident block
+constexpr int kTuneDefault = 2;
 constexpr double kTuneMargin = 0.97;  // a candidate replaces the default only below 97 % of its time
 const char* const kCoopNames[kCoopKernels] = {"k_plateau_relax", "k_flood_merge", "k_flood_jump", "k_flood_spill",
                                               "k_fat_coarse",    "k_fa_walk",     "k_sedt_coarse", "k_sed_walk"};
@@ -709,7 +711,7 @@ lem_status create_common(const lem_grid_desc* grid, const lem_params* params, in
                                                mod_coop_kernels[1], mod_coop_kernels[0]};
     for (int i = 0; i < kCoopKernels; ++i) {
         s.coop_cap[i] = coop_blocks_for(coop_fn[i], 256, 0);
-        s.coop_blocks[i] = s.coop_cap[i];
+        s.coop_blocks[i] = std::min(s.coop_cap[i], blocks);  // untuned: the blocks every one of them can hold
     }
     cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device);
     *out = h;
@@ -740,13 +742,14 @@ lem_status profile_collect(lem_handle* h, std::vector<lem_kernel_stat>& agg) {
 
 int coop_blocks_of(const lem_handle* h, int kernel, int cand) {
     const int cap = h->s.coop_cap[kernel];
+    if (cand == kTuneDefault) return std::min(cap, h->s.max_coop_blocks);
     return kTuneBlocksPerSm[cand] == 0 ? cap : std::max(1, std::min(cap, kTuneBlocksPerSm[cand] * h->sms));
 }
 
 // The schedule of the tuner's current step.
 void tune_apply(lem_handle* h) {
     const Tuner& t = h->tune;
-    const int c = t.step < 0 ? kTuneCands - 1 : t.step % kTuneCands;
+    const int c = t.step < 0 ? kTuneDefault : t.step % kTuneCands;
     for (int i = 0; i < kCoopKernels; ++i) h->s.coop_blocks[i] = coop_blocks_of(h, i, c);
 }
 
@@ -766,7 +769,7 @@ lem_status tune_record(lem_handle* h) {
         t.coop_n[c] += 1;
     }
     if (++t.step < t.steps) return LEM_OK;
-    const int def = kTuneCands - 1;  // the default: every co-resident block (the largest candidate)
+    const int def = kTuneDefault;
     t.default_ms = t.tuned_ms = 0;
     for (int i = 0; i < kCoopKernels; ++i) {
         int best = def;
