@@ -5,7 +5,7 @@ one step.  Tolerances (stated per check):
 * direction codes, sink counts, contributing-cell counts: bit-exact;
 * slopes: 2e-6 relative + 1e-12 absolute (fp32 storage of the reference's
   fp64 quotient);
-* accumulation: 1e-5 relative (the benchmark spec's bound); elevation: 1e-9
+* accumulation: 1e-5 relative (the required bound); elevation: 1e-9
   relative + 1e-6 m (fp64 state, fp32 increments);
 * process grids: |gpu - oracle| <= 1e-5 |oracle| + 1e-6 max|oracle| (fp32
   arithmetic; differences such as geli = soilT - ero and dz cancel);
