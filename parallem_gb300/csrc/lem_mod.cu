@@ -806,32 +806,17 @@ struct SedCoarse {
                 const int start = meta & 2047, nin = (meta >> 11) & 15;
                 const bool nz = (meta >> 15) & 1;
                 float from = r.z;
-                // inputs four at a time: their references and maps, then their
-                // values, each as one batch of independent loads, summed in order
-                for (int j0 = 0; j0 < nin; j0 += 4) {
-                    int32_t ref[4];
-                    float4 mp[4];
-                    float v[4];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        if (j0 + q < nin) {
-                            ref[q] = __ldg(p_ref + pool + start + j0 + q);
-                            mp[q] = __ldg(p_map + pool + start + j0 + q);
-                        }
-                    }
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        if (j0 + q >= nin) continue;
-                        if (ref[q] >= 0)
-                            v[q] = __ldcg(stone + ref[q]);
-                        else if (-ref[q] - 1 < kProgLocal)
-                            v[q] = vals[-ref[q] - 1];
-                        else
-                            v[q] = __ldcg(p_val + nbase - ref[q] - 1);
-                    }
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        if (j0 + q < nin) from = __fadd_rn(from, __fmul_rn(1.0f, map_apply(mp[q], v[q])));
+                for (int jr = 0; jr < nin; ++jr) {
+                    const int32_t ref = __ldg(p_ref + pool + start + jr);
+                    const float4 mp = __ldg(p_map + pool + start + jr);
+                    float v;
+                    if (ref >= 0)
+                        v = __ldcg(stone + ref);
+                    else if (-ref - 1 < kProgLocal)
+                        v = vals[-ref - 1];
+                    else
+                        v = __ldcg(p_val + nbase - ref - 1);
+                    from = __fadd_rn(from, __fmul_rn(1.0f, map_apply(mp, v)));
                 }
                 const float sn = nz ? sed_mix(r.x, r.y, from) : r.x;
                 if (j < kProgLocal)
