@@ -445,7 +445,7 @@ __device__ __forceinline__ SedInit sed_init(const uint8_t* s_code, const uint8_t
     return r;
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)
     k_sedt_local(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd, const float* __restrict__ ero,
                  const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
                  float* fines, float* soilT, int32_t* __restrict__ t_dst, int32_t* __restrict__ t_pend,
@@ -642,6 +642,36 @@ __global__ void __launch_bounds__(256)
         const int l = (ly0 + 8 * q) * kTile + lx;
         if (s_node[l]) atomicAdd(&s_pcnt[s_oslot[s_ptr[l]]], 1);
     }
+    // every waiting cell between nodes: its one waiting in-tile donor (in s_q,
+    // spent since the wave) and its map v -> stone (in place of its own
+    // coefficients, which only nodes need from here on), so that the walks
+    // from a node's inputs up to the next node only compose maps
+    int16_t* s_up = s_q;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
+        if (s_flag[l] != (kFDone | kFTaint) || s_node[l] || s_kind[s_ptr[l]] != kKindOutlet) continue;
+        float Cc = 0.f;
+        int up = l;
+#pragma unroll
+        for (int k2 = 0; k2 < 8; ++k2) {
+            const int d2 = scan_dir(k2);
+            const int ulx = lx + dir_dx(d2), uly = ly + dir_dy(d2);
+            const int uh = hc + dir_dy(d2) * kTH + dir_dx(d2);
+            if (!in_tile(ulx, uly) || !donates(s_code[uh], d2) || s_cls[uh] != kCellIn) continue;
+            const int u = uly * kTile + ulx;
+            if (s_flag[u] & kFTaint)
+                up = u;
+            else
+                Cc = __fadd_rn(Cc, __fmul_rn(1.0f, s_new[u]));
+        }
+        const float4 M = map_cell(s_A[l], s_B[l], Cc, s_nz[l] != 0, s_new[l]);
+        s_A[l] = M.x;
+        s_B[l] = M.y;
+        s_dep[l] = M.z;
+        s_stn[l] = M.w;
+        s_up[l] = (int16_t)up;
+    }
     __syncthreads();
     const int no = s_no, nt = s_nt;
     if (threadIdx.x == 0) {
@@ -718,22 +748,8 @@ __global__ void __launch_bounds__(256)
             // follow the single-input cells up to the node that feeds this input
             float4 H = map_identity();
             for (int guard = 0; !s_node[cur] && guard < kTile * kTile; ++guard) {
-                const int cx = cur & (kTile - 1), cy = cur / kTile, ch = (cy + 1) * kTH + cx + 1;
-                float Cc = 0.f;
-                int up = cur;
-#pragma unroll
-                for (int k2 = 0; k2 < 8; ++k2) {
-                    const int d2 = scan_dir(k2);
-                    const int ulx = cx + dir_dx(d2), uly = cy + dir_dy(d2);
-                    const int uh = ch + dir_dy(d2) * kTH + dir_dx(d2);
-                    if (!in_tile(ulx, uly) || !donates(s_code[uh], d2) || s_cls[uh] != kCellIn) continue;
-                    const int u = uly * kTile + ulx;
-                    if (s_flag[u] & kFTaint)
-                        up = u;
-                    else
-                        Cc = __fadd_rn(Cc, __fmul_rn(1.0f, s_new[u]));
-                }
-                H = map_compose(H, map_cell(s_A[cur], s_B[cur], Cc, s_nz[cur] != 0, s_new[cur]));
+                H = map_compose(H, make_float4(s_A[cur], s_B[cur], s_dep[cur], s_stn[cur]));
+                const int up = s_up[cur];
                 if (up == cur) break;  // not reached: a waiting cell always has a waiting donor or an inflow
                 cur = up;
             }
