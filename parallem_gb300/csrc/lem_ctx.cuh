@@ -76,8 +76,16 @@ struct DevState {
     float4* p_abc;      // node: stone mix coefficients A, B, the settled donors' sum C, inputs and flags
     int32_t* p_ref;     // per tile, kPool node inputs: the feeding node (program slot) or cell
     float4* p_map;      // per tile, kPool node inputs: the map through the cells in between
-    float* p_val;       // slot: values of programs longer than the evaluator's local buffer
+    float* p_val;       // slot: the value of every program node once the coarse wave has run
     uint8_t* t_stat;    // cell: 1 settled inside its tile, 2 waits on another tile, 0 neither
+                        //   (written for the tiles whose waiting cells are routed by a second wave)
+    // per tile, kTile*kTile slots: the waiting cells the final pass stores,
+    // each as its outlet, the program node that feeds it and the map from that
+    // node's value to its own stone
+    int4* f_idx;        // cell, p_val slot of the feeding node, outlet cell, flags
+    float4* f_map;      // clamp map: feeding node's value -> the cell's stone
+    float2* f_ds;       // the cell's deposition and new soil thickness
+    int32_t* t_fcnt;    // tile: number of such cells; -1: its waiting cells need the second wave
     // flooding tables
     unsigned long long* ekey;   // hash keys (label pair)
     unsigned long long* ewt;    // min boundary height key

@@ -355,6 +355,8 @@ __global__ void k_sed_walk(const uint8_t* __restrict__ mask, const uint8_t* __re
 // computed; every other in-grid donor blocks its receiver.
 
 constexpr int kProgLocal = 256;  // program nodes the coarse evaluator keeps in local memory
+constexpr int kFinNz = 1;      // final-pass slot: the cell's sediment column is not empty
+constexpr int kFinOutlet = 2;  // final-pass slot: an outlet (the coarse wave stored it; counted only)
 constexpr int kPool = kTilePool;
 constexpr uint8_t kFDone = 1, kFTaint = 2;
 
@@ -451,7 +453,8 @@ __global__ void __launch_bounds__(256, 5)
                  float* fines, float* soilT, int32_t* __restrict__ t_dst, int32_t* __restrict__ t_pend,
                  int32_t* __restrict__ t_orng, float2* __restrict__ t_out, float4* __restrict__ p_abc,
                  int32_t* __restrict__ p_ref, float4* __restrict__ p_map, uint8_t* __restrict__ t_stat,
-                 int32_t* srcs, ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts) {
+                 int4* __restrict__ f_idx, float4* __restrict__ f_map, float2* __restrict__ f_ds,
+                 int32_t* __restrict__ t_fcnt, int32_t* srcs, ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts) {
     if (!sc->sed_tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -476,7 +479,7 @@ __global__ void __launch_bounds__(256, 5)
     __shared__ int16_t s_pfill[kTileEnt];
     __shared__ int16_t s_q[kTile * kTile];
     __shared__ int16_t s_rnd[kTile * kTile];
-    __shared__ int s_no, s_nt, s_done, s_pool, s_dem, s_qn, s_qend;
+    __shared__ int s_no, s_nt, s_done, s_pool, s_dem, s_qn, s_qend, s_fn;
     __shared__ int s_wcnt[9];  // per-warp counts of the outlet list and the source append
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = ts.tile(blockIdx.x);
@@ -486,7 +489,7 @@ __global__ void __launch_bounds__(256, 5)
         s_ocnt[threadIdx.x] = 0;
         s_pcnt[threadIdx.x] = 0;
     }
-    if (threadIdx.x == 0) s_nt = s_done = 0, s_dem = -1;
+    if (threadIdx.x == 0) s_nt = s_done = s_fn = 0, s_dem = -1;
     __syncthreads();
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     bool src[4];
@@ -589,6 +592,7 @@ __global__ void __launch_bounds__(256, 5)
         }
         if (!__syncthreads_or(ch)) break;  // every pointer is at its path's end
     }
+    bool stray = false;  // a waiting cell whose in-tile path ends inside the tile (at the DEM's outlet, say)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int ly = ly0 + 8 * q, l = ly * kTile + lx;
@@ -597,7 +601,20 @@ __global__ void __launch_bounds__(256, 5)
             const int e = s_ptr[l];
             t_dst[g] = s_kind[e] == kKindOutlet ? (int32_t)((ty0 + e / kTile) * W + tx0 + (e & (kTile - 1))) : -1;
         }
-        if (tx0 + lx < W && ty0 + ly < H) t_stat[g] = (s_flag[l] & kFDone) ? ((s_flag[l] & kFTaint) ? 2 : 1) : 0;
+        stray |= s_flag[l] == (kFDone | kFTaint) && s_kind[s_ptr[l]] != kKindOutlet;
+    }
+    // Such a tile keeps the second wave for its waiting cells (it needs their
+    // status); in every other tile each waiting cell's stone is a map of one
+    // program node's value, stored by the final pass.
+    const bool second_wave = __syncthreads_or(stray);
+    if (second_wave) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int ly = ly0 + 8 * q, l = ly * kTile + lx;
+            if (tx0 + lx < W && ty0 + ly < H)
+                t_stat[(size_t)(ty0 + ly) * W + tx0 + lx] =
+                    (s_flag[l] & kFDone) ? ((s_flag[l] & kFTaint) ? 2 : 1) : 0;
+        }
     }
     list_outlets(s_kind, s_olist, s_oslot, &s_no, s_wcnt);
     __syncthreads();
@@ -642,15 +659,24 @@ __global__ void __launch_bounds__(256, 5)
         const int l = (ly0 + 8 * q) * kTile + lx;
         if (s_node[l]) atomicAdd(&s_pcnt[s_oslot[s_ptr[l]]], 1);
     }
-    // every waiting cell between nodes: its one waiting in-tile donor (in s_q,
+    // Every waiting cell between nodes: its one waiting in-tile donor (in s_q,
     // spent since the wave) and its map v -> stone (in place of its own
-    // coefficients, which only nodes need from here on), so that the walks
-    // from a node's inputs up to the next node only compose maps
+    // coefficients, which only nodes need from here on).  Every waiting cell of
+    // a tile without a second wave also takes a final-pass slot, with its
+    // deposition and soil thickness.
     int16_t* s_up = s_q;
+    const size_t fbase = (size_t)t * kTile * kTile;
+    int fslot[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
-        if (s_flag[l] != (kFDone | kFTaint) || s_node[l] || s_kind[s_ptr[l]] != kKindOutlet) continue;
+        fslot[q] = -1;
+        if (s_flag[l] != (kFDone | kFTaint) || s_kind[s_ptr[l]] != kKindOutlet) continue;
+        if (!second_wave) {
+            fslot[q] = atomicAdd(&s_fn, 1);
+            f_ds[fbase + fslot[q]] = make_float2(s_dep[l], s_stn[l]);
+        }
+        if (s_node[l]) continue;
         float Cc = 0.f;
         int up = l;
 #pragma unroll
@@ -673,6 +699,39 @@ __global__ void __launch_bounds__(256, 5)
         s_up[l] = (int16_t)up;
     }
     __syncthreads();
+    // Pointer jumping along the single-input chains: afterwards s_up of a cell
+    // between nodes is the node at the top of its chain and its map takes that
+    // node's value to its own stone (maps compose, so the chain needs only
+    // log2 of its length in rounds).
+    for (int it = 0; it < 10; ++it) {  // in-tile chains are shorter than 2^10 cells
+        float4 F[4];
+        int16_t P[4];
+        bool ch = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int l = (ly0 + 8 * q) * kTile + lx;
+            P[q] = -1;
+            if (s_flag[l] != (kFDone | kFTaint) || s_node[l] || s_kind[s_ptr[l]] != kKindOutlet) continue;
+            const int p = s_up[l];
+            if (s_node[p]) continue;
+            F[q] = map_compose(make_float4(s_A[l], s_B[l], s_dep[l], s_stn[l]),
+                               make_float4(s_A[p], s_B[p], s_dep[p], s_stn[p]));
+            P[q] = s_up[p];
+            ch = true;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int l = (ly0 + 8 * q) * kTile + lx;
+            if (P[q] < 0) continue;
+            s_A[l] = F[q].x;
+            s_B[l] = F[q].y;
+            s_dep[l] = F[q].z;
+            s_stn[l] = F[q].w;
+            s_up[l] = P[q];
+        }
+        if (!__syncthreads_or(ch)) break;
+    }
     const int no = s_no, nt = s_nt;
     if (threadIdx.x == 0) {
         int a = 0;
@@ -745,13 +804,11 @@ __global__ void __launch_bounds__(256, 5)
                 C = __fadd_rn(C, __fmul_rn(1.0f, s_new[cur]));
                 continue;
             }
-            // follow the single-input cells up to the node that feeds this input
+            // the node that feeds this input, through the single-input cells in between
             float4 H = map_identity();
-            for (int guard = 0; !s_node[cur] && guard < kTile * kTile; ++guard) {
-                H = map_compose(H, make_float4(s_A[cur], s_B[cur], s_dep[cur], s_stn[cur]));
-                const int up = s_up[cur];
-                if (up == cur) break;  // not reached: a waiting cell always has a waiting donor or an inflow
-                cur = up;
+            if (!s_node[cur]) {
+                H = make_float4(s_A[cur], s_B[cur], s_dep[cur], s_stn[cur]);
+                cur = s_up[cur];
             }
             p_ref[pool + start + m] = -(s_pos[cur] - first + 1);
             p_map[pool + start + m] = H;
@@ -760,6 +817,23 @@ __global__ void __launch_bounds__(256, 5)
         p_abc[nbase + pos] =
             make_float4(s_A[l], s_B[l], C, __int_as_float(start | (m << 11) | (s_nz[l] << 15) | ((int)s_rnd[l] << 16)));
     }
+    // the final pass's slots: a node reads its own value, a cell between nodes
+    // maps the value of the node at the top of its chain
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (fslot[q] < 0) continue;
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx;
+        const bool node = s_node[l] != 0;
+        const int src_node = node ? l : s_up[l];
+        const int e = s_ptr[l];
+        // (a chain always ends at a node; -1 only guards the final pass's read)
+        const int vref = s_node[src_node] && s_pos[src_node] >= 0 ? (int)(fbase + s_pos[src_node]) : -1;
+        f_idx[fbase + fslot[q]] = make_int4((ty0 + ly) * W + tx0 + lx, vref,
+                                            (ty0 + e / kTile) * W + tx0 + (e & (kTile - 1)),
+                                            (s_nz[l] ? kFinNz : 0) | (s_kind[l] == kKindOutlet ? kFinOutlet : 0));
+        f_map[fbase + fslot[q]] = node ? map_identity() : make_float4(s_A[l], s_B[l], s_dep[l], s_stn[l]);
+    }
+    if (threadIdx.x == 0) t_fcnt[t] = second_wave ? -1 : s_fn;
     const int j = threadIdx.x;
     bool ready = false;
     int32_t og = 0;
@@ -835,10 +909,8 @@ struct SedCoarse {
                     from = __fadd_rn(from, __fmul_rn(1.0f, map_apply(mp, v)));
                 }
                 const float sn = nz ? sed_mix(r.x, r.y, from) : r.x;
-                if (j < kProgLocal)
-                    vals[j] = sn;
-                else
-                    __stcg(p_val + nbase + j, sn);
+                if (j < kProgLocal) vals[j] = sn;
+                __stcg(p_val + nbase + j, sn);  // the final pass maps every node's value onto its chain
             }
             __syncwarp();
             i += run;
@@ -886,8 +958,38 @@ __global__ void __launch_bounds__(256, 6)
     k_sedt_final(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd, const float* __restrict__ ero,
                  const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
                  float* fines, float* soilT, const int32_t* __restrict__ t_pend, const uint8_t* __restrict__ t_stat,
-                 ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts) {
+                 const int4* __restrict__ f_idx, const float4* __restrict__ f_map, const float2* __restrict__ f_ds,
+                 const int32_t* __restrict__ t_fcnt, const float* __restrict__ p_val, ModelConsts k, DevScalars* sc,
+                 DemCtx dc, TileSet ts) {
     if (!sc->sed_tiled_ok) return;
+    const int t = ts.tile(blockIdx.x);
+    const int nf = t_fcnt[t];
+    if (nf >= 0) {
+        // every waiting cell is a program node or lies on a chain below one:
+        // its stone is the map of that node's value, once its outlet completed
+        const size_t fbase = (size_t)t * kTile * kTile;
+        int done = 0;
+        for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+            const int4 e = f_idx[fbase + i];
+            if (t_pend[e.z] != 0 || e.y < 0) continue;  // the outlet's program never ran
+            ++done;
+            if (e.w & kFinOutlet) continue;
+            const float2 ds = f_ds[fbase + i];
+            depo[e.x] = ds.x;
+            soilT[e.x] = ds.y;
+            if (e.w & kFinNz) {
+                const float sn = map_apply(f_map[fbase + i], __ldcg(p_val + e.y));
+                __stcg(stone + e.x, sn);
+                fines[e.x] = __fsub_rn(100.0f, sn);
+            }
+        }
+        if (nf > 0) {
+            done = wsum(done);
+            const int dem = dem_at(dc, (size_t)f_idx[fbase].x);
+            if ((threadIdx.x & 31) == 0 && done && dem >= 0) atomicAdd(&dc.out[dem].sed_done, done);
+        }
+        return;
+    }
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
     __shared__ uint8_t s_hok[kTH * kTH];
@@ -902,7 +1004,6 @@ __global__ void __launch_bounds__(256, 6)
     __shared__ int16_t s_q[kTile * kTile];
     __shared__ int s_done, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
-    const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
     sed_tile_load(mask, fd, W, H, tx0, ty0, s_code, s_cls);
     if (threadIdx.x < kRing) {
@@ -1210,8 +1311,8 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flag
     if (tiled) {
         const int tiles = ts.n;
         LEM_LAUNCH(L, k_sedt_local, tiles, 256, s.mask, s.fd, s.ero, s.inci, s.geli, s.depo, s.stone, s.fines,
-                   s.soilT, s.t_dst, s.t_pend, s.t_orng, s.t_la, s.p_abc, s.p_ref, s.p_map, s.t_stat, s.list_b, k,
-                   s.sc, s.dems, ts);
+                   s.soilT, s.t_dst, s.t_pend, s.t_orng, s.t_la, s.p_abc, s.p_ref, s.p_map, s.t_stat, s.f_idx,
+                   s.f_map, s.f_ds, s.t_fcnt, s.list_b, k, s.sc, s.dems, ts);
         const uint8_t* fd = s.fd;
         const int32_t* torng = s.t_orng;
         const int32_t* tdst = s.t_dst;
@@ -1236,7 +1337,8 @@ lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flag
         LEM_CUDA_TRY(coop_launch((const void*)k_sedt_coarse, s.coop_blocks[kCkSedCoarse], args, L.st));
         L.post();
         LEM_LAUNCH(L, k_sedt_final, tiles, 256, s.mask, s.fd, s.ero, s.inci, s.geli, s.depo, s.stone, s.fines,
-                   s.soilT, s.t_pend, s.t_stat, k, s.sc, s.dems, ts);
+                   s.soilT, s.t_pend, s.t_stat, s.f_idx, s.f_map, s.f_ds, s.t_fcnt, s.p_val, k, s.sc, s.dems,
+                   ts);
     }
     {
         const uint8_t* mask = s.mask;
