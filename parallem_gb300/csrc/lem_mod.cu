@@ -602,20 +602,12 @@ __global__ void __launch_bounds__(256, 5)
             t_dst[g] = s_kind[e] == kKindOutlet ? (int32_t)((ty0 + e / kTile) * W + tx0 + (e & (kTile - 1))) : -1;
         }
         stray |= s_flag[l] == (kFDone | kFTaint) && s_kind[s_ptr[l]] != kKindOutlet;
+        if (tx0 + lx < W && ty0 + ly < H) t_stat[g] = (s_flag[l] & kFDone) ? ((s_flag[l] & kFTaint) ? 2 : 1) : 0;
     }
-    // Such a tile keeps the second wave for its waiting cells (it needs their
-    // status); in every other tile each waiting cell's stone is a map of one
-    // program node's value, stored by the final pass.
+    // Such a tile keeps the second wave for its waiting cells; in every other
+    // tile each waiting cell's stone is a map of one program node's value,
+    // stored by the final pass.
     const bool second_wave = __syncthreads_or(stray);
-    if (second_wave) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int ly = ly0 + 8 * q, l = ly * kTile + lx;
-            if (tx0 + lx < W && ty0 + ly < H)
-                t_stat[(size_t)(ty0 + ly) * W + tx0 + lx] =
-                    (s_flag[l] & kFDone) ? ((s_flag[l] & kFTaint) ? 2 : 1) : 0;
-        }
-    }
     list_outlets(s_kind, s_olist, s_oslot, &s_no, s_wcnt);
     __syncthreads();
     // inflows per outlet (ring cells flowing into the tile)
@@ -964,14 +956,19 @@ __global__ void __launch_bounds__(256, 6)
     if (!sc->sed_tiled_ok) return;
     const int t = ts.tile(blockIdx.x);
     const int nf = t_fcnt[t];
-    if (nf >= 0) {
+    const size_t fbase = (size_t)t * kTile * kTile;
+    bool stalled = false;  // an outlet whose program never ran (a donor upstream never completes)
+    if (nf >= 0)
+        for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+            const int4 e = f_idx[fbase + i];
+            stalled |= t_pend[e.z] != 0 || e.y < 0;
+        }
+    if (nf >= 0 && !__syncthreads_or(stalled)) {
         // every waiting cell is a program node or lies on a chain below one:
-        // its stone is the map of that node's value, once its outlet completed
-        const size_t fbase = (size_t)t * kTile * kTile;
+        // its stone is the map of that node's value
         int done = 0;
         for (int i = threadIdx.x; i < nf; i += blockDim.x) {
             const int4 e = f_idx[fbase + i];
-            if (t_pend[e.z] != 0 || e.y < 0) continue;  // the outlet's program never ran
             ++done;
             if (e.w & kFinOutlet) continue;
             const float2 ds = f_ds[fbase + i];
