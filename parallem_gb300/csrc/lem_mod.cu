@@ -67,7 +67,7 @@ __device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v
     return m;
 }
 
-__global__ void __launch_bounds__(256, 6)
+__global__ void __launch_bounds__(256, 4)
     k_erosion(const double* __restrict__ z, const double* __restrict__ z_init, const uint8_t* __restrict__ mask,
               const float* __restrict__ slopes, const float2* __restrict__ fa, const float* __restrict__ fines,
               const float* __restrict__ nut, const float* __restrict__ soilT, const float* __restrict__ stone,
@@ -102,13 +102,14 @@ __global__ void __launch_bounds__(256, 6)
         // A multi-direction code among the routed cells (not row 0 / column 0,
         // mfd_accum.cu:42) sends the step's sediment routing to the walk.
         depo[i] = 0.00001f;
-        if (x != 0 && y != 0) {
-            const uint8_t code = fd[i];
-            multi |= (code & (code - 1)) != 0;
-        }
-        // aveslope (eroincidep.cu:8-37): mean of the positive entries
+        // every input of the cell in one batch of loads, ahead of the arithmetic
+        const uint8_t code = fd[i];
         const float4 a = reinterpret_cast<const float4*>(slopes)[2 * i];
         const float4 b = reinterpret_cast<const float4*>(slopes)[2 * i + 1];
+        const float st = soilT[i], tb = totB[i], fi = fines[i], nu = nut[i], sto = stone[i];
+        float T = clim_temp(c, z, z_init, i, outlet, outlet_z);
+        if (x != 0 && y != 0) multi |= (code & (code - 1)) != 0;
+        // aveslope (eroincidep.cu:8-37): mean of the positive entries
         const float sv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
         float total = 0.f;
         int nonzero = 0;
@@ -120,17 +121,16 @@ __global__ void __launch_bounds__(256, 6)
         const float sp = (total > 0.f && nonzero > 0) ? total / (float)nonzero : 0.f;
         slopeptr[i] = sp;
         const float fav = f2.x + f2.y;
-        const float st = soilT[i];
-        const float veg = expf(-0.07f * totB[i] / 76.5f);
+        const float veg = expf(-0.07f * tb / 76.5f);
         // diff_erosion (eroincidep.cu:39-87)
-        float erod = (2.77e-6f * powf(fines[i], 1.14f) * (12.0f - nut[i])) + k.erod_const;
+        float erod = (2.77e-6f * powf(fi, 1.14f) * (12.0f - nu)) + k.erod_const;
         if (erod < 0.f) erod = 0.f;
         float OF = (fav * 1000.0f) / 25.0f;
         if (OF > k.q_threshold) OF = k.q_threshold;
         float slope = sp;
         if (slope == 0.f) slope = 0.0001f;
         if (slope > 5.0f) slope = 5.0f;
-        float e = ((erod * OF * OF * powf(slope, 1.67f) * (powf(110.0f - stone[i], 0.877f) / 61.7023f))) * veg;
+        float e = ((erod * OF * OF * powf(slope, 1.67f) * (powf(110.0f - sto, 0.877f) / 61.7023f))) * veg;
         if (e > st) e = st;
         // conc_erosion (eroincidep.cu:89-152)
         float cslope = sp;
@@ -155,7 +155,6 @@ __global__ void __launch_bounds__(256, 6)
         // gelifluction (eroincidep.cu:154-198).  The quartic kappa(T) cancels near
         // its roots (T ~ -16.8 and 8.6 C) and the range test has edges at -20 and 8.87 C:
         // there the temperature and kappa take the reference's fp64 arithmetic.
-        float T = clim_temp(c, z, z_init, i, outlet, outlet_z);
         float kappa = k.kappa;
         if (T >= -20.f && T <= 8.87f)
             kappa = 0.15711f - 0.011835f * T - 0.001195f * T * T + 0.000038f * T * T * T + 0.000002f * T * T * T * T;
@@ -1138,7 +1137,8 @@ __global__ void __launch_bounds__(256, 4)
     for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
         int x, y;
         const size_t i = region_cell(c, ri, W, &x, &y);
-        sd += depo[i];
+        const float dp = depo[i];
+        sd += dp;
         if (!mask[i]) {
             totB[i] = 0.0f;  // grow_vegetation (updates.cu:102-105)
             if (dz_out) {
@@ -1148,21 +1148,23 @@ __global__ void __launch_bounds__(256, 4)
             }
             continue;
         }
-        const float e = ero[i];
-        const float dz = depo[i] - e - inci[i] - geli[i];  // surface_change (eroincidep.cu:404)
-        const double zold = z[i];
-        const double zc = c.from_current_dem ? (((int)i == outlet) ? outlet_z : zold) : z_init[i];
+        // every input of the cell in one batch of loads, ahead of the arithmetic
+        const float e = ero[i], ic = inci[i], gl = geli[i];
+        const double zold = z[i], z0 = z_init[i];
+        const float2 f2 = fa[i];
+        const float st0 = soilT[i], sn0 = stone[i], sm0 = soilM[i], tb = totB[i], sb0 = soilB[i];
+        const float dz = dp - e - ic - gl;  // surface_change (eroincidep.cu:404)
+        const double zc = c.from_current_dem ? (((int)i == outlet) ? outlet_z : zold) : z0;
         float zch, zcl;
         dsplit(zc, zch, zcl);
         const float T = (float)c.temp - ((zch - (float)kMinHeight) + zcl) * 0.0065f;
         const float rain = rain0 + (float)(y - c.y0) * rinc;
-        const float2 f2 = fa[i];
         const float fav = f2.x + f2.y;
         // weathering type 1 (eroincidep.cu:220-327)
         const float PE = 1.44f * (T + 6.0f) * (T + 6.0f);
         const float surface_flow = fav * 1000.0f;
         const float evap_trans = (rain + surface_flow <= PE) ? rain + surface_flow : rain + surface_flow - PE;
-        float st = soilT[i];
+        float st = st0;
         const float lpco2 = (st > 0.1f ? -2.5f : -3.5f) + ((T - 15.0f) / 10.0f);
         const float Ca2eq = exp10f((lpco2 + dreybrodt(tab, T)) * (1.0f / 3.0f));
         float wC = 0.0148148148f * Ca2eq * (surface_flow / k.rescale_weather);
@@ -1170,7 +1172,7 @@ __global__ void __launch_bounds__(256, 4)
         if (wC > 0.001f) wC = 0.001f;
         const float wP = 7.7e-5f * expf(-2.3f * st);
         st = st + wC * 0.02f + wP;
-        float sn = stone[i], sm = soilM[i];
+        float sn = sn0, sm = sm0;
         if (st <= 0.0f) {
             st = 0.0f;
             sn = 0.0f;
@@ -1205,12 +1207,10 @@ __global__ void __launch_bounds__(256, 4)
         }
         z[i] = zn;
         // update_nutrient_content (updates.cu:48-76)
-        const float tb = totB[i];
-        float nu = nut[i];
-        if (st <= 0.0f) nu = 0.0f;
+        float nu;
         const float leaf_fall = tb / (72.8f * logf(tb + 1.4f));
-        const float decomposition = soilB[i] * expf(0.12f * T - 5.75f);
-        const float sb = soilB[i] + leaf_fall - decomposition;
+        const float decomposition = sb0 * expf(0.12f * T - 5.75f);
+        const float sb = sb0 + leaf_fall - decomposition;
         soilB[i] = sb;
         if (st == 0.0f && sb > 0.0f)
             nu = 100.0f;
@@ -1225,7 +1225,6 @@ __global__ void __launch_bounds__(256, 4)
         // run-in both grids come from the same DEM and scalars, so it is 0.
         float dT = 0.0f;
         if (c.from_current_dem) {
-            const double z0 = z_init[i];
             float h1, l1, h0, l0;
             dsplit(zc, h1, l1);
             dsplit(z0, h0, l0);
