@@ -635,6 +635,7 @@ lem_status create_common(const lem_grid_desc* grid, const lem_params* params, in
         ALLOC(s.f_map, tiles * kTile * kTile);
         ALLOC(s.f_ds, tiles * kTile * kTile);
         ALLOC(s.t_fcnt, tiles);
+        ALLOC(s.n_meta, tiles * kTile * kTile);
     }
     ALLOC(s.t_stat, N);
     if (params->flow_direction_type != 0 && params->mfd_proportions) {

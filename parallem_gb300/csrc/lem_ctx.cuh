@@ -75,17 +75,20 @@ struct DevState {
     // programs (one per outlet, kTile*kTile slots per tile)
     float4* p_abc;      // node: stone mix coefficients A, B, the settled donors' sum C, inputs and flags
     int32_t* p_ref;     // per tile, kPool node inputs: the feeding node (program slot) or cell
+                        //   (the accumulation's program uses the same slots earlier in the step)
     float4* p_map;      // per tile, kPool node inputs: the map through the cells in between
     float* p_val;       // slot: the value of every program node once the coarse wave has run
     uint8_t* t_stat;    // cell: 1 settled inside its tile, 2 waits on another tile, 0 neither
                         //   (written for the tiles whose waiting cells are routed by a second wave)
-    // per tile, kTile*kTile slots: the waiting cells the final pass stores,
-    // each as its outlet, the program node that feeds it and the map from that
-    // node's value to its own stone
-    int4* f_idx;        // cell, p_val slot of the feeding node, outlet cell, flags
+    // per tile, kTile*kTile slots: the waiting cells the final pass stores.
+    // Sediment: each as its outlet, the program node that feeds it and the
+    // map from that node's value to its own stone.  Accumulation (earlier in
+    // the step, same slots): each as its node and its local accumulation.
+    int4* f_idx;        // cell, p_val slot of the feeding node, outlet cell, flags | cell, node, flags
     float4* f_map;      // clamp map: feeding node's value -> the cell's stone
-    float2* f_ds;       // the cell's deposition and new soil thickness
-    int32_t* t_fcnt;    // tile: number of such cells; -1: its waiting cells need the second wave
+    float2* f_ds;       // the cell's deposition and new soil thickness | its local accumulation
+    int32_t* t_fcnt;    // tile: number of such cells (accumulation: | nodes << 16); -1: the second wave
+    int32_t* n_meta;    // accumulation, per tile kTile*kTile nodes: first input in p_ref | count << 11
     // flooding tables
     unsigned long long* ekey;   // hash keys (label pair)
     unsigned long long* ewt;    // min boundary height key

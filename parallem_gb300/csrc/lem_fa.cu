@@ -22,6 +22,12 @@ namespace lem {
 
 namespace {
 
+// k_fat_local's cell status: finished inside the tile, and waiting on an
+// inflow from another tile somewhere upstream (its final value needs the
+// coarse wave)
+constexpr uint8_t kLaDone = 1, kLaWaits = 2;
+constexpr int kLaOutlet = 1;  // final-pass entry: an outlet (stored by the coarse wave; counted only)
+
 // calcrunoffweight (runoffweight.cu:21-58) plus the in-degrees of the wave.
 // A donor outside the catchment is complete from the start when its DEM is
 // nodata (correctmfdflow's okgrid, mfd_simple.cu:279-285) and never otherwise.
@@ -239,7 +245,9 @@ __global__ void __launch_bounds__(256)
     k_fat_local(const double* __restrict__ z, const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                 const float* __restrict__ w, float2* __restrict__ t_la, int32_t* __restrict__ t_dst,
                 int32_t* __restrict__ t_pend, int32_t* __restrict__ t_orng, int32_t* __restrict__ t_ent,
-                int32_t* srcs, ModelConsts k, DevScalars* sc, TileSet ts) {
+                float2* __restrict__ fa, int32_t* __restrict__ n_meta, int32_t* __restrict__ n_ref,
+                int4* __restrict__ f_idx, float2* __restrict__ f_la, int32_t* __restrict__ t_fcnt, int32_t* srcs,
+                ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts) {
     if (!sc->tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -255,12 +263,13 @@ __global__ void __launch_bounds__(256)
     __shared__ int32_t s_ocnt[kTileEnt];
     __shared__ int16_t s_ostart[kTileEnt];
     __shared__ int16_t s_ofill[kTileEnt];
-    __shared__ int s_no, s_qn, s_qend;
+    __shared__ int s_no, s_qn, s_qend, s_nn, s_fn, s_pool;
     __shared__ int s_wcnt[9];  // per-warp counts of the outlet list and the source append
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
     tile_load(z, mask, fd, W, H, tx0, ty0, s_code, s_cls);
+    if (threadIdx.x == 0) s_fn = s_pool = 0;
     __syncthreads();
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     bool src[4];  // chain starts, fixed before any chain runs (a chain may enter them later)
@@ -314,6 +323,7 @@ __global__ void __launch_bounds__(256)
         [&](int cur, int rnd) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             float2 acc = make_float2(0.f, 0.f);
+            bool taint = s_ext[cur] != 0;
 #pragma unroll
             for (int kk = 0; kk < 8; ++kk) {
                 const int d = scan_dir(kk);
@@ -322,10 +332,11 @@ __global__ void __launch_bounds__(256)
                 const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
                 if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
                 acc = ff_add(acc, s_la[nly * kTile + nlx]);
+                taint |= (s_done[nly * kTile + nlx] & kLaWaits) != 0;
             }
             if (acc.x < 0.0f) acc = make_float2(0.f, 0.f);
             s_la[cur] = ff_add(s_la[cur], acc);
-            s_done[cur] = 1;
+            s_done[cur] = taint ? (kLaDone | kLaWaits) : kLaDone;
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
         },
         s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
@@ -343,6 +354,7 @@ __global__ void __launch_bounds__(256)
         }
         if (!__syncthreads_or(ch)) break;  // every pointer is at its path's end
     }
+    bool stray = false;  // a waiting cell whose in-tile path ends inside the tile
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int ly = ly0 + 8 * q, l = ly * kTile + lx;
@@ -351,7 +363,11 @@ __global__ void __launch_bounds__(256)
             t_dst[(size_t)(ty0 + ly) * W + tx0 + lx] =
                 s_kind[e] == kKindOutlet ? (int32_t)((ty0 + e / kTile) * W + tx0 + (e & (kTile - 1))) : -1;
         }
+        stray |= s_done[l] == (kLaDone | kLaWaits) && s_kind[s_ptr[l]] != kKindOutlet;
     }
+    // Such a tile keeps the second wave; every other tile writes its settled
+    // cells here and leaves the final pass a program of nodes (see below).
+    const bool second_wave = __syncthreads_or(stray);
     // outlets in cell order (they lie on the border: at most 124)
     list_outlets(s_kind, s_olist, s_oslot, &s_no, s_wcnt);
     if (threadIdx.x < kTileEnt) s_ocnt[threadIdx.x] = 0;
@@ -420,6 +436,144 @@ __global__ void __launch_bounds__(256)
         ready = (opend == 0);
     }
     block_append(ready, og, srcs, &sc->tile_src, W * H, &sc->err, s_wcnt);
+    if (threadIdx.x == 0) t_fcnt[t] = -1;
+    if (second_wave) return;  // block-uniform
+
+    // The final pass's program.  A waiting cell's accumulation is its local
+    // one plus the inflows of every entry upstream of it.  That sum is the same
+    // along a run of single-input cells, so it is kept per node (an entry, a
+    // join of two waiting branches, or the outlet): the inflows the node takes
+    // from other tiles plus the sums of the nodes at the top of its waiting
+    // inputs.  s_nd: node index + 1 in the low half (0: not a node), the cell
+    // above in the high half (a cell between nodes: its waiting donor, then
+    // the node at the top of its run).
+    int32_t* s_nd = s_pend;  // the in-degrees are spent
+    int done = 0, dem = -1;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
+        const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
+        int32_t nd = 0;
+        if (s_cls[hc] == kCellIn) dem = max(dem, dem_at(dc, g));
+        if (s_done[l] == kLaDone) {
+            if (s_kind[l] != kKindOutlet) {  // the coarse wave stores the outlets
+                fa[g] = s_la[l];
+                ++done;
+            }
+        } else if (s_done[l] == (kLaDone | kLaWaits)) {
+            int ntd = 0, up = l;
+#pragma unroll
+            for (int d = 0; d < 8; ++d) {
+                const int nlx = lx + dir_dx(d), nly = ly + dir_dy(d);
+                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+                if (in_tile(nlx, nly) && donates(s_code[nh], d) && s_cls[nh] == kCellIn &&
+                    (s_done[nly * kTile + nlx] & kLaWaits)) {
+                    ++ntd;
+                    up = nly * kTile + nlx;
+                }
+            }
+            nd = (s_ext[l] != 0 || ntd >= 2 || s_kind[l] == kKindOutlet) ? 1 : (up << 16);
+        }
+        s_nd[l] = nd;
+    }
+    done = wsum(done);
+    dem = __reduce_max_sync(0xffffffffu, dem);  // one DEM per tile
+    if ((threadIdx.x & 31) == 0 && done && dem >= 0) atomicAdd(&dc.out[dem].fa_done, done);
+    __syncthreads();
+    // pointer jumping: every cell between nodes finds the node at the top of its run
+    for (int it = 0; it < 10; ++it) {  // in-tile runs are shorter than 2^10 cells
+        int32_t nu[4];
+        bool ch = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int l = (ly0 + 8 * q) * kTile + lx;
+            nu[q] = -1;
+            const int32_t v = s_nd[l];
+            if (s_done[l] != (kLaDone | kLaWaits) || (v & 0xffff)) continue;
+            const int32_t vp = s_nd[v >> 16];
+            if (vp & 0xffff) continue;  // at the top
+            nu[q] = vp & ~0xffff;
+            ch = true;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (nu[q] >= 0) s_nd[(ly0 + 8 * q) * kTile + lx] = nu[q];
+        if (!__syncthreads_or(ch)) break;
+    }
+    // node indices in the order the wave reached the cells (inputs first)
+    if (threadIdx.x < 32) {
+        const unsigned below = (1u << lx) - 1u;
+        const int qn = s_qn;
+        int base = 0;
+        for (int i0 = 0; i0 < qn; i0 += 32) {
+            const int i = i0 + lx;
+            int c = 0;
+            bool isn = false;
+            if (i < qn) {
+                c = s_q[i];
+                isn = s_done[c] == (kLaDone | kLaWaits) && (s_nd[c] & 0xffff);
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, isn);
+            if (isn) s_nd[c] = base + __popc(b & below) + 1;
+            base += __popc(b);
+        }
+        if (lx == 0) s_nn = base;
+    }
+    __syncthreads();
+    const size_t tb = (size_t)t * kTile * kTile, pool = (size_t)t * kTilePool;
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
+        const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
+        const int32_t v = s_nd[l];
+        if (s_kind[l] == kKindOutlet) {  // counted once the coarse wave stored it
+            f_idx[tb + atomicAdd(&s_fn, 1)] = make_int4((int)g, 0, kLaOutlet, 0);
+            if (s_done[l] != (kLaDone | kLaWaits)) continue;
+        } else if (s_done[l] == (kLaDone | kLaWaits)) {
+            const int node = (v & 0xffff) ? (v & 0xffff) - 1 : (s_nd[v >> 16] & 0xffff) - 1;
+            const int e = atomicAdd(&s_fn, 1);
+            f_idx[tb + e] = make_int4((int)g, node, 0, 0);
+            f_la[tb + e] = s_la[l];
+        }
+        if (s_done[l] != (kLaDone | kLaWaits) || !(v & 0xffff)) continue;
+        // the node's inputs, in the donors' scan order: cells of other tiles, then node indices (negated)
+        int nin = 0;
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+            const int nlx = lx + dir_dx(d), nly = ly + dir_dy(d);
+            const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+            if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
+            if (!in_tile(nlx, nly) || (s_done[nly * kTile + nlx] & kLaWaits)) ++nin;
+        }
+        const int start = atomicAdd(&s_pool, nin);
+        if (start + nin > kTilePool) {
+            atomicOr(&sc->err, ErrFlags::kCapacity);
+            continue;
+        }
+        int m = 0;
+#pragma unroll 1
+        for (int kk = 0; kk < 8; ++kk) {
+            const int d = scan_dir(kk);
+            const int nlx = lx + dir_dx(d), nly = ly + dir_dy(d);
+            const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+            if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
+            int32_t ref;
+            if (!in_tile(nlx, nly)) {
+                ref = (ty0 + nly) * W + tx0 + nlx;
+            } else {
+                const int u = nly * kTile + nlx;
+                if (!(s_done[u] & kLaWaits)) continue;
+                const int32_t vu = s_nd[u];
+                ref = -((vu & 0xffff) ? (vu & 0xffff) : (s_nd[vu >> 16] & 0xffff));
+            }
+            n_ref[pool + start + m] = ref;
+            ++m;
+        }
+        n_meta[tb + (v & 0xffff) - 1] = start | (m << 11);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) t_fcnt[t] = (s_nn << 16) | s_fn;
 }
 
 // One outlet of the coarse wave.
@@ -469,8 +623,10 @@ __global__ void k_fat_coarse(const uint8_t* __restrict__ mask, const uint8_t* __
 
 __global__ void __launch_bounds__(256)
     k_fat_final(const double* __restrict__ z, const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
-                const float* __restrict__ w, const int32_t* __restrict__ t_pend, float2* fa, ModelConsts k,
-                DevScalars* sc, DemCtx dc, TileSet ts) {
+                const float* __restrict__ w, const int32_t* __restrict__ t_pend, float2* fa,
+                const int32_t* __restrict__ n_meta, const int32_t* __restrict__ n_ref, const int4* __restrict__ f_idx,
+                const float2* __restrict__ f_la, const int32_t* __restrict__ t_fcnt, ModelConsts k, DevScalars* sc,
+                DemCtx dc, TileSet ts) {
     if (!sc->tiled_ok) return;
     __shared__ uint8_t s_code[kTH * kTH];
     __shared__ uint8_t s_cls[kTH * kTH];
@@ -482,6 +638,81 @@ __global__ void __launch_bounds__(256)
     __shared__ int s_done, s_dem, s_qn, s_qend;
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = ts.tile(blockIdx.x);
+    const int fc = t_fcnt[t];
+    if (fc >= 0) {
+        // The tile's program: each node's sum of inflows, then every waiting
+        // cell's local accumulation plus the sum of its node.  A node is valid
+        // when every inflow upstream completed.
+        const int ne = fc & 0xffff, nn = fc >> 16;
+        const size_t tb = (size_t)t * kTile * kTile, pool = (size_t)t * kTilePool;
+        float2* s_X = s_val;      // node sums
+        int32_t* s_ok = s_pend;  // node valid
+        for (int n = threadIdx.x; n < nn; n += blockDim.x) {
+            const int meta = n_meta[tb + n];
+            const int start = meta & 2047, nin = meta >> 11;
+            float2 acc = make_float2(0.f, 0.f);
+            int ok = 1;
+            for (int j = 0; j < nin; ++j) {
+                const int32_t ref = n_ref[pool + start + j];
+                if (ref < 0) continue;
+                acc = ff_add(acc, __ldcg(fa + ref));
+                ok &= t_pend[ref] == 0;
+            }
+            s_X[n] = acc;
+            s_ok[n] = ok;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            // in index order (a node's inputs have smaller indices), a run of
+            // nodes with no input inside the run at a time
+            const int lane = threadIdx.x;
+            for (int i = 0; i < nn;) {
+                const int n = i + lane;
+                int meta = 0;
+                bool dep = false;
+                if (n < nn) {
+                    meta = n_meta[tb + n];
+                    for (int j = 0; j < (meta >> 11); ++j) {
+                        const int32_t ref = n_ref[pool + (meta & 2047) + j];
+                        if (ref < 0 && -ref - 1 >= i) dep = true;
+                    }
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, dep);
+                const int run = b ? __ffs(b) - 1 : 32;  // lane 0's inputs all lie before i
+                if (lane < run && n < nn) {
+                    float2 acc = s_X[n];
+                    int ok = s_ok[n];
+                    for (int j = 0; j < (meta >> 11); ++j) {
+                        const int32_t ref = n_ref[pool + (meta & 2047) + j];
+                        if (ref >= 0) continue;
+                        acc = ff_add(acc, s_X[-ref - 1]);
+                        ok &= s_ok[-ref - 1];
+                    }
+                    s_X[n] = acc;
+                    s_ok[n] = ok;
+                }
+                __syncwarp();
+                i += run;
+            }
+        }
+        __syncthreads();
+        int done = 0, dem = -1;
+        for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+            const int4 id = f_idx[tb + e];
+            dem = dem_at(dc, (size_t)id.x);
+            if (id.z & kLaOutlet) {
+                done += t_pend[id.x] == 0;
+                continue;
+            }
+            if (!s_ok[id.y]) continue;
+            fa[id.x] = ff_add(f_la[tb + e], s_X[id.y]);
+            ++done;
+        }
+        done = wsum(done);
+        dem = __reduce_max_sync(0xffffffffu, dem);
+        if ((threadIdx.x & 31) == 0 && done && dem >= 0) atomicAdd(&dc.out[dem].fa_done, done);
+        return;
+    }
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
     tile_load(z, mask, fd, W, H, tx0, ty0, s_code, s_cls);
     // donors in other tiles: outlets of their tiles, final after the coarse wave
@@ -648,7 +879,7 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, uin
         const TileSet ts = tiles_of(s, k.W);
         const int tiles = ts.n;
         LEM_LAUNCH(L, k_fat_local, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_la, s.t_dst, s.t_pend, s.t_orng, s.t_ent,
-                   s.list_b, k, s.sc, ts);
+                   s.fa, s.n_meta, s.p_ref, s.f_idx, s.f_ds, s.t_fcnt, s.list_b, k, s.sc, s.dems, ts);
         const uint8_t* mask = s.mask;
         const uint8_t* fd = s.fd;
         const float2* tla = s.t_la;
@@ -666,7 +897,8 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, uin
         L.pre("k_fat_coarse");
         LEM_CUDA_TRY(coop_launch((const void*)k_fat_coarse, s.coop_blocks[kCkFatCoarse], args, L.st));
         L.post();
-        LEM_LAUNCH(L, k_fat_final, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_pend, s.fa, k, s.sc, s.dems, ts);
+        LEM_LAUNCH(L, k_fat_final, tiles, 256, s.z, s.mask, s.fd, s.w, s.t_pend, s.fa, s.n_meta, s.p_ref, s.f_idx,
+                   s.f_ds, s.t_fcnt, k, s.sc, s.dems, ts);
     }
     {
         const uint8_t* mask = s.mask;
