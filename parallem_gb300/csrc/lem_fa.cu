@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(256)
         const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
         const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
         int32_t nd = 0;
-        if (s_cls[hc] == kCellIn) dem = max(dem, dem_at(dc, g));
+        if (dem < 0 && s_cls[hc] == kCellIn) dem = dem_at(dc, g);
         if (s_done[l] == kLaDone) {
             if (s_kind[l] != kKindOutlet) {  // the coarse wave stores the outlets
                 fa[g] = s_la[l];
@@ -501,24 +501,34 @@ __global__ void __launch_bounds__(256)
             if (nu[q] >= 0) s_nd[(ly0 + 8 * q) * kTile + lx] = nu[q];
         if (!__syncthreads_or(ch)) break;
     }
-    // node indices in the order the wave reached the cells (inputs first)
-    if (threadIdx.x < 32) {
+    // node indices in the order the wave reached the cells (inputs first):
+    // warp w numbers the nodes among queue entries 128 w .. 128 w + 127
+    {
+        const int qn = s_qn, wq = threadIdx.x >> 5;
         const unsigned below = (1u << lx) - 1u;
-        const int qn = s_qn;
-        int base = 0;
-        for (int i0 = 0; i0 < qn; i0 += 32) {
-            const int i = i0 + lx;
-            int c = 0;
+        unsigned b[4];
+        int cnt = 0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int i = wq * 128 + r * 32 + lx;
             bool isn = false;
             if (i < qn) {
-                c = s_q[i];
+                const int c = s_q[i];
                 isn = s_done[c] == (kLaDone | kLaWaits) && (s_nd[c] & 0xffff);
             }
-            const unsigned b = __ballot_sync(0xffffffffu, isn);
-            if (isn) s_nd[c] = base + __popc(b & below) + 1;
-            base += __popc(b);
+            b[r] = __ballot_sync(0xffffffffu, isn);
+            cnt += __popc(b[r]);
         }
-        if (lx == 0) s_nn = base;
+        if (lx == 0) s_wcnt[wq] = cnt;
+        __syncthreads();
+        int base = 0;
+        for (int i = 0; i < wq; ++i) base += s_wcnt[i];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            if ((b[r] >> lx) & 1u) s_nd[s_q[wq * 128 + r * 32 + lx]] = base + __popc(b[r] & below) + 1;
+            base += __popc(b[r]);
+        }
+        if (threadIdx.x == 255) s_nn = base;  // the last warp's end is the total
     }
     __syncthreads();
     const size_t tb = (size_t)t * kTile * kTile, pool = (size_t)t * kTilePool;
@@ -527,16 +537,16 @@ __global__ void __launch_bounds__(256)
         const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
         const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
         const int32_t v = s_nd[l];
-        if (s_kind[l] == kKindOutlet) {  // counted once the coarse wave stored it
-            f_idx[tb + atomicAdd(&s_fn, 1)] = make_int4((int)g, 0, kLaOutlet, 0);
-            if (s_done[l] != (kLaDone | kLaWaits)) continue;
-        } else if (s_done[l] == (kLaDone | kLaWaits)) {
+        const bool waits = s_done[l] == (kLaDone | kLaWaits), outlet = s_kind[l] == kKindOutlet;
+        const int e = warp_slot(waits || outlet, &s_fn);
+        if (outlet) {  // counted once the coarse wave stored it
+            f_idx[tb + e] = make_int4((int)g, 0, kLaOutlet, 0);
+        } else if (waits) {
             const int node = (v & 0xffff) ? (v & 0xffff) - 1 : (s_nd[v >> 16] & 0xffff) - 1;
-            const int e = atomicAdd(&s_fn, 1);
             f_idx[tb + e] = make_int4((int)g, node, 0, 0);
             f_la[tb + e] = s_la[l];
         }
-        if (s_done[l] != (kLaDone | kLaWaits) || !(v & 0xffff)) continue;
+        if (!waits || !(v & 0xffff)) continue;
         // the node's inputs, in the donors' scan order: cells of other tiles, then node indices (negated)
         int nin = 0;
 #pragma unroll

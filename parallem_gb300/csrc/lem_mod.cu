@@ -661,12 +661,10 @@ __global__ void __launch_bounds__(256, 5)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
-        fslot[q] = -1;
-        if (s_flag[l] != (kFDone | kFTaint) || s_kind[s_ptr[l]] != kKindOutlet) continue;
-        if (!second_wave) {
-            fslot[q] = atomicAdd(&s_fn, 1);
-            f_ds[fbase + fslot[q]] = make_float2(s_dep[l], s_stn[l]);
-        }
+        const bool waits = s_flag[l] == (kFDone | kFTaint) && s_kind[s_ptr[l]] == kKindOutlet;
+        fslot[q] = warp_slot(waits && !second_wave, &s_fn);
+        if (!waits) continue;
+        if (fslot[q] >= 0) f_ds[fbase + fslot[q]] = make_float2(s_dep[l], s_stn[l]);
         if (s_node[l]) continue;
         float Cc = 0.f;
         int up = l;
