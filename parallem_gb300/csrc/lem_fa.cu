@@ -323,7 +323,6 @@ __global__ void __launch_bounds__(256)
         [&](int cur, int rnd) {
             const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
             float2 acc = make_float2(0.f, 0.f);
-            bool taint = s_ext[cur] != 0;
 #pragma unroll
             for (int kk = 0; kk < 8; ++kk) {
                 const int d = scan_dir(kk);
@@ -332,14 +331,28 @@ __global__ void __launch_bounds__(256)
                 const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
                 if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
                 acc = ff_add(acc, s_la[nly * kTile + nlx]);
-                taint |= (s_done[nly * kTile + nlx] & kLaWaits) != 0;
             }
             if (acc.x < 0.0f) acc = make_float2(0.f, 0.f);
             s_la[cur] = ff_add(s_la[cur], acc);
-            s_done[cur] = taint ? (kLaDone | kLaWaits) : kLaDone;
+            s_done[cur] = kLaDone;
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
         },
         s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
+    // The waiting cells: every finished cell downstream of an entry (a cell
+    // with a donor in another tile), marked along each entry's in-tile path.
+    // A walk stops where another walk has passed (it carries on from there).
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        int c = (ly0 + 8 * q) * kTile + lx;
+        if (!s_ext[c]) continue;
+        for (int guard = 0; guard < kTile * kTile; ++guard) {
+            if (s_done[c] != kLaDone) break;  // not finished, or marked already
+            s_done[c] = kLaDone | kLaWaits;
+            if (s_kind[c] != kKindIn) break;
+            c = s_ptr[c];
+        }
+    }
+    __syncthreads();
     // the end of every in-tile path: pointer jumping (paths are shorter than 2^10 cells)
     for (int it = 0; it < 10; ++it) {  // in-tile paths are shorter than 2^10 cells
         bool ch = false;
@@ -428,7 +441,7 @@ __global__ void __launch_bounds__(256)
     int32_t og = 0;
     if (j < no) {
         const int o = s_olist[j];
-        const int32_t opend = (s_done[o] ? 0 : kBlocked) + s_ocnt[j];
+        const int32_t opend = ((s_done[o] & kLaDone) ? 0 : kBlocked) + s_ocnt[j];
         og = (ty0 + o / kTile) * W + tx0 + (o & (kTile - 1));
         t_orng[og] = ((int)s_ostart[j] << 16) | s_ocnt[j];
         t_pend[og] = opend;
