@@ -536,29 +536,40 @@ __global__ void __launch_bounds__(256, 5)
         s_pos[l] = -1;
     }
     __syncthreads();
+    // The waiting cells: every cell downstream of an entry (a cell with a donor
+    // in another tile), marked along each entry's in-tile path before the wave.
+    // A walk stops where another walk has passed (it carries on from there).
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        int c = (ly0 + 8 * q) * kTile + lx;
+        if (!s_ext[c]) continue;
+        for (int guard = 0; guard < kTile * kTile; ++guard) {
+            if (s_flag[c] & kFTaint) break;
+            s_flag[c] = kFTaint;
+            if (s_kind[c] != kKindIn) break;
+            c = s_ptr[c];
+        }
+    }
     // settle what depends on this tile only; order the waiting cells
     int done = 0;
     if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
     tile_wave(
         [&](int cur, int rnd) {
-            const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
-            bool taint = s_ext[cur] != 0;
-            float from = 0.f;
-#pragma unroll
-            for (int kk = 0; kk < 8; ++kk) {
-                const int d = scan_dir(kk);
-                const int nlx = cx + dir_dx(d), nly = cy + dir_dy(d);
-                if (!in_tile(nlx, nly)) continue;
-                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
-                if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
-                const int n = nly * kTile + nlx;
-                if (s_flag[n] & kFTaint)
-                    taint = true;
-                else
-                    from = __fadd_rn(from, __fmul_rn(1.0f, s_new[n]));
-            }
+            const bool taint = (s_flag[cur] & kFTaint) != 0;
             if (!taint) {
+                // every donor is inside the tile and settled
+                const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
+                float from = 0.f;
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk) {
+                    const int d = scan_dir(kk);
+                    const int nlx = cx + dir_dx(d), nly = cy + dir_dy(d);
+                    if (!in_tile(nlx, nly)) continue;
+                    const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+                    if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
+                    from = __fadd_rn(from, __fmul_rn(1.0f, s_new[nly * kTile + nlx]));
+                }
                 SedLocal L;
                 L.dep = s_dep[cur];
                 L.A = s_A[cur];
