@@ -357,7 +357,7 @@ constexpr int kProgLocal = 256;  // program nodes the coarse evaluator keeps in 
 constexpr int kFinNz = 1;      // final-pass slot: the cell's sediment column is not empty
 constexpr int kFinOutlet = 2;  // final-pass slot: an outlet (the coarse wave stored it; counted only)
 constexpr int kPool = kTilePool;
-constexpr uint8_t kFDone = 1, kFTaint = 2, kFBlock = 4;
+constexpr uint8_t kFDone = 1, kFTaint = 2;
 
 // Maps of a value through a run of single-input cells: v -> clamp(a*v + b, lo, hi)
 // as float4(a, b, lo, hi); lo > hi encodes the constant b (a cell whose
@@ -475,6 +475,7 @@ __global__ void __launch_bounds__(256, 5)
     __shared__ int32_t s_ocnt[kTileEnt];
     __shared__ int32_t s_pcnt[kTileEnt];
     __shared__ int16_t s_pstart[kTileEnt];
+    __shared__ int16_t s_pfill[kTileEnt];
     __shared__ int16_t s_q[kTile * kTile];
     __shared__ int16_t s_rnd[kTile * kTile];
     __shared__ int s_no, s_nt, s_done, s_pool, s_dem, s_qn, s_qend, s_fn;
@@ -533,7 +534,6 @@ __global__ void __launch_bounds__(256, 5)
         s_nz[l] = nz;
         s_flag[l] = 0;
         s_pos[l] = -1;
-        s_rnd[l] = kind == kKindIn ? 1 : 0;  // cells to the end of the in-tile path, once the pointers have jumped
     }
     __syncthreads();
     // The waiting cells: every cell downstream of an entry (a cell with a donor
@@ -550,30 +550,14 @@ __global__ void __launch_bounds__(256, 5)
             c = s_ptr[c];
         }
     }
-    __syncthreads();
-    // and every cell below a donor that never finishes (outside the catchment)
-#pragma unroll 1
-    for (int q = 0; q < 4; ++q) {
-        const int ly = ly0 + 8 * q;
-        int c = ly * kTile + lx;
-        if (s_cls[(ly + 1) * kTH + lx + 1] != kCellIn || !(s_pend[c] & kBlocked)) continue;
-        for (int guard = 0; guard < kTile * kTile; ++guard) {
-            if (s_flag[c] & kFBlock) break;
-            s_flag[c] |= kFBlock;
-            if (s_kind[c] != kKindIn) break;
-            c = s_ptr[c];
-        }
-    }
-    // settle what depends on this tile only: the wave runs through the other
-    // cells alone, so its rounds follow the depth of their forest
+    // settle what depends on this tile only; order the waiting cells
     int done = 0;
     if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 4; ++q) src[q] = src[q] && !(s_flag[(ly0 + 8 * q) * kTile + lx] & kFTaint);
     tile_wave(
         [&](int cur, int rnd) {
-            {
+            const bool taint = (s_flag[cur] & kFTaint) != 0;
+            if (!taint) {
                 // every donor is inside the tile and settled
                 const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
                 float from = 0.f;
@@ -597,40 +581,24 @@ __global__ void __launch_bounds__(256, 5)
                 sed_store((size_t)(ty0 + cy) * W + tx0 + cx, L, sn, depo, stone, fines, soilT);
                 s_flag[cur] = kFDone;
                 ++done;
+            } else {
+                s_flag[cur] = kFDone | kFTaint;
+                s_rnd[cur] = (int16_t)rnd;  // a level for the coarse evaluation: inputs come from earlier rounds
+                s_topo[atomicAdd(&s_nt, 1)] = (int16_t)cur;
             }
-            // a waiting receiver is not released: it is not part of this wave
-            return s_kind[cur] == kKindIn && !(s_flag[s_ptr[cur]] & kFTaint) ? (int)s_ptr[cur] : -1;
+            return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
         },
         s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
-    // a waiting cell is finished unless a donor that never finishes lies upstream
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int l = (ly0 + 8 * q) * kTile + lx;
-        if ((s_flag[l] & (kFTaint | kFBlock)) == kFTaint) s_flag[l] = kFDone | kFTaint;
-    }
-    // pointer jumping to the end of every in-tile path, summing the path
-    // lengths on the way (in rounds that read before they write)
-    for (int it = 0; it < 11; ++it) {  // in-tile paths are shorter than 2^10 cells
-        int16_t np[4], nd[4];
+    for (int it = 0; it < 10; ++it) {  // in-tile paths are shorter than 2^10 cells
         bool ch = false;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int l = (ly0 + 8 * q) * kTile + lx;
-            const int p = s_ptr[l], pp = s_ptr[p];
-            np[q] = -1;
-            if (pp != p) {
-                np[q] = (int16_t)pp;
-                nd[q] = (int16_t)(s_rnd[l] + s_rnd[p]);
+            const int16_t nx = s_ptr[s_ptr[l]];
+            if (nx != s_ptr[l]) {
+                s_ptr[l] = nx;
                 ch = true;
             }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            if (np[q] < 0) continue;
-            const int l = (ly0 + 8 * q) * kTile + lx;
-            s_ptr[l] = np[q];
-            s_rnd[l] = nd[q];
         }
         if (!__syncthreads_or(ch)) break;  // every pointer is at its path's end
     }
@@ -685,11 +653,7 @@ __global__ void __launch_bounds__(256, 5)
             }
             node = s_ext[l] != 0 || ntd >= 2 || s_kind[l] == kKindOutlet;
         }
-        // the node's sort key: its outlet, then the longest path first (a node's
-        // inputs lie further up), then the cell
-        s_node[l] = node ? (1 << 30) | ((int)s_oslot[s_ptr[l]] << 21) | ((1023 - s_rnd[l]) << 10) | l : 0;
-        const int slot = warp_slot(node, &s_nt);
-        if (node) s_topo[slot] = (int16_t)l;
+        s_node[l] = node;
     }
     __syncthreads();
 #pragma unroll
@@ -773,21 +737,31 @@ __global__ void __launch_bounds__(256, 5)
         int a = 0;
         for (int i = 0; i < no; ++i) {
             s_pstart[i] = (int16_t)a;
+            s_pfill[i] = (int16_t)a;
             a += s_pcnt[i];
         }
         s_pool = 0;
     }
     __syncthreads();
-    // node slots: grouped by outlet, each group in key order (a node's rank
-    // among all the tile's nodes; the groups follow the outlets' order)
-#pragma unroll 1
-    for (int q = 0; q < 4; ++q) {
-        const int l = (ly0 + 8 * q) * kTile + lx;
-        const int key = s_node[l];
-        if (!key) continue;
-        int rank = 0;
-        for (int i = 0; i < nt; ++i) rank += s_node[s_topo[i]] < key;
-        s_pos[l] = (int16_t)rank;
+    // node slots: grouped by outlet, in the order the cells were reached
+    if (threadIdx.x < 32) {
+        const unsigned below = (1u << lx) - 1u;
+        for (int base = 0; base < nt; base += 32) {
+            const int i = base + lx;
+            int key = -1, c = 0;
+            if (i < nt) {
+                c = s_topo[i];
+                if (s_node[c]) key = s_oslot[s_ptr[c]];
+            }
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            const int fill = key >= 0 ? s_pfill[key] : 0;
+            __syncwarp();
+            if (key >= 0) {
+                s_pos[c] = (int16_t)(fill + __popc(peers & below));
+                if ((peers & below) == 0) s_pfill[key] = (int16_t)(fill + __popc(peers));
+            }
+            __syncwarp();
+        }
     }
     __syncthreads();
     const size_t nbase = (size_t)t * kTile * kTile;
