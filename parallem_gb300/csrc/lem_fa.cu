@@ -756,7 +756,7 @@ __global__ void __launch_bounds__(256)
     if (threadIdx.x == 0) s_done = 0, s_dem = -1;
     __syncthreads();
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
-    int done = 0;
+    int done = 0, dem = -1;  // one DEM per tile
     bool outlet[4], src[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -787,12 +787,14 @@ __global__ void __launch_bounds__(256)
                 if (t_pend[(size_t)(ty0 + ly) * W + tx0 + lx] == 0) ++done;
             }
             wl = w[(size_t)(ty0 + ly) * W + tx0 + lx];
-            atomicMax(&s_dem, dem_at(dc, (size_t)(ty0 + ly) * W + tx0 + lx));  // one DEM per tile
+            if (dem < 0) dem = dem_at(dc, (size_t)(ty0 + ly) * W + tx0 + lx);
         }
         s_pend[l] = pend;
         src[q] = pend == 0 && !outlet[q];
         s_val[l] = make_float2(wl, 0.f);
     }
+    dem = __reduce_max_sync(0xffffffffu, dem);
+    if ((threadIdx.x & 31) == 0 && dem >= 0) atomicMax(&s_dem, dem);
     if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
     tile_wave(

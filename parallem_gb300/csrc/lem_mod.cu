@@ -492,6 +492,7 @@ __global__ void __launch_bounds__(256, 5)
     __syncthreads();
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     bool src[4];
+    int dem = -1;  // one DEM per tile
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
@@ -509,7 +510,7 @@ __global__ void __launch_bounds__(256, 5)
             stn = in.L.stn;
             nz = in.L.nz;
             snew = __ldcg(stone + (size_t)(ty0 + ly) * W + tx0 + lx);
-            atomicMax(&s_dem, dem_at(dc, (size_t)(ty0 + ly) * W + tx0 + lx));  // one DEM per tile
+            if (dem < 0) dem = dem_at(dc, (size_t)(ty0 + ly) * W + tx0 + lx);
             const int d = bit_dir(s_code[hc]);
             if (d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn) {
                 const int rlx = lx + dir_dx(d), rly = ly + dir_dy(d);
@@ -535,6 +536,8 @@ __global__ void __launch_bounds__(256, 5)
         s_flag[l] = 0;
         s_pos[l] = -1;
     }
+    dem = __reduce_max_sync(0xffffffffu, dem);
+    if ((threadIdx.x & 31) == 0 && dem >= 0) atomicMax(&s_dem, dem);
     __syncthreads();
     // The waiting cells: every cell downstream of an entry (a cell with a donor
     // in another tile), marked along each entry's in-tile path before the wave.
@@ -1027,7 +1030,7 @@ __global__ void __launch_bounds__(256, 6)
     if (threadIdx.x == 0) s_done = 0, s_dem = -1;
     __syncthreads();
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
-    int done = 0;
+    int done = 0, dem = -1;  // one DEM per tile
     bool src[4], outlet[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -1061,7 +1064,7 @@ __global__ void __launch_bounds__(256, 6)
             }
             st = t_stat[g];
             v = __ldcg(stone + g);
-            atomicMax(&s_dem, dem_at(dc, g));  // one DEM per tile
+            if (dem < 0) dem = dem_at(dc, g);
             if (st == 2 && !outlet[q]) {
                 const SedInit in = sed_init(s_code, s_cls, lx, ly, tx0, ty0, W, ero, inci, geli, soilT, stone, k);
                 s_A[l] = in.L.A;
@@ -1076,6 +1079,8 @@ __global__ void __launch_bounds__(256, 6)
         s_new[l] = v;
         src[q] = pend == 0;
     }
+    dem = __reduce_max_sync(0xffffffffu, dem);
+    if ((threadIdx.x & 31) == 0 && dem >= 0) atomicMax(&s_dem, dem);
     if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
     tile_wave(
