@@ -446,6 +446,40 @@ __device__ __forceinline__ SedInit sed_init(const uint8_t* s_code, const uint8_t
     return r;
 }
 
+// sed_init on the tile's erosion terms staged in shared memory (kTH x kTH
+// halo layout): the same sums in the same order.
+__device__ __forceinline__ SedInit sed_init_staged(const uint8_t* s_code, const uint8_t* s_cls, const float* s_e,
+                                                   const float* s_i, const float* s_g, int lx, int ly, float st0,
+                                                   float stone0, const ModelConsts& k) {
+    const float omd = 1.0f - k.ddk, omc = 1.0f - k.dck, omg = 1.0f - k.dgk;
+    const int hc = (ly + 1) * kTH + lx + 1;
+    SedInit r;
+    r.pend = 0;
+    r.ext = 0;
+    float ad = 0.f, ac = 0.f, ag = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+        const int d = scan_dir(kk);
+        const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
+        if (!donates(s_code[nh], d)) continue;
+        const uint8_t cl = s_cls[nh];
+        if (cl == kCellBlock) {
+            r.pend |= kBlocked;
+            continue;
+        }
+        if (cl != kCellIn) continue;
+        ad = __fadd_rn(ad, __fmul_rn(1.0f, __fmul_rn(s_e[nh], omd)));
+        ac = __fadd_rn(ac, __fmul_rn(1.0f, __fmul_rn(s_i[nh], omc)));
+        ag = __fadd_rn(ag, __fmul_rn(1.0f, __fmul_rn(s_g[nh], omg)));
+        if (in_tile(lx + dir_dx(d), ly + dir_dy(d)))
+            ++r.pend;
+        else
+            ++r.ext;
+    }
+    r.L = sed_local(ad, ac, ag, s_e[hc], s_i[hc], s_g[hc], st0, stone0, k.ddk, k.dck, k.dgk);
+    return r;
+}
+
 __global__ void __launch_bounds__(256, 5)
     k_sedt_local(const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd, const float* __restrict__ ero,
                  const float* __restrict__ inci, const float* __restrict__ geli, float* depo, float* stone,
@@ -459,10 +493,16 @@ __global__ void __launch_bounds__(256, 5)
     __shared__ uint8_t s_cls[kTH * kTH];
     __shared__ int32_t s_pend[kTile * kTile];
     __shared__ float s_new[kTile * kTile];  // settled stone (the old stone until then)
-    __shared__ float s_A[kTile * kTile];
-    __shared__ float s_B[kTile * kTile];
-    __shared__ float s_dep[kTile * kTile];
-    __shared__ float s_stn[kTile * kTile];
+    // A, B, deposition and soil thickness per cell; before them, the halo's
+    // erosion terms (3 kTH x kTH floats) for the set-up
+    __shared__ float s_coef[4 * kTile * kTile];
+    float* const s_A = s_coef;
+    float* const s_B = s_coef + kTile * kTile;
+    float* const s_dep = s_coef + 2 * kTile * kTile;
+    float* const s_stn = s_coef + 3 * kTile * kTile;
+    float* const s_ero = s_coef;
+    float* const s_inc = s_coef + kTH * kTH;
+    float* const s_gel = s_coef + 2 * kTH * kTH;
     __shared__ int16_t s_ptr[kTile * kTile];
     __shared__ int16_t s_topo[kTile * kTile];
     __shared__ int16_t s_pos[kTile * kTile];
@@ -484,6 +524,19 @@ __global__ void __launch_bounds__(256, 5)
     const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
     sed_tile_load(mask, fd, W, H, tx0, ty0, s_code, s_cls);
+    for (int j = threadIdx.x; j < kTH * kTH; j += blockDim.x) {
+        const int gx = tx0 - 1 + j % kTH, gy = ty0 - 1 + j / kTH;
+        float e = 0.f, i = 0.f, g = 0.f;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            const size_t c = (size_t)gy * W + gx;
+            e = __ldg(ero + c);
+            i = __ldg(inci + c);
+            g = __ldg(geli + c);
+        }
+        s_ero[j] = e;
+        s_inc[j] = i;
+        s_gel[j] = g;
+    }
     if (threadIdx.x < kTileEnt) {
         s_ocnt[threadIdx.x] = 0;
         s_pcnt[threadIdx.x] = 0;
@@ -492,6 +545,7 @@ __global__ void __launch_bounds__(256, 5)
     __syncthreads();
     const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     bool src[4];
+    float cA[4], cB[4], cD[4], cS[4];  // the cells' coefficients until the staged terms are spent
     int dem = -1;  // one DEM per tile
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -499,17 +553,19 @@ __global__ void __launch_bounds__(256, 5)
         int32_t pend = kBlocked;
         uint8_t kind = kKindEnd, ext = 0, nz = 0;
         int16_t ptr = (int16_t)l;
-        float A = 0.f, B = 0.f, dep = 0.f, stn = 0.f, snew = 0.f;
+        float snew = 0.f;
+        cA[q] = cB[q] = cD[q] = cS[q] = 0.f;
         if (s_cls[hc] == kCellIn) {
-            const SedInit in = sed_init(s_code, s_cls, lx, ly, tx0, ty0, W, ero, inci, geli, soilT, stone, k);
+            const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
+            snew = __ldcg(stone + g);
+            const SedInit in = sed_init_staged(s_code, s_cls, s_ero, s_inc, s_gel, lx, ly, soilT[g], snew, k);
             pend = in.pend;
             ext = (uint8_t)in.ext;
-            A = in.L.A;
-            B = in.L.B;
-            dep = in.L.dep;
-            stn = in.L.stn;
+            cA[q] = in.L.A;
+            cB[q] = in.L.B;
+            cD[q] = in.L.dep;
+            cS[q] = in.L.stn;
             nz = in.L.nz;
-            snew = __ldcg(stone + (size_t)(ty0 + ly) * W + tx0 + lx);
             if (dem < 0) dem = dem_at(dc, (size_t)(ty0 + ly) * W + tx0 + lx);
             const int d = bit_dir(s_code[hc]);
             if (d >= 0 && s_cls[hc + dir_dy(d) * kTH + dir_dx(d)] == kCellIn) {
@@ -528,16 +584,21 @@ __global__ void __launch_bounds__(256, 5)
         s_ext[l] = ext;
         s_ptr[l] = ptr;
         s_new[l] = snew;
-        s_A[l] = A;
-        s_B[l] = B;
-        s_dep[l] = dep;
-        s_stn[l] = stn;
         s_nz[l] = nz;
         s_flag[l] = 0;
         s_pos[l] = -1;
     }
     dem = __reduce_max_sync(0xffffffffu, dem);
     if ((threadIdx.x & 31) == 0 && dem >= 0) atomicMax(&s_dem, dem);
+    __syncthreads();  // the staged erosion terms are spent
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int l = (ly0 + 8 * q) * kTile + lx;
+        s_A[l] = cA[q];
+        s_B[l] = cB[q];
+        s_dep[l] = cD[q];
+        s_stn[l] = cS[q];
+    }
     __syncthreads();
     // The waiting cells: every cell downstream of an entry (a cell with a donor
     // in another tile), marked along each entry's in-tile path before the wave.
