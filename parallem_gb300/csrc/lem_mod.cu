@@ -725,12 +725,11 @@ __global__ void __launch_bounds__(256, 5)
         const int l = (ly0 + 8 * q) * kTile + lx;
         if (s_node[l]) atomicAdd(&s_pcnt[s_oslot[s_ptr[l]]], 1);
     }
-    // Every waiting cell between nodes: its one waiting in-tile donor (in s_q,
-    // spent since the wave) and its map v -> stone (in place of its own
-    // coefficients, which only nodes need from here on).  Every waiting cell of
-    // a tile without a second wave also takes a final-pass slot, with its
-    // deposition and soil thickness.
-    int16_t* s_up = s_q;
+    // Every waiting cell between nodes: its map v -> stone from its one waiting
+    // in-tile donor (in place of its own coefficients, which only nodes need
+    // from here on).  Every waiting cell of a tile without a second wave also
+    // takes a final-pass slot, with its deposition and soil thickness.
+    int16_t* s_up = s_q;  // the node at the top of a cell's run (s_q is spent since the wave)
     const size_t fbase = (size_t)t * kTile * kTile;
     int fslot[4];
 #pragma unroll
@@ -742,7 +741,6 @@ __global__ void __launch_bounds__(256, 5)
         if (fslot[q] >= 0) f_ds[fbase + fslot[q]] = make_float2(s_dep[l], s_stn[l]);
         if (s_node[l]) continue;
         float Cc = 0.f;
-        int up = l;
 #pragma unroll
         for (int k2 = 0; k2 < 8; ++k2) {
             const int d2 = scan_dir(k2);
@@ -750,52 +748,39 @@ __global__ void __launch_bounds__(256, 5)
             const int uh = hc + dir_dy(d2) * kTH + dir_dx(d2);
             if (!in_tile(ulx, uly) || !donates(s_code[uh], d2) || s_cls[uh] != kCellIn) continue;
             const int u = uly * kTile + ulx;
-            if (s_flag[u] & kFTaint)
-                up = u;
-            else
-                Cc = __fadd_rn(Cc, __fmul_rn(1.0f, s_new[u]));
+            if (!(s_flag[u] & kFTaint)) Cc = __fadd_rn(Cc, __fmul_rn(1.0f, s_new[u]));
         }
         const float4 M = map_cell(s_A[l], s_B[l], Cc, s_nz[l] != 0, s_new[l]);
         s_A[l] = M.x;
         s_B[l] = M.y;
         s_dep[l] = M.z;
         s_stn[l] = M.w;
-        s_up[l] = (int16_t)up;
     }
     __syncthreads();
-    // Pointer jumping along the single-input chains: afterwards s_up of a cell
-    // between nodes is the node at the top of its chain and its map takes that
-    // node's value to its own stone (maps compose, so the chain needs only
-    // log2 of its length in rounds).
-    for (int it = 0; it < 10; ++it) {  // in-tile chains are shorter than 2^10 cells
-        float4 F[4];
-        int16_t P[4];
-        bool ch = false;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int l = (ly0 + 8 * q) * kTile + lx;
-            P[q] = -1;
-            if (s_flag[l] != (kFDone | kFTaint) || s_node[l] || s_kind[s_ptr[l]] != kKindOutlet) continue;
-            const int p = s_up[l];
-            if (s_node[p]) continue;
-            F[q] = map_compose(make_float4(s_A[l], s_B[l], s_dep[l], s_stn[l]),
-                               make_float4(s_A[p], s_B[p], s_dep[p], s_stn[p]));
-            P[q] = s_up[p];
-            ch = true;
+    // The maps of the cells between nodes, composed down each run from the node
+    // at its top: afterwards s_up of such a cell is that node and its map takes
+    // the node's value to its own stone.  One walk per node; no two walks
+    // share a cell (a cell between nodes has one waiting donor).
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        const int l = (ly0 + 8 * q) * kTile + lx;
+        if (!s_node[l] || s_kind[l] != kKindIn) continue;
+        float4 F = map_identity();
+        int c = l;
+        for (int guard = 0; guard < kTile * kTile; ++guard) {
+            const int d = bit_dir(s_code[(c / kTile + 1) * kTH + (c & (kTile - 1)) + 1]);
+            c += dir_dy(d) * kTile + dir_dx(d);  // in the tile: c is not an outlet
+            if (s_flag[c] != (kFDone | kFTaint) || s_node[c]) break;
+            F = map_compose(make_float4(s_A[c], s_B[c], s_dep[c], s_stn[c]), F);
+            s_A[c] = F.x;
+            s_B[c] = F.y;
+            s_dep[c] = F.z;
+            s_stn[c] = F.w;
+            s_up[c] = (int16_t)l;
+            if (s_kind[c] != kKindIn) break;
         }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int l = (ly0 + 8 * q) * kTile + lx;
-            if (P[q] < 0) continue;
-            s_A[l] = F[q].x;
-            s_B[l] = F[q].y;
-            s_dep[l] = F[q].z;
-            s_stn[l] = F[q].w;
-            s_up[l] = P[q];
-        }
-        if (!__syncthreads_or(ch)) break;
     }
+    __syncthreads();
     const int no = s_no, nt = s_nt;
     if (threadIdx.x == 0) {
         int a = 0;
