@@ -149,6 +149,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
                 if (ks == kn) flat += 1;
                 if (ks > kn && kn != knd) {
                     const float s = est(d);
+                    set_slope(sa, sb, d, s);  // kept unless the fp64 arithmetic below replaces it
                     cand |= 1u << d;
                     aspect |= dir_bit(d);
                     smin = fminf(smin, s);
@@ -209,10 +210,6 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
                             bestd = d;
                         }
                     }
-                } else {
-#pragma unroll
-                    for (int d = 0; d < 8; ++d)
-                        if ((cand >> d) & 1u) set_slope(sa, sb, d, est(d));
                 }
                 if (sp4) {
                     sp4[0] = sa;
