@@ -241,7 +241,7 @@ __device__ __forceinline__ void tile_load(const double* __restrict__ z, const ui
     }
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 8)
     k_fat_local(const double* __restrict__ z, const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                 const float* __restrict__ w, float2* __restrict__ t_la, int32_t* __restrict__ t_dst,
                 int32_t* __restrict__ t_pend, int32_t* __restrict__ t_orng, int32_t* __restrict__ t_ent,
@@ -268,10 +268,16 @@ __global__ void __launch_bounds__(256)
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
+    float wq[4];  // the cells' weights, loaded alongside the halo
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int gx = tx0 + lx, gy = ty0 + ly0 + 8 * q;
+        wq[q] = (gx < W && gy < H) ? w[(size_t)gy * W + gx] : 0.f;
+    }
     tile_load(z, mask, fd, W, H, tx0, ty0, s_code, s_cls);
     if (threadIdx.x == 0) s_fn = s_pool = 0;
     __syncthreads();
-    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     bool src[4];  // chain starts, fixed before any chain runs (a chain may enter them later)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -306,7 +312,7 @@ __global__ void __launch_bounds__(256)
                     kind = kKindOutlet;
                 }
             }
-            wl = w[(size_t)(ty0 + ly) * W + tx0 + lx];
+            wl = wq[q];
         }
         s_pend[l] = pend;
         src[q] = pend == 0;
