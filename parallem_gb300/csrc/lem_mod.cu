@@ -90,10 +90,17 @@ __global__ void __launch_bounds__(256, 4)
     for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
         int x, y;
         const size_t i = region_cell(c, ri, W, &x, &y);
+        // every input of the cell in one batch of loads, ahead of the mask test
+        // and the arithmetic (the region's cells outside the catchment are few)
         const float2 f2 = fa[i];
+        const uint8_t mk = mask[i], code = fd[i];
+        const float4 a = reinterpret_cast<const float4*>(slopes)[2 * i];
+        const float4 b = reinterpret_cast<const float4*>(slopes)[2 * i + 1];
+        const float st = soilT[i], tb = totB[i], fi = fines[i], nu = nut[i], sto = stone[i];
+        float T = clim_temp(c, z, z_init, i, outlet, outlet_z);
         const unsigned long long fk = ffkey(f2);
         if (f2.x == f2.x) famax = fk > famax ? fk : famax;  // the reduction skips NaN (thrust::maximum order)
-        if (!mask[i]) {
+        if (!mk) {
             ero[i] = inci[i] = geli[i] = 0.0f;
             slopeptr[i] = 0.0f;
             continue;
@@ -102,12 +109,6 @@ __global__ void __launch_bounds__(256, 4)
         // A multi-direction code among the routed cells (not row 0 / column 0,
         // mfd_accum.cu:42) sends the step's sediment routing to the walk.
         depo[i] = 0.00001f;
-        // every input of the cell in one batch of loads, ahead of the arithmetic
-        const uint8_t code = fd[i];
-        const float4 a = reinterpret_cast<const float4*>(slopes)[2 * i];
-        const float4 b = reinterpret_cast<const float4*>(slopes)[2 * i + 1];
-        const float st = soilT[i], tb = totB[i], fi = fines[i], nu = nut[i], sto = stone[i];
-        float T = clim_temp(c, z, z_init, i, outlet, outlet_z);
         if (x != 0 && y != 0) multi |= (code & (code - 1)) != 0;
         // aveslope (eroincidep.cu:8-37): mean of the positive entries
         const float sv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
@@ -1197,9 +1198,16 @@ __global__ void __launch_bounds__(256, 4)
     for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
         int x, y;
         const size_t i = region_cell(c, ri, W, &x, &y);
+        // every input of the cell in one batch of loads, ahead of the mask test
+        // and the arithmetic (the region's cells outside the catchment are few)
+        const uint8_t mk = mask[i];
         const float dp = depo[i];
+        const float e = ero[i], ic = inci[i], gl = geli[i];
+        const double zold = z[i], z0 = z_init[i];
+        const float2 f2 = fa[i];
+        const float st0 = soilT[i], sn0 = stone[i], sm0 = soilM[i], tb = totB[i], sb0 = soilB[i];
         sd += dp;
-        if (!mask[i]) {
+        if (!mk) {
             totB[i] = 0.0f;  // grow_vegetation (updates.cu:102-105)
             if (dz_out) {
                 dz_out[i] = 0.f;
@@ -1208,11 +1216,6 @@ __global__ void __launch_bounds__(256, 4)
             }
             continue;
         }
-        // every input of the cell in one batch of loads, ahead of the arithmetic
-        const float e = ero[i], ic = inci[i], gl = geli[i];
-        const double zold = z[i], z0 = z_init[i];
-        const float2 f2 = fa[i];
-        const float st0 = soilT[i], sn0 = stone[i], sm0 = soilM[i], tb = totB[i], sb0 = soilB[i];
         const float dz = dp - e - ic - gl;  // surface_change (eroincidep.cu:404)
         const double zc = c.from_current_dem ? (((int)i == outlet) ? outlet_z : zold) : z0;
         float zch, zcl;
