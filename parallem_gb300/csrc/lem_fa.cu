@@ -56,18 +56,19 @@ __global__ void k_fa_prep(const uint8_t* __restrict__ mask, const uint8_t* __res
     for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
         int x, y;
         const size_t i = region_cell(r, ri, W, &x, &y);
-        if (mask[i]) {
+        // the cell's inputs in one batch of loads, ahead of the mask test
+        const uint8_t mk = mask[i], code = fd[i];
+        const float sto = stone[i], tb = totB[i], sm0 = soilM[i];
+        if (mk) {
             ++nact;
-            const float coeff = (1.0f - 0.0085f * stone[i]) * expf(-0.0025f * totB[i] / 76.5f) *
-                                tanhf(0.6f + soilM[i] / 0.2f);
+            const float coeff = (1.0f - 0.0085f * sto) * expf(-0.0025f * tb / 76.5f) * tanhf(0.6f + sm0 / 0.2f);
             const float myppt = (rain0 + (float)(y - r.y0) * rinc) / 1000.0f;
             const float wi = myppt * coeff;
-            float sm = soilM[i] + myppt * (1.0f - coeff);
+            float sm = sm0 + myppt * (1.0f - coeff);
             if (sm > 0.5f) sm = 0.5f;
             soilM[i] = sm;
             w[i] = wi;
             fa[i] = make_float2(wi, 0.0f);
-            const uint8_t code = fd[i];
             untiled |= wi < 0.0f || (code & (code - 1));
         } else {
             w[i] = -9999.0f;
