@@ -1068,9 +1068,12 @@ __global__ void k_flood_raise(const double* __restrict__ z, const uint8_t* __res
         if (!ts.cell(v0, k.W, k.H, x, y)) continue;
         const size_t c = (size_t)y * k.W + x;
         double v = z[c];
+        const uint8_t mk = mask[c];
+        const int dm = dem_at(dc, c);
+        // the basin's raise is read alongside the DEM's sink count
+        const unsigned long long r = mk ? raise[ws[c]] : 0ull;
         // a DEM without sinks keeps its DEM: its second pass repeats the first
-        if (mask[c] && dc.out[dem_at(dc, c)].sinkcount_pass1 != 0) {
-            const unsigned long long r = raise[ws[c]];
+        if (mk && dc.out[dm].sinkcount_pass1 != 0) {
             const unsigned long long kv = dkey(v);
             if (kv != 0 && kv < r) v = dkey_inv(r);  // zs < raise is false for NaN
         }
