@@ -524,15 +524,6 @@ __global__ void __launch_bounds__(256, 5)
     const int W = k.W, H = k.H, TW = (W + kTile - 1) / kTile;
     const int t = ts.tile(blockIdx.x);
     const int tx0 = (t % TW) * kTile, ty0 = (t / TW) * kTile;
-    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
-    float st0q[4], sn0q[4];  // the cells' soil thickness and stone, loaded alongside the halo
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int gx = tx0 + lx, gy = ty0 + ly0 + 8 * q;
-        const bool in = gx < W && gy < H;
-        st0q[q] = in ? soilT[(size_t)gy * W + gx] : 0.f;
-        sn0q[q] = in ? __ldcg(stone + (size_t)gy * W + gx) : 0.f;
-    }
     sed_tile_load(mask, fd, W, H, tx0, ty0, s_code, s_cls);
     for (int j = threadIdx.x; j < kTH * kTH; j += blockDim.x) {
         const int gx = tx0 - 1 + j % kTH, gy = ty0 - 1 + j / kTH;
@@ -553,6 +544,7 @@ __global__ void __launch_bounds__(256, 5)
     }
     if (threadIdx.x == 0) s_nt = s_done = s_fn = 0, s_dem = -1;
     __syncthreads();
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
     bool src[4];
     float cA[4], cB[4], cD[4], cS[4];  // the cells' coefficients until the staged terms are spent
     int dem = -1;  // one DEM per tile
@@ -566,8 +558,8 @@ __global__ void __launch_bounds__(256, 5)
         cA[q] = cB[q] = cD[q] = cS[q] = 0.f;
         if (s_cls[hc] == kCellIn) {
             const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
-            snew = sn0q[q];
-            const SedInit in = sed_init_staged(s_code, s_cls, s_ero, s_inc, s_gel, lx, ly, st0q[q], snew, k);
+            snew = __ldcg(stone + g);
+            const SedInit in = sed_init_staged(s_code, s_cls, s_ero, s_inc, s_gel, lx, ly, soilT[g], snew, k);
             pend = in.pend;
             ext = (uint8_t)in.ext;
             cA[q] = in.L.A;
