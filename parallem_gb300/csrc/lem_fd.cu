@@ -470,17 +470,28 @@ __global__ void k_plateau_final(const double* __restrict__ z, const float* __res
         if (!(v < kFar)) continue;
         const int x = c % W, y = c / W;
         const unsigned long long kc = dkey(z[c]);
-        for (int d = 0; kc != 0 && d < 8; ++d) {
+        if (kc == 0) continue;
+        // the neighbours' heights and distances in one batch of loads
+        unsigned long long kn[8];
+        float vn[8];
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
             const int nx = x + dir_dx(d), ny = y + dir_dy(d);
-            if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
-            const size_t nb = (size_t)ny * W + nx;
-            if (dkey(z[nb]) != kc) continue;
-            if (sp[nb] + ((d & 1) ? 1.41f : 1.0f) == v) {
-                sfd[c] = (uint8_t)dir_bit(d);
-                mfd[c] = (uint8_t)dir_bit(d);
-                if (slopes) slopes[8 * (size_t)c + d] = 0.0001f;
-                break;
+            kn[d] = 0;  // outside the grid: equal to no cell
+            vn[d] = 0.f;
+            if (nx >= 0 && nx < W && ny >= 0 && ny < H) {
+                const size_t nb = (size_t)ny * W + nx;
+                kn[d] = dkey(z[nb]);
+                vn[d] = sp[nb];
             }
+        }
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+            if (kn[d] != kc || vn[d] + ((d & 1) ? 1.41f : 1.0f) != v) continue;
+            sfd[c] = (uint8_t)dir_bit(d);
+            mfd[c] = (uint8_t)dir_bit(d);
+            if (slopes) slopes[8 * (size_t)c + d] = 0.0001f;
+            break;
         }
     }
 }
