@@ -242,7 +242,7 @@ __device__ __forceinline__ void tile_load(const double* __restrict__ z, const ui
     }
 }
 
-__global__ void __launch_bounds__(256, 6)
+__global__ void __launch_bounds__(256, 8)
     k_fat_local(const double* __restrict__ z, const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fd,
                 const float* __restrict__ w, float2* __restrict__ t_la, int32_t* __restrict__ t_dst,
                 int32_t* __restrict__ t_pend, int32_t* __restrict__ t_orng, int32_t* __restrict__ t_ent,
@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(256, 6)
             continue;
         }
         int m = 0;
-#pragma unroll
+#pragma unroll 1
         for (int kk = 0; kk < 8; ++kk) {
             const int d = scan_dir(kk);
             const int nlx = lx + dir_dx(d), nly = ly + dir_dy(d);
