@@ -333,10 +333,10 @@ class EnsembleWork:
             lem._check(L.lem_dem_set_climate(self.b.h, k, C.byref(clim)), "lem_dem_set_climate")
             h2d += C.sizeof(clim)
         lem._check(L.lem_step_batch(self.b.h, 0), "lem_step_batch")
-        tot = lem.Totals()
-        for k in self.ids:
-            lem._check(L.lem_dem_get_totals(self.b.h, k, C.byref(tot)), "lem_dem_get_totals")
-            d2h += C.sizeof(tot)
+        n = len(self.ids)
+        tot = (lem.Totals * n)()
+        lem._check(L.lem_dem_get_totals_n(self.b.h, (C.c_int32 * n)(*self.ids), n, tot), "lem_dem_get_totals_n")
+        d2h += C.sizeof(tot)  # every DEM's budget row of the step
         if j % 50 == 0:
             for k in self.ids:
                 for f in ("fd", "fa", "dem"):

@@ -239,6 +239,9 @@ lem_status lem_dem_set_climate(lem_handle* h, int32_t id, const lem_climate* c);
 /* Flags for this DEM's next step only (LEM_STEP_SET_OUTLET_FROM_FA for its first). */
 lem_status lem_dem_set_step_flags(lem_handle* h, int32_t id, uint32_t flags);
 lem_status lem_dem_get_totals(lem_handle* h, int32_t id, lem_totals* out);  /* synchronous */
+/* The budget rows of n DEMs after one synchronisation (out[k] for ids[k]);
+ * the per-step loop of a batch reads all its rows with it. */
+lem_status lem_dem_get_totals_n(lem_handle* h, const int32_t* ids, int32_t n, lem_totals* out);
 /* One timestep of every active DEM; flags as lem_step, for all DEMs. */
 lem_status lem_step_batch(lem_handle* h, uint32_t flags);
 

@@ -448,9 +448,14 @@ lem_status get_region_field(lem_handle* h, const HostDem& r, int id, lem_field f
     }
 }
 
+lem_status totals_from_host(lem_handle* h, int id, lem_totals* o);
 lem_status totals_of(lem_handle* h, int id, lem_totals* o) {
     lem_status r = sync_scalars(h);
     if (r != LEM_OK) return r;
+    return totals_from_host(h, id, o);
+}
+// the budget row of DEM id from the host copy of the device scalars
+lem_status totals_from_host(lem_handle* h, int id, lem_totals* o) {
     const DevScalars& g = *h->host_sc;
     const DemOut& d = h->host_out[id];
     std::memset(o, 0, sizeof *o);
@@ -1099,6 +1104,18 @@ lem_status lem_dem_get_totals(lem_handle* h, int32_t id, lem_totals* out) {
     if (r != LEM_OK) return r;
     if (!out) return LEM_ERR_INVALID;
     return totals_of(h, id, out);
+}
+
+lem_status lem_dem_get_totals_n(lem_handle* h, const int32_t* ids, int32_t n, lem_totals* out) {
+    if (n < 0 || (n > 0 && (!ids || !out))) return LEM_ERR_INVALID;
+    for (int32_t k = 0; k < n; ++k) {
+        const lem_status r = dem_check(h, ids[k]);
+        if (r != LEM_OK) return r;
+    }
+    if (n == 0) return LEM_OK;
+    lem_status r = totals_of(h, ids[0], out);  // synchronises once
+    for (int32_t k = 1; k < n && r == LEM_OK; ++k) r = totals_from_host(h, ids[k], out + k);
+    return r;
 }
 
 // ---- restart snapshots of one DEM's resident state

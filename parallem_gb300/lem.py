@@ -128,6 +128,7 @@ SIGNATURES = {
     "lem_dem_set_climate": (C.c_int, [_H, C.c_int32, C.POINTER(Climate)]),
     "lem_dem_set_step_flags": (C.c_int, [_H, C.c_int32, C.c_uint32]),
     "lem_dem_get_totals": (C.c_int, [_H, C.c_int32, C.POINTER(Totals)]),
+    "lem_dem_get_totals_n": (C.c_int, [_H, C.POINTER(C.c_int32), C.c_int32, C.POINTER(Totals)]),
     "lem_step_batch": (C.c_int, [_H, C.c_uint32]),
     "lem_set_graphs": (C.c_int, [_H, C.c_int32]),
     "lem_autotune": (C.c_int, [_H, C.c_int32]),
@@ -416,6 +417,14 @@ class Batch:
         t = Totals()
         _check(load().lem_dem_get_totals(self.h, i, C.byref(t)), "lem_dem_get_totals")
         return {k: getattr(t, k) for k, _ in Totals._fields_}
+
+    def totals_n(self, ids) -> list:
+        """The budget rows of several DEMs after one synchronisation."""
+        n = len(ids)
+        idv = (C.c_int32 * n)(*ids)
+        out = (Totals * n)()
+        _check(load().lem_dem_get_totals_n(self.h, idv, n, out), "lem_dem_get_totals_n")
+        return [{k: getattr(t, k) for k, _ in Totals._fields_} for t in out]
 
     @property
     def stream(self) -> int:

@@ -75,6 +75,11 @@ def test_batch_equals_alone(lem):
         got["totals"] = b.totals(i)
         want = run_alone(lem, dem, st, clim, lem.STEP_SET_OUTLET_FROM_FA if n == 1 else 0)
         check_same(got, want, f"dem {n}")
+    # the budget rows of all DEMs after one synchronisation are the rows read one by one
+    rows = b.totals_n(ids[::-1])
+    for i, row in zip(ids[::-1], rows):
+        one = b.totals(i)
+        assert all((row[k] == one[k]) or (row[k] != row[k] and one[k] != one[k]) for k in one), i
     b.close()
 
 
