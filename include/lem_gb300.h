@@ -254,6 +254,23 @@ lem_status lem_step_batch(lem_handle* h, uint32_t flags);
  * eagerly.  The single-stage calls (lem_flow_direction ...) are always eager. */
 lem_status lem_set_graphs(lem_handle* h, int32_t on);
 
+/* Caps of the device loops and tables.  The reference's loops run until their
+ * change flags clear, with no bound (plateau sweeps routeflow.cu:854-872, label
+ * and merge loops routeflow.cu:285-302,314-338, accumulation mfd_simple.cu:
+ * 204-226), and its basin-pair hash table overflows silently
+ * (newflow.cu:860-872).  Here every loop stops after max_rounds rounds and the
+ * next lem_synchronize returns LEM_ERR_NOCONVERGE; the basin-pair table holds
+ * at most 2^edge_table_log2 pairs and a full table makes lem_synchronize return
+ * LEM_ERR_CAPACITY.  After either error the step's results are incomplete but
+ * the handle stays usable.  0 in a field restores its default (65536 rounds;
+ * a table of 8 slots per sink, at least 1024).  Lowering them serves tests of
+ * the error paths and callers that bound a step's device time. */
+typedef struct lem_limits {
+    int32_t max_rounds;       /* rounds of every device loop; 0: 65536                   */
+    int32_t edge_table_log2;  /* log2 of the basin-pair table's slots (1..40); 0: sized per step */
+} lem_limits;
+lem_status lem_set_limits(lem_handle* h, const lem_limits* limits);
+
 /* Autotuner of the launch schedule (no counterpart in the reference).  The
  * handle's next 1 + 4 * cycles steps (lem_step or lem_step_batch; real steps
  * of the model, launched eagerly) run the cooperative kernels with 1, 2 and 4
@@ -288,25 +305,35 @@ size_t lem_snapshot_bytes(lem_handle* h, int32_t id);
 lem_status lem_snapshot_save(lem_handle* h, int32_t id, void* host, size_t bytes);
 lem_status lem_snapshot_load(lem_handle* h, int32_t id, const void* host, size_t bytes);
 
-/* Flow accumulation that allocates nothing.  No counterpart in the reference:
- * it serves callers that must not allocate device memory themselves or through
- * this library -- e.g. a host program that hands the path only buffers from its
+/* Flow accumulation that allocates nothing.  No counterpart in the reference.
+ * It serves callers that must not allocate device memory themselves or through
+ * this library: a host program that hands the path only buffers carved from its
  * own device arena, or a memory-budgeted service that may not call cudaMalloc
- * (a device-wide synchronisation that can also fail under fragmentation) on
- * its request path.  Inputs and the output are the caller's device arrays:
- * d_fd the int32 direction codes (-9999 outside the catchment, as Data.fd),
- * d_weight the runoff weights, d_dem the DEM (cells equal to -9999 are outside
- * and complete with zero flow, like correctmfdflow's okgrid); d_fa receives the
- * accumulation of correctmfdflow with calcpropsSFD proportions (every donor
- * passes its whole flow).  Intermediate data lives in one statically allocated
- * device array sized for LEM_NOALLOC_MAX_CELLS cells (about 27 MB, held by
- * every GPU that loads the library until the process exits); larger grids are
- * rejected with LEM_ERR_CAPACITY before any work.  The first call on a device
- * looks up that array's device address and should come before any stream
- * capture on that device.  All calls share the array: calls whose work
- * overlaps on the GPU (other threads or streams) race, so serialise them.  The
- * call is stream-ordered on `stream` (NULL: the default stream) and returns
- * after its work has finished. */
+ * on its request path (cudaMalloc synchronises the whole device and can fail
+ * under fragmentation).
+ * Inputs and the output are the caller's device arrays, width*height each:
+ *   d_fd      int32 direction codes, one bit per receiving neighbour (N 64,
+ *             NE 128, E 1, SE 2, S 4, SW 8, W 16, NW 32), -9999 outside;
+ *   d_weight  the runoff weight of every cell;
+ *   d_dem     the elevations; cells equal to -9999 are outside the catchment,
+ *             pass no flow and output 0;
+ *   d_fa      receives, for every cell inside, its weight plus the full
+ *             accumulation of every neighbour whose code points at it (a donor
+ *             passes its whole flow to every receiver bit), donors summed in the
+ *             order E, SE, S, SW, W, NW, N, NE.
+ * Cells that no chain of finished donors reaches (a cycle in the codes, or
+ * everything below one) output their own weight and the call returns
+ * LEM_ERR_NOCONVERGE after writing d_fa.
+ * Intermediate data lives in one statically allocated device array sized for
+ * LEM_NOALLOC_MAX_CELLS cells (about 27 MB, held by every GPU that loads the
+ * library until the process exits); larger grids are rejected with
+ * LEM_ERR_CAPACITY before any work.  The call looks up that array's device
+ * address on the current device; the first call on a device must come before
+ * any stream capture on it (later calls inside a capture reuse the address of
+ * the previous call).  All calls share the array and each starts by clearing
+ * what it counts: calls whose work overlaps on the GPU (other threads or
+ * streams) race, so serialise them.  The call is stream-ordered on `stream`
+ * (NULL: the default stream) and returns after its work has finished. */
 #define LEM_NOALLOC_MAX_CELLS (1 << 20)
 lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const double* d_weight, const double* d_dem,
                                        double* d_fa, int32_t width, int32_t height, void* stream);

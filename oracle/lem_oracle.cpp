@@ -4,8 +4,8 @@
 // CPU baseline).  Each function names the reference lines it restates.  The
 // reference's racy GPU sweeps are replaced by deterministic equivalents that
 // reach the same fixpoints:
-//   * plateau routing: the least fixpoint of the float distance relaxation
-//     (newflow.cu:264-350) by repeated raster sweeps; the final direction is the
+//   * plateau routing: the fixpoint of the float distance relaxation
+//     (newflow.cu:264-350) in Dijkstra order; the final direction is the
 //     first direction (N,NE,E,...) whose neighbour attains the cell's distance,
 //     and the 1e-4 slope is written on that direction only;
 //   * basin labels: sink ids are numbered in raster order (the reference uses
@@ -27,7 +27,8 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
-#include <map>
+#include <queue>
+#include <utility>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -123,7 +124,15 @@ void flow_dirs(const Grid& g, const int32_t* mask, const double* zs, double* slo
 }
 
 // shortest_paths_plateaus_initMFD + the route_plateausMFD loop
-// (newflow.cu:234-350, routeflow.cu:826-872 and :632-642).
+// (newflow.cu:234-350, routeflow.cu:826-872 and :632-642).  The reference
+// sweeps dist = min(dist, dist_n + dc) over equal-height neighbours until no
+// cell changes.  That relaxation is monotone, so every fair order of updates
+// ends at the same fixpoint: the greatest one below the start values.  Because
+// fl(d + dc) >= d for dc > 0, a Dijkstra order over the equal-height graph
+// reaches it visiting every cell once: a cell popped with distance v can only
+// be offered fl(v' + dc) >= v' >= v by cells popped after it.  Returns the
+// number of relaxation passes (1; the reference's sweep count depends on its
+// thread schedule).
 int route_plateaus(const Grid& g, const int32_t* mask, const double* zs, double* slopes, int32_t* mfd,
                    int32_t* sfd, float* sp_out) {
     const long N = g.N();
@@ -137,30 +146,48 @@ int route_plateaus(const Grid& g, const int32_t* mask, const double* zs, double*
         if (sfd[i] > 0) sp[i] = 0;
         if (sp[i] != 0) cand.push_back(i);
     }
-    // least fixpoint of sp = min(sp, sp[n] + dc) over equal-height neighbours
-    int sweeps = 0;
-    bool changed = true;
-    while (changed) {
-        changed = false;
-        ++sweeps;
-        for (long i : cand) {
-            int x = (int)(i % g.W), y = (int)(i / g.W);
-            float best = sp[i];
-            for (int d = 0; d < 8; ++d) {
-                int nx = x + kDx[d], ny = y + kDy[d];
-                if (!g.in(nx, ny)) continue;
-                long n = (long)ny * g.W + nx;
+    std::vector<char> is_cand(N, 0);
+    for (long i : cand) is_cand[i] = 1;
+    // seeds: every cell at distance 0 next to an equal-height candidate
+    typedef std::pair<float, long> Item;
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+    for (long i : cand) {
+        int x = (int)(i % g.W), y = (int)(i / g.W);
+        for (int d = 0; d < 8; ++d) {
+            int nx = x + kDx[d], ny = y + kDy[d];
+            if (!g.in(nx, ny)) continue;
+            long n = (long)ny * g.W + nx;
+            if (!is_cand[n] && zs[i] == zs[n]) {
                 float dis = sp[n] + dir_dc(d);
-                if (zs[i] == zs[n] && best > dis) best = dis;
+                if (sp[i] > dis) {
+                    sp[i] = dis;
+                }
             }
-            if (best < sp[i]) {
-                sp[i] = best;
-                changed = true;
+        }
+        if (sp[i] < kFar) heap.push(Item(sp[i], i));
+    }
+    while (!heap.empty()) {
+        Item it = heap.top();
+        heap.pop();
+        long i = it.second;
+        if (it.first != sp[i]) continue;  // a stale entry
+        int x = (int)(i % g.W), y = (int)(i / g.W);
+        for (int d = 0; d < 8; ++d) {
+            int nx = x + kDx[d], ny = y + kDy[d];
+            if (!g.in(nx, ny)) continue;
+            long n = (long)ny * g.W + nx;
+            if (!is_cand[n] || !(zs[i] == zs[n])) continue;
+            float dis = sp[i] + dir_dc(d);  // the step from n to i has the same length
+            if (sp[n] > dis) {
+                sp[n] = dis;
+                heap.push(Item(dis, n));
             }
         }
     }
     // final direction: first neighbour attaining the distance
-    for (long i : cand) {
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < (long)cand.size(); ++k) {
+        const long i = cand[k];
         if (!(sp[i] < kFar)) continue;
         int x = (int)(i % g.W), y = (int)(i / g.W);
         for (int d = 0; d < 8; ++d) {
@@ -177,7 +204,7 @@ int route_plateaus(const Grid& g, const int32_t* mask, const double* zs, double*
     }
     if (sp_out)
         for (long i = 0; i < N; ++i) sp_out[i] = mask[i] == 1 ? sp[i] : 0.0f;
-    return sweeps;
+    return cand.empty() ? 0 : 1;
 }
 
 struct UnionSet {  // union_set (newflow.cu:654-707)
@@ -238,21 +265,35 @@ int flood(const Grid& g, const int32_t* mask, double* zs, const int32_t* sfd, st
     std::vector<long> sinks;
     for (long i = 0; i < N; ++i)
         if (mask[i] == 1 && sfd[i] == 0) sinks.push_back(i);
-    bool changed = true;
-    while (changed) {
-        changed = false;
-        for (long i : sinks) {
-            int x = (int)(i % g.W), y = (int)(i / g.W);
-            int best = ws[i];
-            for (int d = 0; d < 8; ++d) {
-                int nx = x + kDx[d], ny = y + kDy[d];
-                if (!g.in(nx, ny)) continue;
-                long n = (long)ny * g.W + nx;
-                if (zs[n] == zs[i] && ws[n] > best) best = ws[n];
-            }
-            if (best != ws[i]) {
-                ws[i] = best;
-                changed = true;
+    // The loop raises ids to the largest id over equal-height neighbours until
+    // stable: a monotone relaxation, so a worklist that re-examines the
+    // equal-height sink neighbours of every raised cell ends at the same
+    // fixpoint (each connected run of equal-height sinks takes its largest id).
+    std::vector<char> is_sink(N, 0), queued(N, 0);
+    for (long i : sinks) is_sink[i] = 1;
+    std::deque<long> work(sinks.begin(), sinks.end());
+    for (long i : sinks) queued[i] = 1;
+    while (!work.empty()) {
+        long i = work.front();
+        work.pop_front();
+        queued[i] = 0;
+        int x = (int)(i % g.W), y = (int)(i / g.W);
+        int best = ws[i];
+        for (int d = 0; d < 8; ++d) {
+            int nx = x + kDx[d], ny = y + kDy[d];
+            if (!g.in(nx, ny)) continue;
+            long n = (long)ny * g.W + nx;
+            if (zs[n] == zs[i] && ws[n] > best) best = ws[n];
+        }
+        if (best == ws[i]) continue;
+        ws[i] = best;
+        for (int d = 0; d < 8; ++d) {
+            int nx = x + kDx[d], ny = y + kDy[d];
+            if (!g.in(nx, ny)) continue;
+            long n = (long)ny * g.W + nx;
+            if (is_sink[n] && !queued[n] && zs[n] == zs[i] && ws[n] < best) {
+                queued[n] = 1;
+                work.push_back(n);
             }
         }
     }
@@ -272,24 +313,38 @@ int flood(const Grid& g, const int32_t* mask, double* zs, const int32_t* sfd, st
     // identify_watershed_boundary_write_backMFD (newflow.cu:787-877): for every
     // pair of neighbouring cells with different labels the higher cell gives a
     // boundary height; the minimum per unordered label pair is kept.
-    std::map<std::pair<int, int>, double> edges;
-    for (int y = 0; y < g.H; ++y)
-        for (int x = 0; x < g.W; ++x) {
-            long i = (long)y * g.W + x;
-            if (mask[i] != 1) continue;
-            int a = ws[i];
-            for (int d = 0; d < 8; ++d) {
-                int nx = x + kDx[d], ny = y + kDy[d];
-                if (!g.in(nx, ny)) continue;
-                long n = (long)ny * g.W + nx;
-                int b = ws[n];
-                if (a == b) continue;
-                if (!(zs[i] >= zs[n])) continue;
-                std::pair<int, int> key(std::min(a, b), std::max(a, b));
-                auto it = edges.find(key);
-                if (it == edges.end() || zs[i] < it->second) edges[key] = zs[i];
+    struct Pair { int a, b; double w; };
+    std::vector<Pair> pairs;
+#pragma omp parallel
+    {
+        std::vector<Pair> mine;
+#pragma omp for schedule(static)
+        for (int y = 0; y < g.H; ++y)
+            for (int x = 0; x < g.W; ++x) {
+                long i = (long)y * g.W + x;
+                if (mask[i] != 1) continue;
+                int a = ws[i];
+                for (int d = 0; d < 8; ++d) {
+                    int nx = x + kDx[d], ny = y + kDy[d];
+                    if (!g.in(nx, ny)) continue;
+                    long n = (long)ny * g.W + nx;
+                    int b = ws[n];
+                    if (a == b) continue;
+                    if (!(zs[i] >= zs[n])) continue;
+                    mine.push_back({std::min(a, b), std::max(a, b), zs[i]});
+                }
             }
-        }
+#pragma omp critical
+        pairs.insert(pairs.end(), mine.begin(), mine.end());
+    }
+    // the minimum height per unordered label pair, pairs in ascending order
+    std::sort(pairs.begin(), pairs.end(), [](const Pair& p, const Pair& q) {
+        return p.a != q.a ? p.a < q.a : p.b != q.b ? p.b < q.b : p.w < q.w;
+    });
+    std::vector<std::pair<std::pair<int, int>, double>> edges;
+    for (size_t k = 0; k < pairs.size(); ++k)
+        if (k == 0 || pairs[k].a != pairs[k - 1].a || pairs[k].b != pairs[k - 1].b)
+            edges.push_back({{pairs[k].a, pairs[k].b}, pairs[k].w});
     // init_and_sort_watershed_bound_labelsMFD (newflow.cu:905-1050) + Kruskal
     // (routeflow.cu:510-572)
     struct E { int a, b; double w; };
@@ -328,6 +383,7 @@ int flood(const Grid& g, const int32_t* mask, double* zs, const int32_t* sfd, st
     for (int i = 0; i <= max_label; ++i)
         if (raise[i] != 0) raise[i] = raise[set.find_root(i)];
     // raise_watershedMFD (newflow.cu:879-894)
+#pragma omp parallel for schedule(static)
     for (long i = 0; i < N; ++i) {
         if (mask[i] != 1) continue;
         int lab = ws[i];

@@ -3,6 +3,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -1286,6 +1287,16 @@ lem_status lem_set_graphs(lem_handle* h, int32_t on) {
         cudaGraphExecDestroy(h->gexec);
         h->gexec = nullptr;
     }
+    return LEM_OK;
+}
+
+lem_status lem_set_limits(lem_handle* h, const lem_limits* l) {
+    if (!h || !l || l->max_rounds < 0 || l->edge_table_log2 < 0 || l->edge_table_log2 > 40) return LEM_ERR_INVALID;
+    static_assert(offsetof(DevScalars, edge_log_cap) == offsetof(DevScalars, round_cap) + sizeof(int32_t),
+                  "the two limits are adjacent");
+    const int32_t v[2] = {l->max_rounds, l->edge_table_log2};
+    LEM_CUDA_TRY(cudaMemcpyAsync(&h->s.sc->round_cap, v, sizeof v, cudaMemcpyHostToDevice, h->st));
+    LEM_CUDA_TRY(cudaStreamSynchronize(h->st));
     return LEM_OK;
 }
 

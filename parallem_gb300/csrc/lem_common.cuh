@@ -90,7 +90,19 @@ struct DevScalars {
     int32_t tile_src;                // tile outlets with no pending inflow (coarse sources)
     int32_t sed_tiled_ok;            // 1: this step's sediment routing may take the tiled path
     int32_t epoch;                   // flow-direction stages run so far (first-seen marks of basin labels)
+    int32_t round_cap;               // rounds of every device loop before it gives up (0: kDefaultRoundCap)
+    int32_t edge_log_cap;            // log2 slots the basin-pair table may use (0: sized per step)
 };
+
+// Every device loop (grid-barrier rounds, worklist waves) stops after this
+// many rounds and raises ErrFlags::kNoConverge; lem_set_limits lowers it.
+constexpr int kDefaultRoundCap = 1 << 16;
+// Read once at kernel start, so every block of a cooperative launch sees the
+// same value (the host writes it before the launch, in stream order).
+__device__ __forceinline__ int round_cap_of(const DevScalars* sc) {
+    const int c = *((const volatile int32_t*)&sc->round_cap);
+    return c > 0 ? c : kDefaultRoundCap;
+}
 
 // The DEMs of a handle.  A single grid is one DEM covering the whole grid; a
 // batch packs several DEMs into one grid, each in its own region (32-aligned,

@@ -990,6 +990,7 @@ NaDevice g_na[64];
 
 __global__ void k_na_reset(DevScalars* sc, DemOut* dem) {
     dem->fa_done = 0;
+    dem->n_active = 0;
     sc->counters[0] = sc->counters[1] = sc->counters[2] = 0;
     sc->err = 0;
 }
@@ -999,11 +1000,11 @@ __global__ void k_na_reset(DevScalars* sc, DemOut* dem) {
 __global__ void k_na_prep(const int32_t* __restrict__ fd_in, const double* __restrict__ w_in,
                           const double* __restrict__ dem, uint8_t* __restrict__ code, uint8_t* __restrict__ mask,
                           float* __restrict__ w, float2* __restrict__ fa, int32_t* __restrict__ pending,
-                          int32_t* ready, int W, int H, DevScalars* sc) {
+                          int32_t* ready, int W, int H, DevScalars* sc, DemOut* dem_out) {
     const size_t N = (size_t)W * H;
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < N; base += (size_t)gridDim.x * blockDim.x) {
         const size_t i = base + threadIdx.x;
-        bool src = false;
+        bool src = false, act = false;
         if (i < N) {
             const int x = (int)(i % W), y = (int)(i / W);
             const bool in = dem[i] != kNoData;
@@ -1021,7 +1022,10 @@ __global__ void k_na_prep(const int32_t* __restrict__ fd_in, const double* __res
             }
             pending[i] = pend;
             src = in && pend == 0;
+            act = in;
         }
+        const unsigned nact = __ballot_sync(0xffffffffu, act);  // in-catchment cells, one atomic per warp
+        if ((threadIdx.x & 31) == 0 && nact) atomicAdd(&dem_out->n_active, __popc(nact));
         wave_append(src, (int32_t)i, ready, &sc->counters[0], (int)N, &sc->err);
     }
 }
@@ -1042,22 +1046,30 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
     int dev = 0;
     LEM_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return LEM_ERR_INVALID;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    LEM_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
     NaDevice nd;
     {
         std::lock_guard<std::mutex> lock(g_na_mutex);
-        if (!g_na[dev].base) {
-            // once per device, with that device current: the device address of the array
+        if (cap == cudaStreamCaptureStatusNone || !g_na[dev].base) {
+            // With that device current: the device address of the array.  It is
+            // looked up again on every call outside a stream capture, so a
+            // context torn down and created again (cudaDeviceReset) gets the
+            // array's new address; inside a capture the address of the last
+            // call on this device is used.
             void* ptr = nullptr;
             LEM_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
-            int per = 0, sms = 0;
-            LEM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fa_walk, 256, 0));
-            LEM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            if (!g_na[dev].blocks) {
+                int per = 0, sms = 0;
+                LEM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fa_walk, 256, 0));
+                LEM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+                g_na[dev].blocks = (per < 1 ? 1 : per) * sms;
+            }
             g_na[dev].base = static_cast<unsigned char*>(ptr);
-            g_na[dev].blocks = (per < 1 ? 1 : per) * sms;
         }
         nd = g_na[dev];
     }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     DevScalars* sc = reinterpret_cast<DevScalars*>(nd.base);
     DemOut* dem = reinterpret_cast<DemOut*>(nd.base + kNaOffDem);
     uint8_t* code = nd.base + kNaOffCode;
@@ -1070,7 +1082,7 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
     const int T = 256;
     const int blocks = (int)std::min<size_t>((N + T - 1) / T, 152 * 32);
     k_na_reset<<<1, 1, 0, st>>>(sc, dem);  // the array keeps the previous call's contents
-    k_na_prep<<<blocks, T, 0, st>>>(d_fd, d_weight, d_dem, code, mask, w, fa, pending, la, width, height, sc);
+    k_na_prep<<<blocks, T, 0, st>>>(d_fd, d_weight, d_dem, code, mask, w, fa, pending, la, width, height, sc, dem);
     LEM_CUDA_TRY(cudaGetLastError());
     {
         const uint8_t* m = mask;
@@ -1090,10 +1102,16 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
     k_na_out<<<blocks, T, 0, st>>>(fa, d_fa, N);
     LEM_CUDA_TRY(cudaGetLastError());
     uint32_t err = 0;
+    DemOut counts{};
     LEM_CUDA_TRY(cudaMemcpyAsync(&err, &sc->err, sizeof err, cudaMemcpyDeviceToHost, st));
+    LEM_CUDA_TRY(cudaMemcpyAsync(&counts, dem, sizeof counts, cudaMemcpyDeviceToHost, st));
     LEM_CUDA_TRY(cudaStreamSynchronize(st));
     if (err & ErrFlags::kCapacity) return LEM_ERR_CAPACITY;
     if (err) return LEM_ERR_NOCONVERGE;
+    // in-catchment cells the wave never reached (a cycle in the codes, or a
+    // donor chain through one): they hold their own weight, as correctmfdflow
+    // leaves them (mfd_simple.cu:72), and the call says so
+    if (counts.fa_done < counts.n_active) return LEM_ERR_NOCONVERGE;
     return LEM_OK;
 }
 

@@ -20,7 +20,6 @@ namespace {
 constexpr int FD_BX = 32;
 constexpr int FD_BY = 8;
 constexpr float kFar = 20000000.0f;  // shortest_paths_plateaus_initMFD (newflow.cu:252)
-constexpr int kMaxRounds = 1 << 16;
 
 __device__ __forceinline__ unsigned long long key_nodata() { return dkey(-9999.0); }
 
@@ -329,7 +328,7 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
         int32_t* out = (round & 1) ? list_a : list_b;
         const int nin = *((volatile int32_t*)&cnt[round % 3]);
         if (nin == 0) break;
-        if (round >= kMaxRounds) {
+        if (round >= round_cap_of(sc)) {
             if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
             break;
         }
@@ -665,7 +664,7 @@ __global__ void k_flood_merge(const double* __restrict__ z, int32_t* ws, const i
         if (changed) sc->flag[round % 3] = 1;
         grid.sync();
         if (*((volatile int32_t*)&sc->flag[round % 3]) == 0) break;
-        if (round >= kMaxRounds) {
+        if (round >= round_cap_of(sc)) {
             if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
             break;
         }
@@ -713,7 +712,7 @@ __global__ void k_flood_jump(int32_t* ws, int32_t* list_a, int32_t* list_b, Mode
         int32_t* out = (round & 1) ? list_a : list_b;
         const int nin = *((volatile int32_t*)&cnt[round % 3]);
         if (nin == 0) break;
-        if (round >= 64) {
+        if (round >= min(64, round_cap_of(sc))) {  // pointer jumping halves every path per round
             if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
             break;
         }
@@ -752,7 +751,8 @@ __device__ __forceinline__ int edge_logcap(const DevScalars* sc, int logmax) {
     const long long want = 8ll * ((long long)sc->n_sinks + 1);
     int l = 10;
     while (l < logmax && (1ll << l) < want) ++l;
-    return l;
+    const int lim = sc->edge_log_cap;  // lem_set_limits: a smaller table (full tables raise kCapacity)
+    return (lim > 0 && lim < l) ? lim : l;
 }
 
 __global__ void k_edge_clear(unsigned long long* ekey, unsigned long long* ewt, int logmax, DevScalars* sc) {
@@ -976,7 +976,7 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
         if (changed) sc->flag[round % 3] = 1;
         grid.sync();
         if (*((volatile int32_t*)&sc->flag[round % 3]) == 0) break;
-        if (round >= kMaxRounds) {
+        if (round >= round_cap_of(sc)) {
             if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
             break;
         }
@@ -1019,7 +1019,11 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
             }
             if (ch) sc->flag[r % 3] = 1;
             grid.sync();
-            if (*((volatile int32_t*)&sc->flag[r % 3]) == 0 || r >= kMaxRounds) break;
+            if (*((volatile int32_t*)&sc->flag[r % 3]) == 0) break;
+            if (r >= round_cap_of(sc)) {
+                if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+                break;
+            }
         }
         // (b) minimax distance to the component's label basin, in cdist
         for (size_t i = gtid; i < (size_t)n; i += gstride) {
@@ -1043,7 +1047,11 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
             }
             if (ch) sc->flag[r % 3] = 1;
             grid.sync();
-            if (*((volatile int32_t*)&sc->flag[r % 3]) == 0 || r >= kMaxRounds) break;
+            if (*((volatile int32_t*)&sc->flag[r % 3]) == 0) break;
+            if (r >= round_cap_of(sc)) {
+                if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+                break;
+            }
         }
         // (c) the component's largest distance, gathered at its label basin
         for (size_t i = gtid; i < (size_t)n; i += gstride) {

@@ -82,7 +82,6 @@ __device__ __forceinline__ int32_t dec_acq_rel(int32_t* p) {
 }
 
 constexpr int kWaveStack = 8;      // receivers a lane keeps for itself before spilling to the next round
-constexpr int kWaveMaxRounds = 1 << 16;
 
 // The dependency wave shared by flow accumulation and sediment routing, run by
 // every thread of a cooperative launch.  A cell is ready once all its donors
@@ -117,7 +116,7 @@ __device__ int wave_walk(const Op& op, int32_t* pending, int32_t* list_a, int32_
         int32_t* out = (round & 1) ? list_a : list_b;
         const int nin = *((volatile int32_t*)&cnt[round % 3]);
         if (nin == 0) break;
-        if (round >= kWaveMaxRounds) {
+        if (round >= round_cap_of(sc)) {
             if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
             break;
         }
@@ -287,7 +286,7 @@ __device__ void wave_walk_warp(const Op& op, int32_t* pending, int32_t* list_a, 
         int32_t* out = (round & 1) ? list_a : list_b;
         const int nin = *((volatile int32_t*)&cnt[round % 3]);
         if (nin == 0) break;
-        if (round >= kWaveMaxRounds) {
+        if (round >= round_cap_of(sc)) {
             if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
             break;
         }

@@ -89,6 +89,10 @@ def _tuning(h) -> dict:
             "default_ms": t.default_ms, "tuned_ms": t.tuned_ms}
 
 
+class Limits(C.Structure):
+    _fields_ = [("max_rounds", C.c_int32), ("edge_table_log2", C.c_int32)]
+
+
 class KernelStat(C.Structure):
     _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint32), ("total_ms", C.c_double)]
 
@@ -131,6 +135,7 @@ SIGNATURES = {
     "lem_dem_get_totals_n": (C.c_int, [_H, C.POINTER(C.c_int32), C.c_int32, C.POINTER(Totals)]),
     "lem_step_batch": (C.c_int, [_H, C.c_uint32]),
     "lem_set_graphs": (C.c_int, [_H, C.c_int32]),
+    "lem_set_limits": (C.c_int, [_H, C.POINTER(Limits)]),
     "lem_autotune": (C.c_int, [_H, C.c_int32]),
     "lem_get_tuning": (C.c_int, [_H, C.c_void_p]),
     "lem_snapshot_bytes": (C.c_size_t, [_H, C.c_int32]),
@@ -297,6 +302,11 @@ class Model:
 
     def tuning(self) -> dict:
         return _tuning(self.h)
+
+    def limits(self, max_rounds: int = 0, edge_table_log2: int = 0):
+        """Caps of the device loops and of the basin-pair table (lem_set_limits; 0 = default)."""
+        _check(load().lem_set_limits(self.h, C.byref(Limits(int(max_rounds), int(edge_table_log2)))),
+               "lem_set_limits")
 
     def profile(self) -> dict:
         """{kernel name: (launches, total device ms)} since the previous read."""

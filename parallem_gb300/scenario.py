@@ -177,26 +177,48 @@ def config_large(seed: int = 2, n: int = 4096, steps: int = 100) -> Scenario:
     return Scenario(dem, 30.0, rain, temp, 900.0, 9.0, True)
 
 
-def config_ensemble(seed: int = 4, count: int = 64, steps: int = 200, lo: int = 256, hi: int = 2048) -> list:
+def config_ensemble(seed: int = 4, count: int = 64, steps: int = 200, lo: int = 256, hi: int = 2048,
+                    only=None) -> list:
     """The batched ensemble: `count` square DEMs with sides log-uniform in
     [lo, hi], Hurst U(0.6, 0.9), relief U(200, 2000) m, 1-5 % nodata border,
     pits and plateaus at the density of the 4096x4096 grid, each with its own
-    climate series (rain lognormal mean 900 cv 0.3, temperature N(9, 2))."""
+    climate series (rain lognormal mean 900 cv 0.3, temperature N(9, 2)).
+    only: indices of the DEMs to build (the others are None); the random
+    stream is the same, so a DEM is identical with or without it."""
     rng = np.random.default_rng(seed)
     out = []
     cv = 0.3
     sigma = np.sqrt(np.log(1.0 + cv * cv))
     mu = np.log(900.0) - 0.5 * sigma * sigma
+    keep = None if only is None else set(only)
     for i in range(count):
         n = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
         scale = (n / 4096.0) ** 2
-        dem = make_dem(n, float(rng.uniform(0.6, 0.9)), float(rng.uniform(200.0, 2000.0)),
-                       float(rng.uniform(0.01, 0.05)), max(1, int(5000 * scale)), max(1, int(300 * scale)),
-                       seed * 1000 + i)
+        hurst, relief, nodata = float(rng.uniform(0.6, 0.9)), float(rng.uniform(200.0, 2000.0)), \
+            float(rng.uniform(0.01, 0.05))
+        dem = None
+        if keep is None or i in keep:
+            dem = make_dem(n, hurst, relief, nodata, max(1, int(5000 * scale)), max(1, int(300 * scale)),
+                           seed * 1000 + i)
         rain = rng.lognormal(mu, sigma, size=steps)
         temp = rng.normal(9.0, 2.0, size=steps)
-        out.append(Scenario(dem, 30.0, rain, temp, 900.0, 9.0, True))
+        out.append(Scenario(dem, 30.0, rain, temp, 900.0, 9.0, True) if dem is not None else None)
     return out
+
+
+def ensemble_sides(seed: int = 4, count: int = 64, steps: int = 200, lo: int = 256, hi: int = 2048) -> list:
+    """The side lengths config_ensemble draws for the same arguments, without
+    building the DEMs."""
+    rng = np.random.default_rng(seed)
+    sides = []
+    for _ in range(count):
+        sides.append(int(round(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
+        rng.uniform(0.6, 0.9)
+        rng.uniform(200.0, 2000.0)
+        rng.uniform(0.01, 0.05)
+        rng.lognormal(0.0, 1.0, size=steps)
+        rng.normal(9.0, 2.0, size=steps)
+    return sides
 
 
 def config_routing(seed: int = 3, n: int = 8192) -> Scenario:
