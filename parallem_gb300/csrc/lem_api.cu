@@ -976,12 +976,14 @@ lem_status lem_synchronize(lem_handle* h) {
     if (!h) return LEM_ERR_INVALID;
     lem_status r = sync_scalars(h);
     if (r != LEM_OK) return r;
-    const uint32_t err = h->host_sc->err;
+    const uint32_t err = h->host_sc->err, first = h->host_sc->err_first;
     if (err) {
-        uint32_t zero = 0;
-        LEM_CUDA_TRY(cudaMemcpy(&h->s.sc->err, &zero, sizeof zero, cudaMemcpyHostToDevice));
-        if (err & ErrFlags::kCapacity) return LEM_ERR_CAPACITY;
-        return LEM_ERR_NOCONVERGE;
+        const uint32_t zero[2] = {0, 0};  // err and err_first
+        LEM_CUDA_TRY(cudaMemcpy(&h->s.sc->err, zero, sizeof zero, cudaMemcpyHostToDevice));
+        // the first error raised; a later one may be its consequence
+        if (first == ErrFlags::kNoConverge) return LEM_ERR_NOCONVERGE;
+        if (first == ErrFlags::kCapacity) return LEM_ERR_CAPACITY;
+        return (err & ErrFlags::kCapacity) ? LEM_ERR_CAPACITY : LEM_ERR_NOCONVERGE;
     }
     return LEM_OK;
 }

@@ -1,6 +1,7 @@
 // lem_common.cuh -- shared device helpers of the GB300 landscape-evolution path.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -73,6 +74,15 @@ struct ErrFlags {  // bits of the device error word
     static constexpr uint32_t kNoConverge = 2u;
 };
 
+// Raises an error flag.  `err` is DevScalars::err; the word after it keeps the
+// first flag raised, which the host reports: a loop that stops at its round
+// cap leaves later tables inconsistent, and an overflow those raise is a
+// consequence, not the cause.
+__device__ __forceinline__ void raise_error(uint32_t* err, uint32_t flag) {
+    atomicOr(err, flag);
+    atomicCAS(err + 1, 0u, flag);
+}
+
 // Device-side scalars of one handle (one allocation, read back only on request).
 struct DevScalars {
     int32_t sinkcount_pass1;         // masked-in SFD == 0 after the first plateau pass, all DEMs
@@ -82,7 +92,8 @@ struct DevScalars {
     int32_t n_edges;                 // distinct basin pairs
     int32_t n_basins;
     int32_t flood_sweeps, label_rounds, spill_rounds;
-    uint32_t err;
+    uint32_t err;                    // ErrFlags raised since the host last read them
+    uint32_t err_first;              // the first of them (a later one may be its consequence)
     int32_t round_id;                // monotonic id of worklist rounds (de-duplication marks)
     int32_t flag[4];                 // convergence flags of the cooperative loops
     int32_t counters[8];
@@ -103,6 +114,9 @@ __device__ __forceinline__ int round_cap_of(const DevScalars* sc) {
     const int c = *((const volatile int32_t*)&sc->round_cap);
     return c > 0 ? c : kDefaultRoundCap;
 }
+
+static_assert(offsetof(DevScalars, err_first) == offsetof(DevScalars, err) + sizeof(uint32_t),
+              "raise_error keeps the first flag in the word after err");
 
 // The DEMs of a handle.  A single grid is one DEM covering the whole grid; a
 // batch packs several DEMs into one grid, each in its own region (32-aligned,

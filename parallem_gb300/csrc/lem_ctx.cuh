@@ -226,7 +226,7 @@ __device__ __forceinline__ void block_append(bool pred, int32_t value, int32_t* 
         if (pos < cap)
             list[pos] = value;
         else
-            atomicOr(err, ErrFlags::kCapacity);
+            raise_error(err, ErrFlags::kCapacity);
     }
 }
 

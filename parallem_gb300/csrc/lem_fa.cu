@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(256, 8)
         }
         const int start = atomicAdd(&s_pool, nin);
         if (start + nin > kTilePool) {
-            atomicOr(&sc->err, ErrFlags::kCapacity);
+            raise_error(&sc->err, ErrFlags::kCapacity);
             continue;
         }
         int m = 0;
@@ -993,6 +993,7 @@ __global__ void k_na_reset(DevScalars* sc, DemOut* dem) {
     dem->n_active = 0;
     sc->counters[0] = sc->counters[1] = sc->counters[2] = 0;
     sc->err = 0;
+    sc->err_first = 0;
 }
 
 // Codes, mask, weights, initial accumulation and in-degrees from the caller's
@@ -1101,13 +1102,14 @@ extern "C" lem_status lem_accumulate_flow_noalloc(const int32_t* d_fd, const dou
     }
     k_na_out<<<blocks, T, 0, st>>>(fa, d_fa, N);
     LEM_CUDA_TRY(cudaGetLastError());
-    uint32_t err = 0;
+    uint32_t err[2] = {0, 0};  // err and err_first
     DemOut counts{};
-    LEM_CUDA_TRY(cudaMemcpyAsync(&err, &sc->err, sizeof err, cudaMemcpyDeviceToHost, st));
+    LEM_CUDA_TRY(cudaMemcpyAsync(err, &sc->err, sizeof err, cudaMemcpyDeviceToHost, st));
     LEM_CUDA_TRY(cudaMemcpyAsync(&counts, dem, sizeof counts, cudaMemcpyDeviceToHost, st));
     LEM_CUDA_TRY(cudaStreamSynchronize(st));
-    if (err & ErrFlags::kCapacity) return LEM_ERR_CAPACITY;
-    if (err) return LEM_ERR_NOCONVERGE;
+    if (err[1] == ErrFlags::kCapacity || (err[0] & ErrFlags::kCapacity && err[1] != ErrFlags::kNoConverge))
+        return LEM_ERR_CAPACITY;
+    if (err[0]) return LEM_ERR_NOCONVERGE;
     // in-catchment cells the wave never reached (a cycle in the codes, or a
     // donor chain through one): they hold their own weight, as correctmfdflow
     // leaves them (mfd_simple.cu:72), and the call says so

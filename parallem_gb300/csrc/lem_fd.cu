@@ -52,7 +52,7 @@ __device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t* l
         if (pos < cap)
             list[pos] = value;
         else
-            atomicOr(err, ErrFlags::kCapacity);
+            raise_error(err, ErrFlags::kCapacity);
     }
 }
 
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
         const int nin = *((volatile int32_t*)&cnt[round % 3]);
         if (nin == 0) break;
         if (round >= round_cap_of(sc)) {
-            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            if (gtid == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
             break;
         }
         if (gtid == 0) cnt[(round + 2) % 3] = 0;
@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
                         if (pos < ncap)
                             out[pos] = nt;
                         else
-                            atomicOr(&sc->err, ErrFlags::kCapacity);
+                            raise_error(&sc->err, ErrFlags::kCapacity);
                     }
                 }
             }
@@ -665,7 +665,7 @@ __global__ void k_flood_merge(const double* __restrict__ z, int32_t* ws, const i
         grid.sync();
         if (*((volatile int32_t*)&sc->flag[round % 3]) == 0) break;
         if (round >= round_cap_of(sc)) {
-            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            if (gtid == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
             break;
         }
     }
@@ -713,7 +713,7 @@ __global__ void k_flood_jump(int32_t* ws, int32_t* list_a, int32_t* list_b, Mode
         const int nin = *((volatile int32_t*)&cnt[round % 3]);
         if (nin == 0) break;
         if (round >= min(64, round_cap_of(sc))) {  // pointer jumping halves every path per round
-            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            if (gtid == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
             break;
         }
         if (gtid == 0) cnt[(round + 2) % 3] = 0;
@@ -777,7 +777,7 @@ __device__ __forceinline__ void edge_insert(unsigned long long* ekey, unsigned l
         }
         h = (h + 1) & capm;
         if (probes >= 4096) {
-            atomicOr(&sc->err, ErrFlags::kCapacity);
+            raise_error(&sc->err, ErrFlags::kCapacity);
             return;
         }
     }
@@ -977,7 +977,7 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
         grid.sync();
         if (*((volatile int32_t*)&sc->flag[round % 3]) == 0) break;
         if (round >= round_cap_of(sc)) {
-            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            if (gtid == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
             break;
         }
     }
@@ -1021,7 +1021,7 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
             grid.sync();
             if (*((volatile int32_t*)&sc->flag[r % 3]) == 0) break;
             if (r >= round_cap_of(sc)) {
-                if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+                if (gtid == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
                 break;
             }
         }
@@ -1049,7 +1049,7 @@ __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __r
             grid.sync();
             if (*((volatile int32_t*)&sc->flag[r % 3]) == 0) break;
             if (r >= round_cap_of(sc)) {
-                if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+                if (gtid == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
                 break;
             }
         }

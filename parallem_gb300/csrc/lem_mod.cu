@@ -832,7 +832,7 @@ __global__ void __launch_bounds__(256, 5)
         }
         const int start = atomicAdd(&s_pool, nin);
         if (start + nin > kPool) {
-            atomicOr(&sc->err, ErrFlags::kCapacity);
+            raise_error(&sc->err, ErrFlags::kCapacity);
             continue;
         }
         float C = 0.f;

@@ -50,7 +50,7 @@ __device__ __forceinline__ void wave_append(bool pred, int32_t value, int32_t* l
         if (pos < cap)
             list[pos] = value;
         else
-            atomicOr(err, ErrFlags::kCapacity);
+            raise_error(err, ErrFlags::kCapacity);
     }
 }
 
@@ -117,7 +117,7 @@ __device__ int wave_walk(const Op& op, int32_t* pending, int32_t* list_a, int32_
         const int nin = *((volatile int32_t*)&cnt[round % 3]);
         if (nin == 0) break;
         if (round >= round_cap_of(sc)) {
-            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            if (gtid == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
             break;
         }
         if (gtid == 0) {
@@ -146,7 +146,7 @@ __device__ int wave_walk(const Op& op, int32_t* pending, int32_t* list_a, int32_
             }
             if (!__any_sync(0xffffffffu, cur >= 0)) break;
             if (guard > 2 * N + 64) {  // every cell is finished at most once
-                if (lane == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+                if (lane == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
                 break;
             }
             int32_t spill[8];
@@ -287,7 +287,7 @@ __device__ void wave_walk_warp(const Op& op, int32_t* pending, int32_t* list_a, 
         const int nin = *((volatile int32_t*)&cnt[round % 3]);
         if (nin == 0) break;
         if (round >= round_cap_of(sc)) {
-            if (gtid == 0) atomicOr(&sc->err, ErrFlags::kNoConverge);
+            if (gtid == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
             break;
         }
         if (gtid == 0) {
