@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE.  The reference's hot path is CUDA C: its kernel bodies are
 plain C++ apart from the launch syntax of the host files that call them.  This
 recipe copies the named kernel and helper definitions out of the reference
-files where they lie (default /root/reference, or $PARALLEM_REF) into
+files where they lie ($PARALLEM_REF, else a `reference` folder beside the
+repository) into
 oracle/_ref/ref_kernels.inc -- a build product that stays out of git -- and
 compiles them with oracle/ref_shim.h (sequential emulation of a CUDA grid) and
 oracle/ref_harness.cpp (the host loops of cuFlowDirection, correctmfdflow and
@@ -20,7 +21,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libref.so")
-REF = os.environ.get("PARALLEM_REF", "/root/reference")
+# the reference tree: $PARALLEM_REF, else a `reference` folder beside the repository
+REF = os.environ.get("PARALLEM_REF") or os.path.normpath(os.path.join(HERE, os.pardir, os.pardir, "reference"))
 
 # (file, list of definition-start regexes) in the order they are emitted
 PIECES = [

@@ -7,8 +7,9 @@ one step.  Tolerances (stated per check):
   fp64 quotient);
 * accumulation: 1e-5 relative (the required bound); elevation: 1e-9
   relative + 1e-6 m (fp64 state, fp32 increments);
-* process grids: |gpu - oracle| <= 1e-5 |oracle| + 1e-6 max|oracle| (fp32
-  arithmetic; differences such as geli = soilT - ero and dz cancel);
+* process grids: 1e-5 relative; gelifluction and incision, whose formulas
+  cancel (geli = soilT - ero, fa*cs^2/1e4 - Qthreshold), and the diagnostics
+  dz, weatherC, weatherP add 1e-6 of the field's largest magnitude;
 * budget totals: 1e-5 relative.
 The headline configurations are compared with the oracle at full size: one
 step of the 4096x4096 grid, the 8192x8192 routing stress grid (directions,
@@ -123,11 +124,18 @@ def report(name, stats):
     print(f"ERRDIST {name} {json.dumps(stats, sort_keys=True)}")
 
 
+# Process grids whose formulas cancel: gelifluction is capped at soilT - ero and
+# incision starts at fa*cs^2/1e4 - Qthreshold, so near those points a 1e-7
+# relative input difference is a much larger relative output difference.  They
+# keep an additive term of 1e-6 of the field's largest magnitude; every other
+# process grid is held to 1e-5 relative alone.  (Measured at the headline sizes:
+# 0.004-0.04 % of cells of these two need the additive term, none of the rest.)
+CANCELLING = ("geli", "inci")
+
+
 def check_mod(o, g, mask, diag=False):
-    # fp32 process arithmetic: 1e-5 of the value plus 1e-6 of the field's largest
-    # magnitude (differences such as geli = soilT - ero or dz cancel)
     for f in MOD_FIELDS:
-        close(f, g.get(f), o[f], mask, afrac=1e-6)
+        close(f, g.get(f), o[f], mask, afrac=1e-6 if f in CANCELLING else 0.0)
     if diag:
         for f in ("dz", "wC", "wP"):
             close(f, g.get(f), o[f], mask, afrac=1e-6)

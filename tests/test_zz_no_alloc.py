@@ -36,6 +36,7 @@ def _handle_path_and_oracle(seed: int, n: int) -> dict:
     o.flow_direction()
     o.flow_accumulation()
     out["oracle"] = {f: o[f].copy() for f in ("fd", "runoff", "fa")}
+    out["unreached"] = o.s.fa_uncomputed  # e.g. a 2-cycle at the outlet, whose code is forced to 16
     return out
 
 
@@ -63,15 +64,17 @@ def test_noalloc_matches_the_oracle_and_the_handle_path_on_consecutive_calls():
     for seed, n in ((31, 256), (37, 384), (31, 256)):
         ref = _handle_path_and_oracle(seed, n)
         inside = ref["dem"] != -9999
+        # LEM_ERR_NOCONVERGE exactly when the oracle leaves cells unreached; d_fa is written either way
+        want = 3 if ref["unreached"] else 0
         # from the oracle's own codes and weights: correctmfdflow directly
         o = ref["oracle"]
         rc, fa = _noalloc(L, o["fd"], o["runoff"], ref["dem"])
-        assert rc == 0, lem.STATUS.get(rc, rc)
+        assert rc == want, lem.STATUS.get(rc, rc)
         np.testing.assert_allclose(fa[inside], o["fa"][inside], rtol=1e-5, atol=0)
         assert np.all(fa[~inside] == 0.0)
         # from the handle path's codes and weights: the existing entry point
         rc, fa = _noalloc(L, ref["fd"], ref["runoff"], ref["dem"])
-        assert rc == 0, lem.STATUS.get(rc, rc)
+        assert rc == want, lem.STATUS.get(rc, rc)
         np.testing.assert_allclose(fa[inside], ref["fa"][inside], rtol=1e-5, atol=0)
         assert np.all(fa[~inside] == 0.0)
 
