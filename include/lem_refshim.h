@@ -18,7 +18,8 @@
  *                     testoutletislowest), sinkcount
  *   computeRunOffWeights  runoffweight, soilMPtr (runs the whole
  *                     accumulation stage: runoff, proportions, correctmfdflow)
- *   correctmfdflow    fa, FA_max, and on the first iteration outletcellidx
+ *   correctmfdflow    fa, FA_max (from the fa mirror), and on the first
+ *                     iteration outletcellidx
  *   erosionGPU        dem, SlopePtr, the seven soil and vegetation grids,
  *                     eroPtr, inciPtr, geliPtr, depoPtr, dz, weatherC, weatherP
  *                     (when allocated) and the tot* budget scalars

@@ -234,10 +234,18 @@ void correctmfdflow(Data* data, Data* device, int iter) {
     Shim* sh = need(data, "correctmfdflow");
     if (!sh) return;
     lem_totals t;
-    if (!pull(data, sh, LEM_F_FA, data->fa, "correctmfdflow: fa")) return;
+    if (!data->fa || !pull(data, sh, LEM_F_FA, data->fa, "correctmfdflow: fa")) return;
     if (!ok(data, "correctmfdflow: totals", lem_get_totals(sh->h, &t))) return;
-    data->FA_max = t.fa_max;
-    if (first_iteration(data, iter)) data->outletcellidx = t.outlet;  // mfd_simple.cu:336-349
+    // FA_max: the largest accumulation, from 0 up (mfd_simple.cu:338-354); the
+    // device derives it later, in the erosion stage, so it is taken here from
+    // the mirror
+    double fa_max = 0.0;
+    for (long i = 0; i < cells(data); ++i)
+        if (data->fa[i] > fa_max) fa_max = data->fa[i];
+    data->FA_max = fa_max;
+    // the first iteration's outlet, which the stage moved to the first cell
+    // holding that maximum (mfd_simple.cu:336-349)
+    if (first_iteration(data, iter)) data->outletcellidx = t.outlet;
     if (data->outlog) {
         std::fprintf(data->outlog, "Number of actual cells not computed = %d\n", t.fa_uncomputed);
         std::fprintf(data->outlog, "FA: Maximum FA is  %.6f \n\n", data->FA_max);
