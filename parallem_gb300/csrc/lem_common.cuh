@@ -140,7 +140,7 @@ struct DemOut {
     unsigned long long lowest_key;   // min masked-in DEM key (testoutletislowest)
     unsigned long long fa_max_key;   // FA_max as an ordered key of hi+lo
     double base_level;               // update_newSurface base (updates.cu:151)
-    double outlet_z_clim;            // z[outlet] as seen by the climate grids
+    double outlet_z_clim;            // z[outlet] as seen by the climate grids ...
     double tot_e, tot_i, tot_g, tot_d, tot_wc, tot_wp, tot_bio;
     int32_t outlet;                  // grid cell index
     int32_t sink_counter, flat_counter;
@@ -149,6 +149,8 @@ struct DemOut {
     int32_t fa_done, sed_done, n_active;
     int32_t argmax;                  // first cell holding FA_max
     int32_t zero_seen;               // epoch of the last sinkcount that counted basin 0
+    int32_t outlet_clim;             // ... for this cell: the outlet when the step's directions were
+                                     //   computed (the accumulation stage may move the outlet)
 };
 
 struct DemCtx {

@@ -1125,7 +1125,8 @@ __global__ void k_fd_outlets(uint8_t* __restrict__ fd, double* z, DemCtx dc) {
     fd[outlet] = 16;
     if (o.sinkcount_pass1 == 0) o.sinkcount = 0;
     const double zo = z[outlet];
-    o.outlet_z_clim = zo;
+    o.outlet_z_clim = zo;  // SetClimateMatrices ran before testoutletislowest lowers it (lem.cpp:80-84)
+    o.outlet_clim = outlet;
     unsigned long long low = o.lowest_key;
     const unsigned long long k1000 = dkey(1000.0);
     if (low > k1000) low = k1000;

@@ -28,8 +28,8 @@ constexpr double kMinHeight = 467.228;  // Data.cpp:252
 // grids were built from (the initial DEM during run-in, the DEM at the start of
 // the step otherwise; the outlet uses its value before the stage-1 adjustment).
 __device__ __forceinline__ float clim_temp(const DemIn& c, const double* z, const double* z_init, size_t i,
-                                           int outlet, double outlet_z) {
-    double zc = c.from_current_dem ? (((int)i == outlet) ? outlet_z : z[i]) : z_init[i];
+                                           int outlet_clim, double outlet_z) {
+    double zc = c.from_current_dem ? (((int)i == outlet_clim) ? outlet_z : z[i]) : z_init[i];
     float hi, lo;
     dsplit(zc, hi, lo);
     return (float)c.temp - ((hi - (float)kMinHeight) + lo) * 0.0065f;
@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(256, 4)
     DemOut& o = dc.out[ch.d];
     const int W = k.W;
     const int outlet = o.outlet;
+    const int outlet_clim = o.outlet_clim;  // the cell whose climate elevation is outlet_z_clim
     const double outlet_z = o.outlet_z_clim;
     if (ch.first == 0 && threadIdx.x == 0) o.base_level = z[outlet] - 0.00012;  // updates.cu:151
     float se = 0.f, si = 0.f, sg = 0.f;
@@ -97,7 +98,7 @@ __global__ void __launch_bounds__(256, 4)
         const float4 a = reinterpret_cast<const float4*>(slopes)[2 * i];
         const float4 b = reinterpret_cast<const float4*>(slopes)[2 * i + 1];
         const float st = soilT[i], tb = totB[i], fi = fines[i], nu = nut[i], sto = stone[i];
-        float T = clim_temp(c, z, z_init, i, outlet, outlet_z);
+        float T = clim_temp(c, z, z_init, i, outlet_clim, outlet_z);
         const unsigned long long fk = ffkey(f2);
         if (f2.x == f2.x) famax = fk > famax ? fk : famax;  // the reduction skips NaN (thrust::maximum order)
         if (!mk) {
@@ -160,7 +161,7 @@ __global__ void __launch_bounds__(256, 4)
         if (T >= -20.f && T <= 8.87f)
             kappa = 0.15711f - 0.011835f * T - 0.001195f * T * T + 0.000038f * T * T * T + 0.000002f * T * T * T * T;
         if (fabsf(T - 8.87f) < 1e-3f || fabsf(T + 20.0f) < 1e-3f || fabsf(kappa) < 4e-3f) {
-            const double zc = c.from_current_dem ? (((int)i == outlet) ? outlet_z : z[i]) : z_init[i];
+            const double zc = c.from_current_dem ? (((int)i == outlet_clim) ? outlet_z : z[i]) : z_init[i];
             const double Td = c.temp - ((zc - kMinHeight) * 0.0065);
             double kd = (double)k.kappa;
             if (Td >= -20. && Td <= 8.87)
@@ -1190,6 +1191,7 @@ __global__ void __launch_bounds__(256, 4)
     const DemIn& c = dc.in[ch.d];
     DemOut& o = dc.out[ch.d];
     const int outlet = o.outlet;
+    const int outlet_clim = o.outlet_clim;  // the cell whose climate elevation is outlet_z_clim
     const double outlet_z = o.outlet_z_clim;
     const double base = o.base_level;
     const float rain0 = (float)c.rain, rinc = (float)c.rain_inc;
@@ -1217,7 +1219,7 @@ __global__ void __launch_bounds__(256, 4)
             continue;
         }
         const float dz = dp - e - ic - gl;  // surface_change (eroincidep.cu:404)
-        const double zc = c.from_current_dem ? (((int)i == outlet) ? outlet_z : zold) : z0;
+        const double zc = c.from_current_dem ? (((int)i == outlet_clim) ? outlet_z : zold) : z0;
         float zch, zcl;
         dsplit(zc, zch, zcl);
         const float T = (float)c.temp - ((zch - (float)kMinHeight) + zcl) * 0.0065f;

@@ -59,13 +59,17 @@ def resync(o, g):
 
 
 def close(name, gv, ov, mask, rtol=1e-5, afrac=1e-8, atol=0.0):
+    cells = np.flatnonzero(np.broadcast_to(mask, np.shape(gv)))
     gv, ov = np.asarray(gv)[mask], np.asarray(ov)[mask]
     both_nan = np.isnan(gv) & np.isnan(ov)
     scale = np.nanmax(np.abs(ov)) if ov.size else 0.0
     err = np.where(both_nan, 0.0, np.abs(gv - ov))
     bad = ~(err <= rtol * np.abs(ov) + afrac * scale + atol) & ~both_nan
-    assert not bad.any(), (f"{name}: {int(bad.sum())} of {bad.size} outside tolerance, max err "
-                           f"{np.nanmax(err):.3e} (scale {scale:.3e})")
+    if bad.any():
+        w = int(np.nanargmax(np.where(bad, err, -1.0)))
+        raise AssertionError(f"{name}: {int(bad.sum())} of {bad.size} outside tolerance, max err "
+                             f"{np.nanmax(err):.3e} (scale {scale:.3e}); worst at flat index {int(cells[w])}: "
+                             f"gpu {gv[w]!r}, oracle {ov[w]!r}")
 
 
 def check_fd(o, g, mask):
