@@ -10,6 +10,7 @@
 // calcpropsSFD, correctmfdflow, cleardevicespace_FA, setdevicespace_Process,
 // erosionGPU, cleardevicespace_Process, the summary row, zerogrids; finally
 // clearDeviceSpace.
+#include <chrono>
 #include <cstdlib>
 #include <cstring>
 
@@ -22,16 +23,23 @@ double* dup(const double* src, long n) {
     return p;
 }
 double* zeros(long n) { return (double*)std::calloc(n, sizeof(double)); }
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
 }  // namespace
 
 // soil: stone, fines, soilT, soilM, soilB, nut, TotB (7 * N).  out: dem, fa,
 // runoffweight, SlopePtr, stone, fines, soilT, soilM, soilB, nut, TotB, ero,
 // inci, geli, depo, dz (16 * N).  codes: fd, SFD (2 * N).  rows: per step
 // totE, totI, totG, totD, totweatherC, totweatherP, totbio, FA_max, sinkcount,
-// outletcellidx (10 per step).  Returns lem_refshim_status().
+// outletcellidx (10 per step).  stage_ms (optional): per step the flow-direction,
+// accumulation and erosion calls with their device-space calls, and the whole
+// step, wall clock.  Returns lem_refshim_status().
 extern "C" int refshim_run(int W, int H, double cellsize, const double* dem, const double* soil, int outlet,
                            const lem_params* p, double init_rain, double init_temp, int first_iter, int steps,
-                           const double* rain, const double* temp, double* out, int* codes, double* rows) {
+                           const double* rain, const double* temp, double* out, int* codes, double* rows,
+                           double* stage_ms) {
     const long N = (long)W * H;
     Data data;
     Data device;
@@ -96,18 +104,28 @@ extern "C" int refshim_run(int W, int H, double cellsize, const double* dem, con
             data.rain = rain[k];
             data.temp = temp[k];
         }
+        const double t0 = now_ms();
         setdevicespace_FD(&data, &device);
         cuFlowDirection(&data, &device, i);
         cleardevicespace_FD(&data, &device);
+        const double t1 = now_ms();
         setdevicespace_FA(&data, &device);
         computeRunOffWeights(&data, &device);
         calcwater(&data);
         calcpropsSFD(&data, &device);
         correctmfdflow(&data, &device, i);
         cleardevicespace_FA(&data, &device);
+        const double t2 = now_ms();
         setdevicespace_Process(&data, &device);
         erosionGPU(&data, &device, i);
         cleardevicespace_Process(&data, &device);
+        const double t3 = now_ms();  // every shim call returns after its device work
+        if (stage_ms) {
+            stage_ms[4 * k + 0] = t1 - t0;
+            stage_ms[4 * k + 1] = t2 - t1;
+            stage_ms[4 * k + 2] = t3 - t2;
+            stage_ms[4 * k + 3] = t3 - t0;
+        }
         double* r = rows + 10 * k;  // writeSummaryDataToFile's fields (io.cpp:233-263)
         r[0] = data.totE;
         r[1] = data.totI;

@@ -76,12 +76,12 @@ def driver(tmp_path_factory):
     L = C.CDLL(so)
     P = C.c_void_p
     L.refshim_run.argtypes = [C.c_int, C.c_int, C.c_double, P, P, C.c_int, P, C.c_double, C.c_double, C.c_int,
-                              C.c_int, P, P, P, P, P]
+                              C.c_int, P, P, P, P, P, P]
     L.refshim_run.restype = C.c_int
     return L
 
 
-def run_driver(L, dem, st, params, init_rain, init_temp, first_iter, rain, temp):
+def run_driver(L, dem, st, params, init_rain, init_temp, first_iter, rain, temp, stage_ms=None):
     H, W = dem.shape
     N = H * W
     steps = len(rain)
@@ -94,7 +94,7 @@ def run_driver(L, dem, st, params, init_rain, init_temp, first_iter, rain, temp)
     t = np.ascontiguousarray(temp, np.float64)
     rc = L.refshim_run(W, H, 30.0, dem.ctypes.data, soil.ctypes.data, int(st["outlet"]), C.addressof(params),
                        init_rain, init_temp, first_iter, steps, r.ctypes.data, t.ctypes.data, out.ctypes.data,
-                       codes.ctypes.data, rows.ctypes.data)
+                       codes.ctypes.data, rows.ctypes.data, None if stage_ms is None else stage_ms.ctypes.data)
     assert rc == 0, f"lem_refshim_status {rc}"
     res = {f: out[k] for k, f in enumerate(OUT)}
     res["fd"], res["sfd"] = codes[0], codes[1]
