@@ -292,6 +292,28 @@ typedef struct lem_tuning {
 lem_status lem_autotune(lem_handle* h, int32_t cycles);
 lem_status lem_get_tuning(lem_handle* h, lem_tuning* out);
 
+/* Asynchronous export of finished grids.  No counterpart in the reference,
+ * whose writegrids (MEM_kernels/io.cpp:201-230) reads host arrays that every
+ * stage copied back synchronously.  lem_dem_export snapshots the given fields
+ * of DEM `id` (0 for a single-grid handle) on the handle's stream -- after the
+ * steps enqueued so far, before any later step or lem_dem_remove changes the
+ * region -- and copies the snapshot to pinned host memory on a second stream,
+ * so the copy overlaps the handle's next steps; it returns at once.
+ * lem_export_ready says whether the copy has finished; lem_export_wait waits
+ * for it, writes field k into host[k] in the types of lem_get_field (a NULL
+ * host[k] skips the field) and releases the export.  Every export must be
+ * waited for, and before lem_destroy (which refuses with LEM_ERR_STATE while
+ * exports are open).  LEM_F_DEM_ROUTED cannot be exported. */
+typedef struct lem_export lem_export;
+lem_status lem_dem_export(lem_handle* h, int32_t id, const lem_field* fields, int32_t nfields, lem_export** out);
+lem_status lem_export_ready(lem_export* e, int32_t* ready);
+lem_status lem_export_wait(lem_export* e, void* const* host);
+
+/* Bytes of device memory the handle holds for its resident state (what an
+ * admission budget counts; exports add their snapshot while in flight).  No
+ * counterpart in the reference. */
+size_t lem_device_bytes(lem_handle* h);
+
 /* Restart snapshot of one DEM's resident state: the DEM, the DEM of the
  * initial climate grids, the mask, the persistent slopes (whose stale entries
  * the next steps read), the seven soil and vegetation fields, the outlet and

@@ -136,7 +136,23 @@ struct lem_handle {
     int sms = 0;                   // SMs of the handle's device
     Tuner tune;
     cudaEvent_t events[16] = {};
+    size_t device_bytes = 0;       // bytes of the handle's resident allocations
+    cudaStream_t side = nullptr;   // exports' device-to-host copies (created on first use)
+    std::vector<std::pair<void*, size_t>> pinned_free;  // exports' pinned host buffers for reuse
+    int exports = 0;               // exports started and not yet waited for
     Launch launch() { return Launch{st, &launches, profiling ? &prof : nullptr}; }
+};
+
+struct lem_export {
+    lem_handle* h = nullptr;
+    int32_t x0 = 0, y0 = 0, w = 0, hgt = 0;  // the DEM's region when the export started
+    std::vector<lem_field> fields;
+    std::vector<size_t> off;               // byte offset of each field's raw copy in the staging
+    size_t mask_off = 0, out_off = 0;      // the region's mask and DemOut (for the direction codes)
+    size_t bytes = 0;
+    void* host = nullptr;                  // pinned staging
+    size_t host_cap = 0;
+    cudaEvent_t done = nullptr;            // the device-to-host copy has finished
 };
 
 namespace {
@@ -147,6 +163,7 @@ lem_status dalloc(lem_handle* h, T** p, size_t count) {
     cudaError_t e = cudaMalloc(&q, sizeof(T) * (count ? count : 1));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc", __FILE__, __LINE__) == LEM_ERR_CUDA ? LEM_ERR_NOMEM : LEM_ERR_NOMEM;
     h->allocs.push_back(q);
+    h->device_bytes += sizeof(T) * (count ? count : 1);
     e = cudaMemsetAsync(q, 0, sizeof(T) * (count ? count : 1), h->st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync", __FILE__, __LINE__);
     *p = static_cast<T*>(q);
@@ -875,7 +892,13 @@ lem_status lem_create(const lem_grid_desc* grid, const lem_params* params, doubl
 
 lem_status lem_destroy(lem_handle* h) {
     if (!h) return LEM_ERR_INVALID;
+    if (h->exports) return LEM_ERR_STATE;  // wait for every export first
     if (h->st) cudaStreamSynchronize(h->st);
+    if (h->side) {
+        cudaStreamSynchronize(h->side);
+        cudaStreamDestroy(h->side);
+    }
+    for (auto& b : h->pinned_free) cudaFreeHost(b.first);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     for (cudaEvent_t e : h->prof.pool) cudaEventDestroy(e);
     for (cudaEvent_t e : h->events)
@@ -1120,6 +1143,218 @@ lem_status lem_dem_get_totals_n(lem_handle* h, const int32_t* ids, int32_t n, le
     for (int32_t k = 1; k < n && r == LEM_OK; ++k) r = totals_from_host(h, ids[k], out + k);
     return r;
 }
+
+// ---- asynchronous exports of one DEM's fields
+
+namespace {
+
+// Bytes per cell of a field's device representation, or 0 when it cannot be exported.
+size_t raw_bytes(lem_field f) {
+    switch (f) {
+        case LEM_F_DEM: return 8;
+        case LEM_F_MASK: case LEM_F_FD: case LEM_F_SFD: case LEM_F_SFD_PASS1: return 1;
+        case LEM_F_CONTRIB: case LEM_F_WATERSHED: return 4;
+        case LEM_F_SLOPES: return 32;
+        case LEM_F_FA: return 8;
+        case LEM_F_DEM_ROUTED: return 0;  // which grid holds it depends on the step's sinks
+        default: return f >= 0 && f < LEM_F_COUNT ? 4 : 0;
+    }
+}
+
+const void* raw_source(lem_handle* h, lem_field f) {
+    DevState& s = h->s;
+    switch (f) {
+        case LEM_F_DEM: return s.z;
+        case LEM_F_MASK: return s.mask;
+        case LEM_F_FD: return s.fd;
+        case LEM_F_SFD: return s.sfd;
+        case LEM_F_SFD_PASS1: return s.sfd1;
+        case LEM_F_CONTRIB: return s.contrib;
+        case LEM_F_WATERSHED: return s.ws;
+        case LEM_F_SLOPES: return s.slopes;
+        case LEM_F_FA: return s.fa;
+        default: return float_field(h, f);
+    }
+}
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+lem_status lem_dem_export(lem_handle* h, int32_t id, const lem_field* fields, int32_t nfields, lem_export** out) {
+    if (!h || !fields || nfields < 1 || !out) return LEM_ERR_INVALID;
+    *out = nullptr;
+    if (h->batch) {
+        if (dem_check(h, id) != LEM_OK) return LEM_ERR_INVALID;
+    } else if (id != 0 || !h->dem_set) {
+        return LEM_ERR_INVALID;
+    }
+    const HostDem& r = h->dems[id];
+    const size_t n = (size_t)r.w * r.h, W = (size_t)h->k.W, cell0 = (size_t)r.y0 * W + r.x0;
+    lem_export* e = new lem_export();
+    e->h = h;
+    e->x0 = r.x0;
+    e->y0 = r.y0;
+    e->w = r.w;
+    e->hgt = r.h;
+    bool codes = false;
+    for (int32_t k = 0; k < nfields; ++k) {
+        const size_t b = raw_bytes(fields[k]);
+        if (!b || !raw_source(h, fields[k])) {
+            delete e;
+            return LEM_ERR_INVALID;
+        }
+        codes |= fields[k] == LEM_F_FD || fields[k] == LEM_F_SFD || fields[k] == LEM_F_SFD_PASS1;
+        e->fields.push_back(fields[k]);
+        e->off.push_back(e->bytes);
+        e->bytes = align256(e->bytes + n * b);
+    }
+    e->mask_off = e->bytes;  // the mask gives codes outside the catchment their -9999
+    if (codes) e->bytes = align256(e->bytes + n);
+    e->out_off = e->bytes;
+    e->bytes = align256(e->bytes + sizeof(DemOut));
+    lem_status st = LEM_OK;
+    void* dstage = nullptr;
+    auto fail = [&](lem_status x) {
+        if (e->done) cudaEventDestroy(e->done);
+        if (e->host) h->pinned_free.emplace_back(e->host, e->host_cap);
+        delete e;
+        return x;
+    };
+    // pinned host staging, reused from earlier exports when one is large enough
+    for (size_t k = 0; k < h->pinned_free.size(); ++k)
+        if (h->pinned_free[k].second >= e->bytes) {
+            e->host = h->pinned_free[k].first;
+            e->host_cap = h->pinned_free[k].second;
+            h->pinned_free.erase(h->pinned_free.begin() + k);
+            break;
+        }
+    if (!e->host) {
+        if (cudaHostAlloc(&e->host, e->bytes, cudaHostAllocDefault) != cudaSuccess) return fail(LEM_ERR_NOMEM);
+        e->host_cap = e->bytes;
+    }
+    if (!h->side && cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "cudaStreamCreate", __FILE__, __LINE__));
+    cudaEvent_t copied = nullptr;
+    cudaError_t ce = cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
+    // a snapshot on the handle's stream (ordered after the steps enqueued so far,
+    // and before any later step or removal touches the region) ...
+    if (ce == cudaSuccess) ce = cudaMallocAsync(&dstage, e->bytes, h->st);
+    for (size_t k = 0; ce == cudaSuccess && k < e->fields.size(); ++k) {
+        const size_t b = raw_bytes(e->fields[k]);
+        const char* src = static_cast<const char*>(raw_source(h, e->fields[k])) + cell0 * b;
+        ce = cudaMemcpy2DAsync(static_cast<char*>(dstage) + e->off[k], r.w * b, src, W * b, r.w * b, r.h,
+                               cudaMemcpyDeviceToDevice, h->st);
+    }
+    if (ce == cudaSuccess && codes)
+        ce = cudaMemcpy2DAsync(static_cast<char*>(dstage) + e->mask_off, r.w, h->s.mask + cell0, W, r.w, r.h,
+                               cudaMemcpyDeviceToDevice, h->st);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(static_cast<char*>(dstage) + e->out_off, h->dem_out + id, sizeof(DemOut),
+                             cudaMemcpyDeviceToDevice, h->st);
+    if (ce == cudaSuccess) ce = cudaEventRecord(copied, h->st);
+    // ... then the device-to-host copy on the side stream, overlapping later steps
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(h->side, copied, 0);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(e->host, dstage, e->bytes, cudaMemcpyDeviceToHost, h->side);
+    if (ce == cudaSuccess) ce = cudaFreeAsync(dstage, h->side);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e->done, h->side);
+    if (copied) cudaEventDestroy(copied);  // released once its record completes
+    if (ce != cudaSuccess) {
+        st = cuda_fail(ce, "lem_dem_export", __FILE__, __LINE__);
+        if (e->done) cudaEventSynchronize(e->done);
+        cudaStreamSynchronize(h->side);
+        return fail(st);
+    }
+    ++h->exports;
+    *out = e;
+    return LEM_OK;
+}
+
+lem_status lem_export_ready(lem_export* e, int32_t* ready) {
+    if (!e || !ready) return LEM_ERR_INVALID;
+    const cudaError_t q = cudaEventQuery(e->done);
+    if (q == cudaErrorNotReady) {
+        *ready = 0;
+        return LEM_OK;
+    }
+    if (q != cudaSuccess) return cuda_fail(q, "cudaEventQuery", __FILE__, __LINE__);
+    *ready = 1;
+    return LEM_OK;
+}
+
+lem_status lem_export_wait(lem_export* e, void* const* host) {
+    if (!e || !host) return LEM_ERR_INVALID;
+    lem_handle* h = e->h;
+    const cudaError_t ce = cudaEventSynchronize(e->done);
+    lem_status st = ce == cudaSuccess ? LEM_OK : cuda_fail(ce, "cudaEventSynchronize", __FILE__, __LINE__);
+    const size_t n = (size_t)e->w * e->hgt;
+    const char* base = static_cast<const char*>(e->host);
+    if (st == LEM_OK) {
+        // the outlet (a grid cell in the staged DemOut) as an index of the DEM's own grid
+        DemOut o;
+        std::memcpy(&o, base + e->out_off, sizeof o);
+        const int64_t W = h->k.W;
+        const int64_t ol = ((int64_t)o.outlet / W - e->y0) * e->w + ((int64_t)o.outlet % W - e->x0);
+        for (size_t k = 0; k < e->fields.size(); ++k) {
+            const lem_field f = e->fields[k];
+            const char* src = base + e->off[k];
+            if (!host[k]) continue;
+            switch (f) {
+                case LEM_F_DEM:
+                    std::memcpy(host[k], src, n * 8);
+                    break;
+                case LEM_F_MASK: {
+                    int32_t* out = static_cast<int32_t*>(host[k]);
+                    for (size_t i = 0; i < n; ++i) out[i] = static_cast<const uint8_t*>((const void*)src)[i];
+                    break;
+                }
+                case LEM_F_FD:
+                case LEM_F_SFD:
+                case LEM_F_SFD_PASS1: {
+                    const uint8_t* c = reinterpret_cast<const uint8_t*>(src);
+                    const uint8_t* m = reinterpret_cast<const uint8_t*>(base + e->mask_off);
+                    int32_t* out = static_cast<int32_t*>(host[k]);
+                    for (size_t i = 0; i < n; ++i) {
+                        int32_t v = m[i] ? (int32_t)c[i] : -9999;          // newflow.cu:74
+                        if (f == LEM_F_FD && (int64_t)i == ol) v = 16;     // routeflow.cu:953
+                        out[i] = v;
+                    }
+                    break;
+                }
+                case LEM_F_CONTRIB:
+                case LEM_F_WATERSHED:
+                    std::memcpy(host[k], src, n * 4);
+                    break;
+                case LEM_F_SLOPES: {
+                    const float* t = reinterpret_cast<const float*>(src);
+                    double* out = static_cast<double*>(host[k]);
+                    for (size_t i = 0; i < 8 * n; ++i) out[i] = t[i];
+                    break;
+                }
+                case LEM_F_FA: {
+                    const float2* t = reinterpret_cast<const float2*>(src);
+                    double* out = static_cast<double*>(host[k]);
+                    for (size_t i = 0; i < n; ++i) out[i] = (double)t[i].x + (double)t[i].y;
+                    break;
+                }
+                default: {
+                    const float* t = reinterpret_cast<const float*>(src);
+                    double* out = static_cast<double*>(host[k]);
+                    for (size_t i = 0; i < n; ++i) out[i] = t[i];
+                    break;
+                }
+            }
+        }
+    }
+    cudaEventDestroy(e->done);
+    h->pinned_free.emplace_back(e->host, e->host_cap);
+    --h->exports;
+    delete e;
+    return st;
+}
+
+size_t lem_device_bytes(lem_handle* h) { return h ? h->device_bytes : 0; }
 
 // ---- restart snapshots of one DEM's resident state
 

@@ -138,6 +138,10 @@ SIGNATURES = {
     "lem_set_limits": (C.c_int, [_H, C.POINTER(Limits)]),
     "lem_autotune": (C.c_int, [_H, C.c_int32]),
     "lem_get_tuning": (C.c_int, [_H, C.c_void_p]),
+    "lem_dem_export": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_int), C.c_int32, C.POINTER(C.c_void_p)]),
+    "lem_export_ready": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "lem_export_wait": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "lem_device_bytes": (C.c_size_t, [_H]),
     "lem_snapshot_bytes": (C.c_size_t, [_H, C.c_int32]),
     "lem_snapshot_save": (C.c_int, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
     "lem_snapshot_load": (C.c_int, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
@@ -158,6 +162,39 @@ def snapshot_save(h, i: int = 0) -> bytes:
 def snapshot_load(h, data: bytes, i: int = 0):
     buf = (C.c_char * len(data)).from_buffer_copy(data)
     _check(load().lem_snapshot_load(h, i, buf, len(data)), "lem_snapshot_load")
+
+class Export:
+    """A DEM's fields on their way to the host (lem_dem_export): the copy runs on
+    the library's second stream while the handle steps on; wait() returns them."""
+
+    def __init__(self, h, i: int, names, shape):
+        self.names = tuple(names)
+        self.shape = shape
+        fields = (C.c_int * len(self.names))(*[FIELDS[f] for f in self.names])
+        e = C.c_void_p()
+        _check(load().lem_dem_export(h, i, fields, len(self.names), C.byref(e)), "lem_dem_export")
+        self.e = e
+
+    def ready(self) -> bool:
+        r = C.c_int32()
+        _check(load().lem_export_ready(self.e, C.byref(r)), "lem_export_ready")
+        return bool(r.value)
+
+    def wait(self) -> dict:
+        hgt, wid = self.shape
+        out = {}
+        for f in self.names:
+            if f in INT_FIELDS:
+                out[f] = np.empty((hgt, wid), np.int32)
+            elif f == "slopes":
+                out[f] = np.empty((hgt, wid, 8), np.float64)
+            else:
+                out[f] = np.empty((hgt, wid), np.float64)
+        ptrs = (C.c_void_p * len(self.names))(*[out[f].ctypes.data for f in self.names])
+        e, self.e = self.e, None
+        _check(load().lem_export_wait(e, ptrs), "lem_export_wait")
+        return out
+
 
 _lib = None
 
@@ -371,6 +408,13 @@ class Batch:
         self.shape[i.value] = (hgt, wid)
         self.place[i.value] = r
         return i.value
+
+    def export(self, i: int, names) -> Export:
+        """Starts the asynchronous copy of DEM i's fields `names` to the host."""
+        return Export(self.h, i, names, self.shape[i])
+
+    def device_bytes(self) -> int:
+        return int(load().lem_device_bytes(self.h))
 
     def remove(self, i: int):
         _check(load().lem_dem_remove(self.h, i), "lem_dem_remove")
