@@ -347,9 +347,11 @@ class EnsembleWork:
                     d2h += self.b.get(k, f).nbytes
         return h2d, d2h
 
-    def plain_sample(self, args, steps=3, budget_s=20.0):
+    def plain_sample(self, args, steps=5, budget_s=25.0):
         """The plain path on the same DEMs, one handle and one grid at a time:
-        every fourth DEM by size (all sizes covered), `steps` timed steps each."""
+        every fourth DEM by size (all sizes covered), each with the batched arm's
+        launch schedule -- CUDA-graph steps and the autotuner (lem_autotune(1):
+        5 tuning steps) -- then 2 warm-up and `steps` device-timed steps."""
         lem = self.lem
         from parallem_gb300 import scenario as S
         order = sorted(range(len(self.ens)), key=lambda i: self.ens[i].dem.size)
@@ -363,11 +365,17 @@ class EnsembleWork:
             st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
             m = lem.Model(sc.dem, 30.0, sc.init_rain, sc.init_temp)
             m.set_state(st)
-            m.step(sc.rain[0], sc.temp[0], True)
+            m.graphs(not args.no_graphs)
+            m.autotune(1)
+            k = 0
+            for _ in range(5 + 2):  # tuning, then warm-up steps
+                m.step(sc.rain[k % len(sc.rain)], sc.temp[k % len(sc.temp)], True)
+                k += 1
             m.synchronize()
             m.record(0)
-            for s in range(1, 1 + steps):
-                m.step(sc.rain[s], sc.temp[s], True)
+            for _ in range(steps):
+                m.step(sc.rain[k % len(sc.rain)], sc.temp[k % len(sc.temp)], True)
+                k += 1
             m.record(1)
             secs += m.elapsed_ms(0, 1) / 1e3
             cells += int((st["mask"] == 1).sum()) * steps
@@ -376,8 +384,8 @@ class EnsembleWork:
             if time.perf_counter() - t_start > budget_s:
                 break
         return {"value": cells / secs, "unit": "cell-timesteps/s",
-                "sample": f"{done} of the {len(self.ens)} DEMs (every fourth by size), each on its own handle, "
-                          f"{steps} device-timed steps each"}
+                "sample": f"{done} of the {len(self.ens)} DEMs (every fourth by size), each on its own handle with "
+                          f"graph steps and its own autotuned schedule, {steps} device-timed steps each"}
 
     def config(self, args):
         sides = sorted(x.dem.shape[0] for x in self.ens)
@@ -387,6 +395,61 @@ class EnsembleWork:
 
     def close(self):
         self.b.close()
+
+
+def grid_sample(args, steps=5):
+    """The plain path on the single large grid (4096x4096, per-step climate):
+    graph steps, the autotuner's 13 steps, 3 warm-up steps, `steps` timed."""
+    from parallem_gb300 import lem
+    from parallem_gb300 import scenario as S
+    sc = S.config_large(2, n=4096, steps=100)
+    st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+    cells = int((st["mask"] == 1).sum())
+    g = lem.Model(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+    g.set_state(st)
+    g.graphs(True)
+    g.autotune(3)
+    k = 0
+    for _ in range(13 + 3):
+        g.step(sc.rain[k], sc.temp[k], True)
+        k += 1
+    g.synchronize()
+    g.record(0)
+    for _ in range(steps):
+        g.step(sc.rain[k], sc.temp[k], True)
+        k += 1
+    g.record(1)
+    ms = g.elapsed_ms(0, 1) / steps
+    g.close()
+    return {"workload": "single large grid 4096x4096, per-step climate series (the plain path)",
+            "value": cells / (ms / 1e3), "unit": "cell-timesteps/s", "ms_per_step": ms, "active_cells": cells,
+            "steps": steps}
+
+
+def serve_sample(rate=20.0, requests=24, canvas=(16384, 12288), budget_gb=150.0):
+    """The serving workload at one arrival rate: Poisson arrivals, sides
+    log-uniform in [128, 4096], 10-500 steps, own climate series, continuously
+    batched under the HBM budget; p50/p99 latency from arrival to the result
+    grids on the host."""
+    from parallem_gb300 import serve as SV
+    rng = np.random.default_rng(11)
+    t = 0.0
+    reqs = []
+    for i in range(requests):
+        t += float(rng.exponential(1.0 / rate))
+        reqs.append(SV.make_request(i, rng, t))
+    srv = SV.Server(canvas[0], canvas[1], budget_bytes=budget_gb * 1e9, max_dems=max(64, requests))
+    warm = SV.make_request(-1, np.random.default_rng(1), 0.0, side_lo=128, side_hi=256, steps_lo=3, steps_hi=3)
+    srv.run([warm])
+    srv.steps_run = 0
+    stats = srv.run(reqs)
+    srv.close()
+    return {"workload": "serving: Poisson arrivals, sides log-uniform in [128, 4096], 10-500 steps",
+            "rate_per_s": rate, "requests": stats["requests"], "refused": stats["refused"],
+            "p50_latency_s": stats["p50_latency_s"], "p99_latency_s": stats["p99_latency_s"],
+            "value": stats["cell_timesteps_per_s"], "unit": "cell-timesteps/s", "wall_s": stats["wall_s"],
+            "batch_steps": stats["batch_steps"], "hbm_budget_gb": budget_gb,
+            "bytes_per_canvas_cell": stats["bytes_per_cell"]}
 
 
 def run_serve(args):
@@ -452,6 +515,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path sample of the ensemble")
     ap.add_argument("--no-graphs", action="store_true", help="step eagerly instead of one CUDA graph per step")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch schedule (no autotuning steps)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="ensemble: skip the 4096x4096 plain-path and serving samples")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -589,8 +654,13 @@ def main():
     if plain is not None:
         line["plain"] = plain
         line["batched_over_plain"] = value / plain["value"]
-    print(json.dumps(line))
     work.close()
+    if args.workload == "ensemble" and not args.no_extras and world == 1:
+        # the other two workloads, measured in the same run: the single large
+        # grid on the plain path and serving at 20 requests/s
+        line["grid_4096"] = grid_sample(args)
+        line["serving"] = serve_sample()
+    print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
     return 0
