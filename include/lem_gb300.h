@@ -274,9 +274,10 @@ lem_status lem_set_limits(lem_handle* h, const lem_limits* limits);
 /* Autotuner of the launch schedule (no counterpart in the reference).  The
  * handle's next 1 + 4 * cycles steps (lem_step or lem_step_batch; real steps
  * of the model, launched eagerly) run the cooperative kernels with 1, 2 and 4
- * blocks per SM and with all their co-resident blocks in turn, and time them
- * with events; afterwards each keeps the block count with the lowest mean
- * time if it beats the default by more than 3 %.  The default, also before
+ * blocks per SM and with all their co-resident blocks in turn, and the
+ * flow-direction kernel with TMA tiles of 8, 16, 32 and 8 rows, and time them
+ * with events; afterwards each keeps the block count (the tile shape) with the
+ * lowest mean time if it beats the default by more than 3 %.  The default, also before
  * any tuning, is the block count every cooperative kernel can hold at once.  Results are the same under every block count.  LEM_ERR_STATE while
  * profiling is on (and lem_set_profiling and lem_profile_read return it while
  * tuning). */
@@ -288,6 +289,10 @@ typedef struct lem_tuning {
     int32_t coop_blocks[LEM_TUNE_COOP];     /* blocks each cooperative kernel launches with    */
     double default_ms;                      /* ms per step of these kernels, default schedule  */
     double tuned_ms;                        /*   and with the schedule kept (as measured)       */
+    int32_t flowdirs_tile_rows;             /* rows of the flow-direction kernel's 32-column TMA
+                                               tiles (8, 16 or 32); 0: plain loads (grid width
+                                               not a multiple of 16)                             */
+    int32_t pad;
 } lem_tuning;
 lem_status lem_autotune(lem_handle* h, int32_t cycles);
 lem_status lem_get_tuning(lem_handle* h, lem_tuning* out);

@@ -84,6 +84,9 @@ constexpr int kTuneCands = 4;
 constexpr int kTuneBlocksPerSm[kTuneCands] = {1, 2, 4, 0};  // 0: every co-resident block
 constexpr int kTuneDefault = 2;
 constexpr double kTuneMargin = 0.97;  // a candidate replaces the default only below 97 % of its time
+// The flow-direction kernel's tile shape tried in each candidate step (an
+// index into kFdRows); the default shape is candidate kTuneDefault's.
+constexpr int kTuneFdShape[kTuneCands] = {0, 1, 2, 0};
 const char* const kCoopNames[kCoopKernels] = {"k_plateau_relax", "k_flood_merge", "k_flood_jump", "k_flood_spill",
                                               "k_fat_coarse",    "k_fa_walk",     "k_sedt_coarse", "k_sed_walk"};
 struct Tuner {
@@ -91,6 +94,7 @@ struct Tuner {
     int step = -1;  // tuning step (-1: the unmeasured first one)
     int steps = 0;  // measured steps in all
     double coop_ms[kCoopKernels][kTuneCands] = {};  // device ms, summed over the steps of each candidate
+    double fd_ms[kTuneCands] = {};                  // the flow-direction kernel, by candidate tile shape
     int coop_n[kTuneCands] = {};
     double default_ms = 0, tuned_ms = 0;
 };
@@ -136,6 +140,7 @@ struct lem_handle {
     int sms = 0;                   // SMs of the handle's device
     Tuner tune;
     cudaEvent_t events[16] = {};
+    FdTmaMaps fd_maps{};           // tensor maps of the TMA flow-direction kernel (when s.fd_tma is set)
     size_t device_bytes = 0;       // bytes of the handle's resident allocations
     cudaStream_t side = nullptr;   // exports' device-to-host copies (created on first use)
     std::vector<std::pair<void*, size_t>> pinned_free;  // exports' pinned host buffers for reuse
@@ -742,6 +747,11 @@ lem_status create_common(const lem_grid_desc* grid, const lem_params* params, in
         s.coop_blocks[i] = std::min(s.coop_cap[i], blocks);  // untuned: the blocks every one of them can hold
     }
     cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device);
+    // the flow-direction tiles move by TMA where the grid's rows allow it
+    s.fd_tma = nullptr;
+    s.fd_rows = kTuneFdShape[kTuneDefault];
+    if (fd_tma_setup(s, k, &h->fd_maps) == LEM_OK) s.fd_tma = &h->fd_maps;
+    cudaGetLastError();  // a grid the maps cannot describe keeps the plain-load kernel
     *out = h;
     return LEM_OK;
 }
@@ -779,6 +789,7 @@ void tune_apply(lem_handle* h) {
     const Tuner& t = h->tune;
     const int c = t.step < 0 ? kTuneDefault : t.step % kTuneCands;
     for (int i = 0; i < kCoopKernels; ++i) h->s.coop_blocks[i] = coop_blocks_of(h, i, c);
+    h->s.fd_rows = kTuneFdShape[c];
 }
 
 // Books the kernel times of a tuning step; after the last one, keeps for every
@@ -791,9 +802,11 @@ lem_status tune_record(lem_handle* h) {
     if (r != LEM_OK) return r;
     if (t.step >= 0) {
         const int c = t.step % kTuneCands;
-        for (const lem_kernel_stat& st : agg)
+        for (const lem_kernel_stat& st : agg) {
             for (int i = 0; i < kCoopKernels; ++i)
                 if (!std::strcmp(st.name, kCoopNames[i])) t.coop_ms[i][c] += st.total_ms;
+            if (!std::strcmp(st.name, "k_flowdirs")) t.fd_ms[c] += st.total_ms;
+        }
         t.coop_n[c] += 1;
     }
     if (++t.step < t.steps) return LEM_OK;
@@ -808,6 +821,14 @@ lem_status tune_record(lem_handle* h) {
         t.default_ms += t.coop_ms[i][def] / t.coop_n[def];
         t.tuned_ms += t.coop_ms[i][best] / t.coop_n[best];
     }
+    // the flow-direction tile shape: the fastest, unless the default is within the margin
+    int fbest = def;
+    for (int c = 0; c < kTuneCands; ++c)
+        if (t.fd_ms[c] / t.coop_n[c] < t.fd_ms[fbest] / t.coop_n[fbest]) fbest = c;
+    if (t.fd_ms[fbest] / t.coop_n[fbest] > kTuneMargin * t.fd_ms[def] / t.coop_n[def]) fbest = def;
+    h->s.fd_rows = kTuneFdShape[fbest];
+    t.default_ms += t.fd_ms[def] / t.coop_n[def];
+    t.tuned_ms += t.fd_ms[fbest] / t.coop_n[fbest];
     t.state = 2;
     h->profiling = false;
     if (h->gexec) {  // captured with other launch arguments
@@ -1513,6 +1534,7 @@ lem_status lem_get_tuning(lem_handle* h, lem_tuning* out) {
     for (int i = 0; i < kCoopKernels; ++i) out->coop_blocks[i] = h->s.coop_blocks[i];
     out->default_ms = h->tune.default_ms;
     out->tuned_ms = h->tune.tuned_ms;
+    out->flowdirs_tile_rows = h->s.fd_tma ? kFdRows[h->s.fd_rows] : 0;
     return LEM_OK;
 }
 

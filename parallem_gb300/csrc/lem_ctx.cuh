@@ -1,6 +1,8 @@
 // lem_ctx.cuh -- resident device state of one grid and the stage launchers.
 #pragma once
 
+#include <cuda.h>
+
 #include "lem_common.cuh"
 
 namespace lem {
@@ -39,6 +41,19 @@ struct ModelConsts {  // per-handle constants derived on the host in double
 enum CoopKernel { kCkPlateau = 0, kCkMerge, kCkJump, kCkSpill, kCkFatCoarse, kCkFaWalk, kCkSedCoarse, kCkSedWalk,
                   kCoopKernels };
 
+
+// Tile shapes of the TMA flow-direction kernel (rows of a 32-column strip),
+// chosen per handle by the autotuner.
+constexpr int kFdShapes = 3;
+constexpr int kFdRows[kFdShapes] = {8, 16, 32};
+
+// Tensor maps of the TMA flow-direction kernel, one set per tile shape: the
+// elevations of both passes, the mask and the persistent slopes (host memory
+// of the handle; passed to the kernels by value).
+struct FdTmaMaps {
+    CUtensorMap z[kFdShapes], zf[kFdShapes], mask[kFdShapes], slopes[kFdShapes];
+    int blocks[kFdShapes];  // co-resident blocks of each shape's kernel on the device
+};
 
 struct DevState {
     // grids
@@ -115,6 +130,8 @@ struct DevState {
     int32_t max_coop_blocks;    // co-resident blocks of the cooperative kernels
     int32_t coop_blocks[kCoopKernels];  // blocks each cooperative kernel launches with (<= its coop_cap)
     int32_t coop_cap[kCoopKernels];     // co-resident blocks of each cooperative kernel
+    const FdTmaMaps* fd_tma;    // host: the TMA flow-direction kernel's maps (null: rows TMA cannot address)
+    int32_t fd_rows;            // its tile shape, an index into kFdRows
 };
 
 // The tiles a canvas-wide kernel visits: in a batch grid the 32x32 tiles that
@@ -260,5 +277,8 @@ lem_status launch_flow_accumulation(const DevState& s, const ModelConsts& k, uin
 lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flags,
                           const Launch& L);
 int coop_blocks_for(const void* kernel, int threads, size_t smem);
+// Encodes the TMA flow-direction kernel's tensor maps for the state's grids
+// (rows must be multiples of 16 bytes: width a multiple of 16).
+lem_status fd_tma_setup(const DevState& s, const ModelConsts& k, FdTmaMaps* maps);
 
 }  // namespace lem

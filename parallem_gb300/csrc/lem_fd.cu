@@ -10,6 +10,9 @@
 #include <cooperative_groups.h>
 
 #include "lem_ctx.cuh"
+#include "lem_tma.cuh"
+
+#include <cudaTypedefs.h>
 
 namespace cg = cooperative_groups;
 
@@ -71,18 +74,180 @@ __device__ __forceinline__ void set_slope(float4& a, float4& b, int d, float v) 
 }
 
 // --------------------------------------------------------------------------
-// FlowDirs (newflow.cu:49-174) on a 32x8 tile with a one-cell halo in shared
-// memory.  Pass 1 writes the downslope slopes into the persistent 8-per-cell
-// array (other entries keep their stale values, newflow.cu:126-140) and the
-// sink/flat counters and lowest elevation; pass 2 writes codes only.
+// FlowDirs (newflow.cu:49-174) of one cell from its 3x3 neighbourhood staged in
+// shared memory: elevation keys (0 = outside the grid or NaN, never compared)
+// and the fp32 head/tail split of each elevation, at pitch P.  sa/sb hold the
+// cell's persistent slopes; the downslope entries are replaced (the others
+// keep their stale values, newflow.cu:126-140) and *touched says whether any
+// was.
+struct FdCell {
+    uint8_t cs = kMaskedCode, cm = kMaskedCode;  // SFD and MFD codes
+    int is_sink = 0, is_flat = 0;
+    bool is_cand = false, has_equal = false;
+    unsigned long long low = ~0ull;             // the cell's key when it is in the catchment
+};
+
+template <int P>
+__device__ __forceinline__ FdCell fd_cell(const unsigned long long* __restrict__ skey, const float* __restrict__ shi,
+                                         const float* __restrict__ slo, int li, bool mk, float4& sa, float4& sb,
+                                         bool* touched, const ModelConsts& k) {
+    FdCell o;
+    *touched = false;
+    if (mk) o.cs = o.cm = 0;  // a NaN elevation compares false with every neighbour: no direction
+    if (mk && skey[li] != 0) {
+        const unsigned long long ks = skey[li];
+        const unsigned long long knd = key_nodata();
+        const float hs = shi[li], ls = slo[li];
+        // the fp32 estimate of the slope towards d (from the head/tail split of z)
+        auto nb = [&](int d) { return li + dir_dy(d) * P + dir_dx(d); };
+        auto est = [&](int d) { return ((hs - shi[nb(d)]) + (ls - slo[nb(d)])) * k.inv_len[d]; };
+        o.low = ks;
+        int up = 0, flat = 0;
+        uint32_t aspect = 0, cand = 0;
+        int bestd = -1;
+        float best = -1.0f, second = -1.0f, smin = 3.0e38f;
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+            const unsigned long long kn = skey[nb(d)];
+            if (kn == 0) continue;
+            if (ks < kn) up += 1;
+            if (ks == kn) flat += 1;
+            if (ks > kn && kn != knd) {
+                const float s = est(d);
+                set_slope(sa, sb, d, s);  // kept unless the fp64 arithmetic below replaces it
+                cand |= 1u << d;
+                aspect |= dir_bit(d);
+                smin = fminf(smin, s);
+                if (s > best) {
+                    second = best;
+                    best = s;
+                    bestd = d;
+                } else if (s > second) {
+                    second = s;
+                }
+            }
+        }
+        o.has_equal = flat > 0;
+        if (cand) {
+            // certify the steepest direction against the exact fp64 quotients
+            const float zs_mag = fabsf(hs);
+            const float inv_b = (bestd & 1) ? k.inv_len[1] : k.inv_len[0];  // the length depends on d's parity
+            const float err_b = best * 1.0e-6f + fmaxf(zs_mag, 1.0f) * 1.0e-12f * inv_b;
+            // Quick test with the largest per-direction error (the axial one):
+            // every drop far above the split error and the runner-up clearly
+            // below the best certify every direction, since the per-direction
+            // tests below are monotone in the estimate and in the error.
+            const float abs_max = fmaxf(zs_mag, 1.0f) * 1.0e-12f * fmaxf(k.inv_len[0], k.inv_len[1]);
+            bool certain = !(smin < 1.0e5f * abs_max) &&
+                           (second < 0.0f || second + (second * 1.0e-6f + abs_max) < best - err_b);
+            if (!certain) {  // the full test, direction by direction
+                certain = true;
+                const unsigned long long kb = skey[nb(bestd)];
+#pragma unroll
+                for (int d = 0; d < 8; ++d) {
+                    if (!((cand >> d) & 1u)) continue;
+                    const float sd = est(d);
+                    const float abs_d = fmaxf(zs_mag, 1.0f) * 1.0e-12f * k.inv_len[d];
+                    // a drop close to the split error of z: the estimate is not
+                    // within 1e-7 of the reference's slope (and may even round to 0,
+                    // while the reference stores a positive slope that aveslope counts)
+                    if (sd < 1.0e5f * abs_d) certain = false;
+                    if (d == bestd) continue;
+                    const float err_d = sd * 1.0e-6f + abs_d;
+                    if (sd + err_d < best - err_b) continue;
+                    if (((d ^ bestd) & 1) == 0 && skey[nb(d)] == kb && d > bestd) continue;  // exact tie
+                    certain = false;
+                }
+            }
+            if (!certain) {
+                // the reference's arithmetic (newflow.cu:117,130-135)
+                const double zs = dkey_inv(ks);
+                double smax = 0.0;
+                bestd = -1;
+#pragma unroll
+                for (int d = 0; d < 8; ++d) {
+                    if (!((cand >> d) & 1u)) continue;
+                    const double st = (zs - dkey_inv(skey[nb(d)])) / k.len[d];
+                    set_slope(sa, sb, d, (float)st);
+                    if (st > smax) {
+                        smax = st;
+                        bestd = d;
+                    }
+                }
+            }
+            *touched = true;
+        }
+        uint32_t asfd = bestd >= 0 ? dir_bit(bestd) : 0u;
+        if (up > 7) {
+            o.is_sink = 1;
+            aspect = asfd = 0;
+        }
+        if (flat + up > 7 && up <= 7) {
+            o.is_flat = 1;
+            aspect = asfd = 0;
+        }
+        o.cs = (uint8_t)asfd;
+        o.cm = (uint8_t)aspect;
+    }
+    // the plateau candidates (newflow.cu:234-350): masked-in cells with no
+    // downslope direction start at distance 2e7, every other cell at 0
+    o.is_cand = mk && o.cs == 0 && o.cm == 0;
+    return o;
+}
+
+// The staged form of one elevation: its order-preserving key and fp32 split
+// (0 outside the grid, which is never compared).
+__device__ __forceinline__ void fd_stage(double v, bool in_grid, unsigned long long& key, float& hi, float& lo) {
+    key = 0;
+    hi = lo = 0.f;
+    if (in_grid) {
+        key = dkey(v);
+        dsplit(v, hi, lo);
+    }
+}
+
+// The block's sink and flat counts and lowest cell into its DEM's counters
+// (pass 1; a block's cells lie in one DEM), one atomic each.
+__device__ __forceinline__ void fd_counters(int is_sink, int is_flat, unsigned long long low, int dem_of_warp,
+                                            DemCtx dc, int* s_sinks, int* s_flats, unsigned long long* s_low,
+                                            int* s_dem) {
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    if (tid == 0) {
+        *s_sinks = *s_flats = 0;
+        *s_low = ~0ull;
+        *s_dem = -1;
+    }
+    __syncthreads();
+    const int s1 = warp_sum(is_sink), f1 = warp_sum(is_flat);
+    low = warp_min_u64(low);
+    if ((tid & 31) == 0) {
+        if (s1) atomicAdd(s_sinks, s1);
+        if (f1) atomicAdd(s_flats, f1);
+        if (low != ~0ull) atomicMin(s_low, low);
+        if (dem_of_warp >= 0) atomicMax(s_dem, dem_of_warp);
+    }
+    __syncthreads();
+    if (tid == 0 && *s_dem >= 0) {
+        DemOut& o = dc.out[*s_dem];
+        if (*s_sinks) atomicAdd(&o.sink_counter, *s_sinks);
+        if (*s_flats) atomicAdd(&o.flat_counter, *s_flats);
+        if (*s_low != ~0ull) atomicMin(&o.lowest_key, *s_low);
+    }
+}
+
+// FlowDirs on a 32x8 tile with a one-cell halo staged by plain loads (grids
+// whose rows TMA cannot address: width not a multiple of 16).  Pass 1 writes
+// the downslope slopes into the persistent 8-per-cell array and the sink/flat
+// counters and lowest elevation; pass 2 writes codes only.
 __global__ void __launch_bounds__(FD_BX* FD_BY)
     k_flowdirs(const double* __restrict__ z, const uint8_t* __restrict__ mask, float* __restrict__ slopes,
                uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, float* __restrict__ sp, int32_t* plateau,
                ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts, int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
-    __shared__ unsigned long long skey[FD_BY + 2][FD_BX + 2];
-    __shared__ float shi[FD_BY + 2][FD_BX + 2];
-    __shared__ float slo[FD_BY + 2][FD_BX + 2];
+    constexpr int P = FD_BX + 2;
+    __shared__ unsigned long long skey[(FD_BY + 2) * P];
+    __shared__ float shi[(FD_BY + 2) * P];
+    __shared__ float slo[(FD_BY + 2) * P];
     __shared__ int s_cnt[FD_BX * FD_BY / 32 + 1];
     __shared__ int s_sinks, s_flats, s_dem;
     __shared__ unsigned long long s_low;
@@ -91,7 +256,6 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     const int x0 = (t % ts.tw) * kTile, y0 = (t / ts.tw) * kTile + blockIdx.y * FD_BY;
     const int tid = threadIdx.y * FD_BX + threadIdx.x;
     const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
-    const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
     const bool inb = x < W && y < H;
     const size_t self = (size_t)y * W + x;
     const uint8_t mk = inb ? mask[self] : 0;
@@ -102,166 +266,180 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
         sa = sp4[0];
         sb = sp4[1];
     }
-    for (int t = tid; t < (FD_BX + 2) * (FD_BY + 2); t += FD_BX * FD_BY) {
-        int ly = t / (FD_BX + 2), lx = t % (FD_BX + 2);
-        int gx = x0 + lx - 1, gy = y0 + ly - 1;
-        unsigned long long key = 0;  // 0 = outside the grid or NaN: never compared
-        float hi = 0.f, lo = 0.f;
-        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-            double v = z[(size_t)gy * W + gx];
-            key = dkey(v);
-            dsplit(v, hi, lo);
-        }
-        skey[ly][lx] = key;
-        shi[ly][lx] = hi;
-        slo[ly][lx] = lo;
+    for (int e = tid; e < (FD_BX + 2) * (FD_BY + 2); e += FD_BX * FD_BY) {
+        const int ly = e / P, lx = e % P;
+        const int gx = x0 + lx - 1, gy = y0 + ly - 1;
+        const bool g = gx >= 0 && gx < W && gy >= 0 && gy < H;
+        fd_stage(g ? z[(size_t)gy * W + gx] : 0.0, g, skey[e], shi[e], slo[e]);
     }
     __syncthreads();
-
-    int is_sink = 0, is_flat = 0;
-    bool is_cand = false, has_equal = false;
-    unsigned long long low = ~0ull;
+    FdCell c;
     if (inb) {
-        uint8_t cs = kMaskedCode, cm = kMaskedCode;
-        if (mk) {
-            cs = cm = 0;  // a NaN elevation compares false with every neighbour: no direction
+        bool touched = false;
+        c = fd_cell<P>(skey, shi, slo, (threadIdx.y + 1) * P + threadIdx.x + 1, mk != 0, sa, sb, &touched, k);
+        if (sp4 && touched) {
+            sp4[0] = sa;
+            sp4[1] = sb;
         }
-        if (mk && skey[ly][lx] != 0) {
-            const unsigned long long ks = skey[ly][lx];
-            const unsigned long long knd = key_nodata();
-            const float hs = shi[ly][lx], ls = slo[ly][lx];
-            // the fp32 estimate of the slope towards d (from the head/tail split of z)
-            auto est = [&](int d) {
-                return ((hs - shi[ly + dir_dy(d)][lx + dir_dx(d)]) + (ls - slo[ly + dir_dy(d)][lx + dir_dx(d)])) *
-                       k.inv_len[d];
-            };
-            low = ks;
-            int up = 0, flat = 0;
-            uint32_t aspect = 0, cand = 0;
-            int bestd = -1;
-            float best = -1.0f, second = -1.0f, smin = 3.0e38f;
-#pragma unroll
-            for (int d = 0; d < 8; ++d) {
-                const unsigned long long kn = skey[ly + dir_dy(d)][lx + dir_dx(d)];
-                if (kn == 0) continue;
-                if (ks < kn) up += 1;
-                if (ks == kn) flat += 1;
-                if (ks > kn && kn != knd) {
-                    const float s = est(d);
-                    set_slope(sa, sb, d, s);  // kept unless the fp64 arithmetic below replaces it
-                    cand |= 1u << d;
-                    aspect |= dir_bit(d);
-                    smin = fminf(smin, s);
-                    if (s > best) {
-                        second = best;
-                        best = s;
-                        bestd = d;
-                    } else if (s > second) {
-                        second = s;
-                    }
-                }
-            }
-            has_equal = flat > 0;
-            if (cand) {
-                // certify the steepest direction against the exact fp64 quotients
-                const float zs_mag = fabsf(hs);
-                const float inv_b = (bestd & 1) ? k.inv_len[1] : k.inv_len[0];  // the length depends on d's parity
-                const float err_b = best * 1.0e-6f + fmaxf(zs_mag, 1.0f) * 1.0e-12f * inv_b;
-                // Quick test with the largest per-direction error (the axial one):
-                // every drop far above the split error and the runner-up clearly
-                // below the best certify every direction, since the per-direction
-                // tests below are monotone in the estimate and in the error.
-                const float abs_max = fmaxf(zs_mag, 1.0f) * 1.0e-12f * fmaxf(k.inv_len[0], k.inv_len[1]);
-                bool certain = !(smin < 1.0e5f * abs_max) &&
-                               (second < 0.0f || second + (second * 1.0e-6f + abs_max) < best - err_b);
-                if (!certain) {  // the full test, direction by direction
-                    certain = true;
-                    const unsigned long long kb = skey[ly + dir_dy(bestd)][lx + dir_dx(bestd)];
-#pragma unroll
-                    for (int d = 0; d < 8; ++d) {
-                        if (!((cand >> d) & 1u)) continue;
-                        const float sd = est(d);
-                        const float abs_d = fmaxf(zs_mag, 1.0f) * 1.0e-12f * k.inv_len[d];
-                        // a drop close to the split error of z: the estimate is not
-                        // within 1e-7 of the reference's slope (and may even round to 0,
-                        // while the reference stores a positive slope that aveslope counts)
-                        if (sd < 1.0e5f * abs_d) certain = false;
-                        if (d == bestd) continue;
-                        const float err_d = sd * 1.0e-6f + abs_d;
-                        if (sd + err_d < best - err_b) continue;
-                        if (((d ^ bestd) & 1) == 0 && skey[ly + dir_dy(d)][lx + dir_dx(d)] == kb && d > bestd)
-                            continue;  // exact tie
-                        certain = false;
-                    }
-                }
-                if (!certain) {
-                    // the reference's arithmetic (newflow.cu:117,130-135)
-                    const double zs = dkey_inv(ks);
-                    double smax = 0.0;
-                    bestd = -1;
-#pragma unroll
-                    for (int d = 0; d < 8; ++d) {
-                        if (!((cand >> d) & 1u)) continue;
-                        const double st = (zs - dkey_inv(skey[ly + dir_dy(d)][lx + dir_dx(d)])) / k.len[d];
-                        set_slope(sa, sb, d, (float)st);
-                        if (st > smax) {
-                            smax = st;
-                            bestd = d;
-                        }
-                    }
-                }
-                if (sp4) {
-                    sp4[0] = sa;
-                    sp4[1] = sb;
-                }
-            }
-            uint32_t asfd = bestd >= 0 ? dir_bit(bestd) : 0u;
-            if (up > 7) {
-                is_sink = 1;
-                aspect = asfd = 0;
-            }
-            if (flat + up > 7 && up <= 7) {
-                is_flat = 1;
-                aspect = asfd = 0;
-            }
-            cs = (uint8_t)asfd;
-            cm = (uint8_t)aspect;
-        }
-        sfd[self] = cs;
-        mfd[self] = cm;
-        // the plateau candidates (newflow.cu:234-350): masked-in cells with no
-        // downslope direction start at distance 2e7, every other cell at 0
-        is_cand = mk && cs == 0 && cm == 0;
-        sp[self] = is_cand ? kFar : 0.f;
+        sfd[self] = c.cs;
+        mfd[self] = c.cm;
+        sp[self] = c.is_cand ? kFar : 0.f;
     }
     // Only a candidate with an equal-height neighbour can be routed: the others
     // (single-cell pits, NaN cells) keep 2e7 and no direction, and stay off
     // the list the relaxation and the final directions work through.
-    block_append(is_cand && has_equal, (int32_t)self, plateau, &sc->n_cand, (int)((size_t)W * H), &sc->err, s_cnt);
-    if (pass == 1) {
-        // the block's counters and lowest cell, one atomic each (a block lies in one DEM)
-        if (tid == 0) {
-            s_sinks = s_flats = 0;
-            s_low = ~0ull;
-            s_dem = -1;
+    block_append(c.is_cand && c.has_equal, (int32_t)self, plateau, &sc->n_cand, (int)((size_t)W * H), &sc->err,
+                 s_cnt);
+    if (pass == 1)
+        fd_counters(c.is_sink, c.is_flat, c.low, warp_dem(dc, self, mk != 0), dc, &s_sinks, &s_flats, &s_low,
+                    &s_dem);
+}
+
+// ---------------------------------------------------------------------------
+// FlowDirs with the tile moved by the Tensor Memory Accelerator.  A persistent
+// grid of 32x8-thread blocks takes strips of 32 x ROWS cells (ROWS = 8, 16 or
+// 32: the autotuned tile shape); each thread owns ROWS / 8 cells of a column.
+// Per strip three tensor copies land in shared memory and complete on one
+// mbarrier: the elevations with a one-cell halo (a 36 x (ROWS + 2) box of
+// doubles from x0 - 2, so the inner coordinate stays 16-byte aligned; cells
+// outside the grid read as zero and are masked by their coordinates), the mask
+// (32 x ROWS bytes) and, in pass 1, the persistent slopes (ROWS rows of 256
+// floats).  Two stages: the next strip's copies are issued before the current
+// strip is computed, so they overlap its arithmetic and stores.
+template <int ROWS>
+struct FdTma {
+    static constexpr int kBoxW = kTile + 4;          // doubles per elevation box row
+    static constexpr int kStageW = kTile + 2;        // staged keys per row (pitch)
+    static constexpr int kZBytes = kBoxW * (ROWS + 2) * 8;
+    static constexpr int kMBytes = kTile * ROWS;
+    static constexpr int kSBytes = 8 * kTile * ROWS * 4;
+    static constexpr int kZOff = 0;
+    static constexpr int kMOff = (kZBytes + 127) / 128 * 128;
+    static constexpr int kSOff = kMOff + (kMBytes + 127) / 128 * 128;
+    static constexpr int kStage = kSOff + kSBytes;   // bytes per pipeline stage (a multiple of 128)
+    static constexpr int kKeys = kStageW * (ROWS + 2);
+    static constexpr int kSmem = 2 * kStage + kKeys * 16 + 256;
+    static_assert(kStage % 128 == 0, "stages stay 128-byte aligned");
+};
+
+constexpr uint32_t kTmaSpin = 1u << 20;  // mbarrier polls before a wait gives up
+
+template <int ROWS>
+__global__ void __launch_bounds__(FD_BX* FD_BY)
+    k_flowdirs_tma(const __grid_constant__ CUtensorMap tm_z, const __grid_constant__ CUtensorMap tm_mask,
+                   const __grid_constant__ CUtensorMap tm_slopes, float* __restrict__ slopes,
+                   uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, float* __restrict__ sp, int32_t* plateau,
+                   ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts, int pass) {
+    using L = FdTma<ROWS>;
+    constexpr int SPT = kTile / ROWS;  // strips per tile
+    constexpr int P = L::kStageW;
+    if (pass == 2 && sc->sinkcount_pass1 == 0) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ int s_cnt[FD_BX * FD_BY / 32 + 1];
+    __shared__ int s_sinks, s_flats, s_dem;
+    __shared__ unsigned long long s_low;
+    unsigned long long* skey = reinterpret_cast<unsigned long long*>(smem + 2 * L::kStage);
+    float* shi = reinterpret_cast<float*>(smem + 2 * L::kStage + L::kKeys * 8);
+    float* slo = shi + L::kKeys;
+    const int W = k.W, H = k.H;
+    const int tid = threadIdx.y * FD_BX + threadIdx.x;
+    const int n_items = ts.n * SPT;
+    const bool with_slopes = pass == 1 && slopes != nullptr;
+    const uint32_t tx_bytes = L::kZBytes + L::kMBytes + (with_slopes ? L::kSBytes : 0);
+    auto origin = [&](int item, int& x0, int& y0) {
+        const int t = ts.tile(item / SPT);
+        x0 = (t % ts.tw) * kTile;
+        y0 = (t / ts.tw) * kTile + (item % SPT) * ROWS;
+    };
+    // one thread issues a strip's copies into a stage
+    auto issue = [&](int item, int st) {
+        int x0, y0;
+        origin(item, x0, y0);
+        unsigned char* base = smem + st * L::kStage;
+        mbar_arrive_expect_tx(&s_bar[st], tx_bytes);
+        tma_load_2d(base + L::kZOff, &tm_z, x0 - 2, y0 - 1, &s_bar[st]);
+        tma_load_2d(base + L::kMOff, &tm_mask, x0, y0, &s_bar[st]);
+        if (with_slopes) tma_load_2d(base + L::kSOff, &tm_slopes, 8 * x0, y0, &s_bar[st]);
+    };
+    if (tid == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+        fence_mbarrier_init();
+        if (blockIdx.x < n_items) issue(blockIdx.x, 0);
+    }
+    __syncthreads();
+    int it = 0;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++it) {
+        const int st = it & 1;
+        // the next strip's copies go into the other stage, free since the end of the previous strip
+        if (tid == 0 && item + (int)gridDim.x < n_items) {
+            fence_proxy_async_shared();
+            issue(item + gridDim.x, st ^ 1);
+        }
+        // every thread observes the copies' completion on the barrier
+        const bool arrived = mbar_wait(&s_bar[st], (it >> 1) & 1, kTmaSpin);
+        if (__syncthreads_or(!arrived)) {
+            // the copies never arrived: give up, and let those in flight land
+            // before the block's shared memory is released
+            if (tid == 0) {
+                raise_error(&sc->err, ErrFlags::kNoConverge);
+                mbar_wait(&s_bar[st], (it >> 1) & 1, kTmaSpin);
+                if (item + (int)gridDim.x < n_items) mbar_wait(&s_bar[st ^ 1], ((it + 1) >> 1) & 1, kTmaSpin);
+            }
+            __syncthreads();
+            break;
+        }
+        int x0, y0;
+        origin(item, x0, y0);
+        const unsigned char* base = smem + st * L::kStage;
+        const double* zb = reinterpret_cast<const double*>(base + L::kZOff);
+        const uint8_t* mb = base + L::kMOff;
+        const float* sb_ = reinterpret_cast<const float*>(base + L::kSOff);
+        for (int e = tid; e < L::kKeys; e += FD_BX * FD_BY) {
+            const int ly = e / P, lx = e % P;
+            const int gx = x0 + lx - 1, gy = y0 + ly - 1;
+            fd_stage(zb[ly * L::kBoxW + lx + 1], gx >= 0 && gx < W && gy >= 0 && gy < H, skey[e], shi[e], slo[e]);
         }
         __syncthreads();
-        const int s1 = warp_sum(is_sink), f1 = warp_sum(is_flat);
-        low = warp_min_u64(low);
-        const int d = warp_dem(dc, self, mk != 0);
-        if ((tid & 31) == 0) {
-            if (s1) atomicAdd(&s_sinks, s1);
-            if (f1) atomicAdd(&s_flats, f1);
-            if (low != ~0ull) atomicMin(&s_low, low);
-            if (d >= 0) atomicMax(&s_dem, d);
+        int n_sink = 0, n_flat = 0, dem_w = -1;
+        unsigned long long low = ~0ull;
+#pragma unroll
+        for (int r = 0; r < ROWS / FD_BY; ++r) {
+            const int ly = threadIdx.y + FD_BY * r;
+            const int x = x0 + threadIdx.x, y = y0 + ly;
+            const bool inb = x < W && y < H;
+            const size_t self = (size_t)y * W + x;
+            const bool mk = inb && mb[ly * kTile + threadIdx.x] != 0;
+            float4 sa = make_float4(0.f, 0.f, 0.f, 0.f), sbb = sa;
+            if (with_slopes && mk) {
+                const float4* s4 = reinterpret_cast<const float4*>(sb_ + (ly * kTile + threadIdx.x) * 8);
+                sa = s4[0];
+                sbb = s4[1];
+            }
+            FdCell c;
+            if (inb) {
+                bool touched = false;
+                c = fd_cell<P>(skey, shi, slo, (ly + 1) * P + threadIdx.x + 1, mk, sa, sbb, &touched, k);
+                if (with_slopes && mk && touched) {
+                    float4* g4 = reinterpret_cast<float4*>(slopes + 8 * self);
+                    g4[0] = sa;
+                    g4[1] = sbb;
+                }
+                sfd[self] = c.cs;
+                mfd[self] = c.cm;
+                sp[self] = c.is_cand ? kFar : 0.f;
+            }
+            block_append(c.is_cand && c.has_equal, (int32_t)self, plateau, &sc->n_cand, (int)((size_t)W * H),
+                         &sc->err, s_cnt);
+            n_sink += c.is_sink;
+            n_flat += c.is_flat;
+            low = c.low < low ? c.low : low;
+            const int d = warp_dem(dc, self, mk);
+            dem_w = d > dem_w ? d : dem_w;
         }
-        __syncthreads();
-        if (tid == 0 && s_dem >= 0) {
-            DemOut& o = dc.out[s_dem];
-            if (s_sinks) atomicAdd(&o.sink_counter, s_sinks);
-            if (s_flats) atomicAdd(&o.flat_counter, s_flats);
-            if (s_low != ~0ull) atomicMin(&o.lowest_key, s_low);
-        }
+        if (pass == 1) fd_counters(n_sink, n_flat, low, dem_w, dc, &s_sinks, &s_flats, &s_low, &s_dem);
+        __syncthreads();  // every thread is done with this stage before it is refilled
     }
 }
 
@@ -1181,6 +1359,22 @@ static int flat_blocks(size_t n, int threads, int cap_blocks) {
     return (int)b;
 }
 
+template <int ROWS>
+static lem_status launch_flowdirs_tma(const DevState& s, const ModelConsts& k, const Launch& L, const TileSet& ts,
+                                      int pass, int shape) {
+    const FdTmaMaps& m = *s.fd_tma;
+    const int items = ts.n * (kTile / ROWS);
+    const int blocks = items < m.blocks[shape] ? items : m.blocks[shape];
+    if (blocks < 1) return LEM_OK;
+    L.pre("k_flowdirs");
+    k_flowdirs_tma<ROWS><<<blocks, dim3(FD_BX, FD_BY), FdTma<ROWS>::kSmem, L.st>>>(
+        pass == 1 ? m.z[shape] : m.zf[shape], m.mask[shape], m.slopes[shape], pass == 1 ? s.slopes : nullptr, s.sfd,
+        s.mfd, s.sp, s.list_a, k, s.sc, s.dems, ts, pass);
+    L.post();
+    LEM_CUDA_TRY(cudaGetLastError());
+    return LEM_OK;
+}
+
 // One pass of FlowDirs + plateau routing.  Pass 1 reads the stage's DEM and
 // updates the persistent slopes; pass 2 reads the raised DEM.
 static lem_status direction_pass(const DevState& s, const ModelConsts& k, const Launch& L, int pass) {
@@ -1191,7 +1385,18 @@ static lem_status direction_pass(const DevState& s, const ModelConsts& k, const 
     const double* zz = pass == 1 ? s.z : s.zf;
     float* slopes = pass == 1 ? s.slopes : nullptr;
     if (pass == 2) LEM_LAUNCH(L, k_cand_reset, 1, 1, s.sc);
-    LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, s.dems, ts, pass);
+    if (s.fd_tma) {
+        lem_status r = LEM_OK;
+        switch (s.fd_rows) {
+            case 1: r = launch_flowdirs_tma<16>(s, k, L, ts, pass, 1); break;
+            case 2: r = launch_flowdirs_tma<32>(s, k, L, ts, pass, 2); break;
+            default: r = launch_flowdirs_tma<8>(s, k, L, ts, pass, 0); break;
+        }
+        if (r != LEM_OK) return r;
+    } else {
+        LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, s.dems, ts,
+                   pass);
+    }
     {
         // candidates in list_a; frontiers in list_b and `pending` (an int32 grid unused in this stage)
         float* sp = s.sp;
@@ -1276,6 +1481,50 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
     LEM_LAUNCH(L, k_fd_outlets, (s.dems.n + 127) / 128, 128, s.fd, s.z, s.dems);
     LEM_CUDA_TRY(cudaGetLastError());
     return LEM_OK;
+}
+
+namespace {
+template <int ROWS>
+lem_status fd_tma_shape(const DevState& s, const ModelConsts& k, FdTmaMaps* m, int shape,
+                        PFN_cuTensorMapEncodeTiled_v12000 encode) {
+    using L = FdTma<ROWS>;
+    const cuuint64_t W = (cuuint64_t)k.W, H = (cuuint64_t)k.H;
+    const cuuint32_t one[2] = {1, 1};
+    auto enc = [&](CUtensorMap* map, CUtensorMapDataType type, void* base, cuuint64_t w, cuuint64_t stride,
+                   cuuint32_t bw, cuuint32_t bh) {
+        const cuuint64_t dims[2] = {w, H};
+        const cuuint64_t strides[1] = {stride};
+        const cuuint32_t box[2] = {bw, bh};
+        return encode(map, type, 2, base, dims, strides, box, one, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    };
+    if (enc(&m->z[shape], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, s.z, W, W * 8, L::kBoxW, ROWS + 2) != CUDA_SUCCESS ||
+        enc(&m->zf[shape], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, s.zf, W, W * 8, L::kBoxW, ROWS + 2) != CUDA_SUCCESS ||
+        enc(&m->mask[shape], CU_TENSOR_MAP_DATA_TYPE_UINT8, s.mask, W, W, kTile, ROWS) != CUDA_SUCCESS ||
+        enc(&m->slopes[shape], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, s.slopes, 8 * W, W * 32, 8 * kTile, ROWS) !=
+            CUDA_SUCCESS)
+        return LEM_ERR_INVALID;
+    LEM_CUDA_TRY(cudaFuncSetAttribute(k_flowdirs_tma<ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kSmem));
+    int per = 0, dev = 0, sms = 0;
+    LEM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flowdirs_tma<ROWS>, FD_BX * FD_BY, L::kSmem));
+    LEM_CUDA_TRY(cudaGetDevice(&dev));
+    LEM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    m->blocks[shape] = (per < 1 ? 1 : per) * sms;
+    return LEM_OK;
+}
+}  // namespace
+
+lem_status fd_tma_setup(const DevState& s, const ModelConsts& k, FdTmaMaps* maps) {
+    if (k.W % 16 != 0) return LEM_ERR_INVALID;  // rows of the mask and elevations must be 16-byte multiples
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    LEM_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (!fn || q != cudaDriverEntryPointSuccess) return LEM_ERR_INVALID;
+    const auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    lem_status r;
+    if ((r = fd_tma_shape<8>(s, k, maps, 0, encode)) != LEM_OK) return r;
+    if ((r = fd_tma_shape<16>(s, k, maps, 1, encode)) != LEM_OK) return r;
+    return fd_tma_shape<32>(s, k, maps, 2, encode);
 }
 
 // cooperative kernels of this file, for the co-residency query at handle creation

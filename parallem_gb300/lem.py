@@ -74,7 +74,8 @@ class Totals(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("state", C.c_int32), ("steps_left", C.c_int32), ("coop_blocks", C.c_int32 * 8),
-                ("default_ms", C.c_double), ("tuned_ms", C.c_double)]
+                ("default_ms", C.c_double), ("tuned_ms", C.c_double), ("flowdirs_tile_rows", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 COOP_KERNELS = ("k_plateau_relax", "k_flood_merge", "k_flood_jump", "k_flood_spill", "k_fat_coarse", "k_fa_walk",
@@ -86,7 +87,7 @@ def _tuning(h) -> dict:
     _check(load().lem_get_tuning(h, C.byref(t)), "lem_get_tuning")
     return {"state": ("default", "tuning", "tuned")[t.state], "steps_left": t.steps_left,
             "coop_blocks": dict(zip(COOP_KERNELS, list(t.coop_blocks))),
-            "default_ms": t.default_ms, "tuned_ms": t.tuned_ms}
+            "default_ms": t.default_ms, "tuned_ms": t.tuned_ms, "flowdirs_tile_rows": t.flowdirs_tile_rows}
 
 
 class Limits(C.Structure):

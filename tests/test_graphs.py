@@ -111,3 +111,47 @@ def test_autotuned_schedule_gives_the_same_grids(lem):
     assert t0["state"] == "default" and t1["state"] == "tuned" and t1["steps_left"] == 0
     assert all(b > 0 for b in t1["coop_blocks"].values())
     assert t1["tuned_ms"] <= t1["default_ms"] + 1e-9
+
+
+def test_every_flow_direction_tile_shape_gives_the_same_steps(lem):
+    """The autotuner's candidate steps run the TMA flow-direction kernel with
+    tiles of 8, 16, 32 and again 8 rows; each of those steps equals, bit for
+    bit, the same step under the default schedule.  A width that is not a
+    multiple of 16 takes the plain-load kernel, and the same DEM inside a
+    32-aligned batch canvas takes the TMA kernel: those agree too."""
+    dem = S.make_dem(256, 0.75, 600.0, 0.04, 60, 6, 91)
+    st = S.initial_state(dem, 30.0, 900.0, 9.0)
+    rng = np.random.default_rng(92)
+    clim = [(float(rng.lognormal(np.log(900), 0.3)), float(rng.normal(9, 2))) for _ in range(5)]
+    a = lem.Model(dem, 30.0, 900.0, 9.0)
+    b = lem.Model(dem, 30.0, 900.0, 9.0)
+    for m in (a, b):
+        m.set_state(st)
+    assert b.tuning()["flowdirs_tile_rows"] in (8, 16, 32)  # a width of 256 takes the TMA kernel
+    b.autotune(1)  # one unmeasured step, then the four candidates
+    for rain, temp in clim:
+        a.step(rain, temp, True)
+        b.step(rain, temp, True)
+        for f in ("fd", "sfd", "slopes", "fa", "dem", "stone"):
+            np.testing.assert_array_equal(a.get(f), b.get(f), err_msg=f)
+    assert b.tuning()["state"] == "tuned"
+    a.close()
+    b.close()
+    # a width of 250 (not a multiple of 16): the plain-load kernel, against the TMA kernel on the canvas
+    d2 = dem[:, :250].copy()
+    d2[:, -2:] = S.NODATA
+    st2 = S.initial_state(d2, 30.0, 900.0, 9.0)
+    c = lem.Model(d2, 30.0, 900.0, 9.0)
+    c.set_state(st2)
+    assert c.tuning()["flowdirs_tile_rows"] == 0
+    bt = lem.Batch(512, 512, 30.0, max_dems=4)
+    i = bt.add(d2, 900.0, 9.0)
+    bt.set_state(i, st2)
+    for rain, temp in clim[:2]:
+        c.step(rain, temp, True)
+        bt.set_climate(i, rain, temp, True)
+        bt.step()
+        for f in ("fd", "sfd", "slopes", "fa", "dem"):
+            np.testing.assert_array_equal(c.get(f), bt.get(i, f), err_msg=f)
+    c.close()
+    bt.close()
