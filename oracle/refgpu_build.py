@@ -33,6 +33,9 @@ UNITS = ["FD_kernels/newflow.cu", "FD_kernels/routeflow.cu", "FA_kernels/mfd_sim
          "MOD_kernels/runoffweight.cu", "MOD_kernels/eroincidep.cu", "MOD_kernels/mfd_accum.cu",
          "MOD_kernels/updates.cu", "MOD_kernels/erosion.cu", "MEM_kernels/memory_dev.cu", "MEM_kernels/memory.cu",
          "MEM_kernels/MapInfo.cu", "MEM_kernels/Data.cpp", "MEM_kernels/io.cpp"]
+# the driver itself: not part of the library, but copied so that the shim's
+# link test can build lem.cpp unchanged against liblem_refshim.so
+DRIVER = "lem.cpp"
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-w",
          "-x", "cu", "-include", os.path.join(COMPAT, "compat.h")]
 
@@ -40,7 +43,7 @@ FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-Xc
 def _copy_sources() -> bool:
     """Refreshes the copy from the reference tree; False when neither exists."""
     if os.path.isdir(os.path.join(REF, "FD_kernels")):
-        for rel in UNITS + [os.path.join("headers", h) for h in os.listdir(os.path.join(REF, "headers"))]:
+        for rel in UNITS + [DRIVER] + [os.path.join("headers", h) for h in os.listdir(os.path.join(REF, "headers"))]:
             src, dst = os.path.join(REF, rel), os.path.join(SRC, rel)
             os.makedirs(os.path.dirname(dst), exist_ok=True)
             if not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(src):

@@ -166,3 +166,29 @@ def test_driver_loop_on_the_shim_matches_the_oracle(driver):
                   ("tot_weather_c", "totWC"), ("tot_weather_p", "totWP"), ("tot_bio", "totbio"),
                   ("fa_max", "FA_max")):
         assert abs(r[k] - getattr(o.s, ok)) <= 1e-5 * abs(getattr(o.s, ok)) + 1e-12, (k, r[k], getattr(o.s, ok))
+
+
+def test_reference_driver_links_unchanged_against_the_shim(tmp_path):
+    """The reference's own lem.cpp, with its host files Data.cpp, io.cpp,
+    memory.cu and MapInfo.cu, compiles and links against liblem_refshim.so in
+    place of its FD_kernels, FA_kernels, MOD_kernels and memory_dev.cu objects:
+    every stage name it calls is resolved by the shim (no GPU needed).
+    Skipped where the reference sources are not present."""
+    import shutil
+    from oracle import refgpu_build as rg
+    rb, lib = _shim()
+    if not rg._copy_sources() or not os.path.isfile(os.path.join(rg.SRC, rg.DRIVER)):
+        pytest.skip("the reference sources are not present")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    src = rg.SRC
+    exe = str(tmp_path / "lem_on_shim")
+    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O1", "-std=c++17", "-w", "-x", "cu",
+           "-include", os.path.join(rg.COMPAT, "compat.h"), "-I", rg.COMPAT, "-I", os.path.join(src, "headers"),
+           os.path.join(src, "lem.cpp")] + [os.path.join(src, "MEM_kernels", f) for f in
+                                            ("Data.cpp", "io.cpp", "memory.cu", "MapInfo.cu")] + \
+          ["-L", rb.LIBDIR, "-llem_refshim", "-llem_gb300", "-Xlinker", "-rpath," + rb.LIBDIR, "-o", exe]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stdout[-3000:] + res.stderr[-3000:]
+    undefined = subprocess.run(["nm", "-uC", exe], capture_output=True, text=True, check=True).stdout
+    for name in ("cuFlowDirection", "correctmfdflow", "erosionGPU", "computeRunOffWeights", "createDeviceSpace"):
+        assert name in undefined  # taken from the shim library, not from objects of its own
