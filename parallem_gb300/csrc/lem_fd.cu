@@ -318,7 +318,7 @@ struct FdTma {
     static constexpr int kSOff = kMOff + (kMBytes + 127) / 128 * 128;
     static constexpr int kStage = kSOff + kSBytes;   // bytes per pipeline stage (a multiple of 128)
     static constexpr int kKeys = kStageW * (ROWS + 2);
-    static constexpr int kSmem = 2 * kStage + kKeys * 16 + 256;
+    static constexpr int kSmem = 2 * kStage + kKeys * 16 + 256;  // + room to align the base to 128 bytes
     static_assert(kStage % 128 == 0, "stages stay 128-byte aligned");
 };
 
@@ -334,7 +334,9 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
     constexpr int SPT = kTile / ROWS;  // strips per tile
     constexpr int P = L::kStageW;
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
-    extern __shared__ __align__(128) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // the copies' destinations are 128-byte aligned (the size carries the slack)
+    unsigned char* const smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
     __shared__ __align__(8) uint64_t s_bar[2];
     __shared__ int s_cnt[FD_BX * FD_BY / 32 + 1];
     __shared__ int s_sinks, s_flats, s_dem;

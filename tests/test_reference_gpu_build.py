@@ -6,10 +6,12 @@ lem.cpp's set-up and timestep loop on them; tests/refshim/driver.cpp runs the
 same loop on liblem_refshim.so (this path behind the reference's names).  Both
 start from the same DEM and state.
 
-gpu checks, one step: the reference's direction codes equal the oracle's on all
-but a small share of cells (the plateau ties whose winner depends on the
-reference's thread order; both answers attain the plateau distance), and its
-budget totals agree with the oracle's and with this path's.  Lines starting
+gpu checks, one step: wherever the reference's direction code differs from the
+oracle's, it points to another neighbour that attains the cell's plateau
+distance on the routed DEM (a plateau tie, whose winner depends on the
+reference's thread order), and its budget totals agree with the oracle's and
+with this path's to 2 % (the tie choices move some water and sediment between
+paths).  Lines starting
 REFGPU give the wall-clock milliseconds per stage of both implementations
 (each stage call with its setdevicespace_*/cleardevicespace_* calls, host
 mirrors included).  LEM_REFGPU_LARGE=1 adds the 4080x4096 grid.
@@ -117,26 +119,52 @@ def compare_and_time(ref_gpu, w, h, steps, seed):
     o.step(float(rain[0]), float(temp[0]), True, lem.STEP_SET_OUTLET_FROM_FA)
     differ = (ref["sfd"] != o["sfd"]) & mask
     share = float(differ.sum()) / float(mask.sum())
-    assert share < 0.02, f"{share:.4f} of the cells take another direction than the oracle's"
+    bad = plateau_tie_violations(ref["sfd"], o, differ)
     tot = {"tot_e": "totE", "tot_i": "totI", "tot_g": "totG", "tot_d": "totD", "tot_bio": "totbio"}
-    for k, ok in tot.items():
-        a, b = ref_rows[0][k], getattr(o.s, ok)
-        assert abs(a - b) <= 0.02 * abs(b) + 1e-9, (k, a, b)
-    return dem, st, params, rain, temp, ref_ms, share
+    far = {k: (ref_rows[0][k], getattr(o.s, ok)) for k, ok in tot.items()
+           if abs(ref_rows[0][k] - getattr(o.s, ok)) > 0.02 * abs(getattr(o.s, ok)) + 1e-9}
+    return dem, st, params, rain, temp, ref_ms, share, bad, far
+
+
+def plateau_tie_violations(ref_sfd, o, differ) -> int:
+    """Cells where the reference's direction differs from the oracle's and is
+    not another neighbour attaining the cell's plateau distance on the routed
+    DEM (the oracle's distances are the relaxation's unique fixpoint, so the
+    reference's are the same; only the winner among tied neighbours depends on
+    its thread order)."""
+    H, W = ref_sfd.shape
+    z, sp = o["dem_routed"], o["shortest_paths"].astype(np.float32)
+    dxl, dyl, dcl, okl = (np.zeros(256, np.int64), np.zeros(256, np.int64), np.zeros(256, np.float32),
+                          np.zeros(256, bool))
+    for code, (dx, dy, dc) in {64: (0, -1, 1.0), 128: (1, -1, 1.41), 1: (1, 0, 1.0), 2: (1, 1, 1.41),
+                               4: (0, 1, 1.0), 8: (-1, 1, 1.41), 16: (-1, 0, 1.0), 32: (-1, -1, 1.41)}.items():
+        dxl[code], dyl[code], dcl[code], okl[code] = dx, dy, dc, True
+    ys, xs = np.nonzero(differ)
+    codes = ref_sfd[ys, xs]
+    single = (codes >= 0) & (codes < 256)
+    c = np.where(single, codes, 0)
+    valid = single & okl[c]
+    ny, nx = ys + dyl[c], xs + dxl[c]
+    inside = valid & (nx >= 0) & (nx < W) & (ny >= 0) & (ny < H)
+    nyc, nxc = np.clip(ny, 0, H - 1), np.clip(nx, 0, W - 1)
+    tie = inside & (z[nyc, nxc] == z[ys, xs]) & ((sp[nyc, nxc] + dcl[c]).astype(np.float32) == sp[ys, xs])
+    return int((~tie).sum())
 
 
 def test_reference_build_runs_and_agrees_with_the_oracle_and_this_path(ref_gpu, tmp_path_factory):
     w, h, steps = 1000, 1024, 3
-    dem, st, params, rain, temp, _, share = compare_and_time(ref_gpu, w, h, steps, 81)
+    dem, st, params, rain, temp, _, share, bad, far = compare_and_time(ref_gpu, w, h, steps, 81)
     # timing: the same loop, several steps, both implementations
     _, ref_rows, ref_ms = run_reference(ref_gpu, dem, st, params, rain, temp)
     L = _driver(tmp_path_factory)
     ms = np.zeros((steps, 4))
     ours, rows = run_driver(L, dem, st, params, 900.0, 9.0, 0, rain, temp, stage_ms=ms)
+    report(w, h, dem, ref_ms, ms, share, bad)
+    assert bad == 0, f"{bad} cells take a direction that is not a plateau tie"
+    assert not far, far
     for k in ("tot_e", "tot_i", "tot_g", "tot_d", "tot_bio"):
         for a, b in zip(rows, ref_rows):
             assert abs(a[k] - b[k]) <= 0.05 * abs(b[k]) + 1e-9, (k, a[k], b[k])
-    report(w, h, dem, ref_ms, ms, share)
 
 
 def _driver(tmp_path_factory):
@@ -159,9 +187,10 @@ def _driver(tmp_path_factory):
     return L
 
 
-def report(w, h, dem, ref_ms, ms, share):
+def report(w, h, dem, ref_ms, ms, share, bad):
     cells = int((dem != -9999).sum())
-    line = {"grid": f"{w}x{h}", "active_cells": cells, "steps": len(ms), "tie_share": share,
+    line = {"grid": f"{w}x{h}", "active_cells": cells, "steps": len(ms), "direction_differs_share": share,
+            "differs_not_a_plateau_tie": bad,
             "reference_ms_per_stage": ref_ms.mean(axis=0).round(3).tolist(),
             "this_path_via_shim_ms_per_stage": ms.mean(axis=0).round(3).tolist(),
             "stages": ["flow direction", "accumulation", "erosion", "step"],
@@ -173,9 +202,11 @@ def report(w, h, dem, ref_ms, ms, share):
 @pytest.mark.skipif(os.environ.get("LEM_REFGPU_LARGE") != "1", reason="LEM_REFGPU_LARGE=1 runs the 4080x4096 grid")
 def test_reference_build_on_the_large_grid(ref_gpu, tmp_path_factory):
     w, h, steps = 4080, 4096, 2
-    dem, st, params, rain, temp, _, share = compare_and_time(ref_gpu, w, h, 1, 82)
+    dem, st, params, rain, temp, _, share, bad, far = compare_and_time(ref_gpu, w, h, 1, 82)
     _, ref_rows, ref_ms = run_reference(ref_gpu, dem, st, params, rain[:1].repeat(steps), temp[:1].repeat(steps))
     L = _driver(tmp_path_factory)
     ms = np.zeros((steps, 4))
     run_driver(L, dem, st, params, 900.0, 9.0, 0, rain[:1].repeat(steps), temp[:1].repeat(steps), stage_ms=ms)
-    report(w, h, dem, ref_ms, ms, share)
+    report(w, h, dem, ref_ms, ms, share, bad)
+    assert bad == 0, f"{bad} cells take a direction that is not a plateau tie"
+    assert not far, far
