@@ -53,26 +53,45 @@ __global__ void k_fa_prep(const uint8_t* __restrict__ mask, const uint8_t* __res
     const float rain0 = (float)r.rain, rinc = (float)r.rain_inc;
     int nact = 0;
     bool untiled = false;
-    for (int64_t ri = ch.first + threadIdx.x; ri < ch.end; ri += blockDim.x) {
-        int x, y;
-        const size_t i = region_cell(r, ri, W, &x, &y);
-        // the cell's inputs in one batch of loads, ahead of the mask test
-        const uint8_t mk = mask[i], code = fd[i];
-        const float sto = stone[i], tb = totB[i], sm0 = soilM[i];
-        if (mk) {
-            ++nact;
-            const float coeff = (1.0f - 0.0085f * sto) * expf(-0.0025f * tb / 76.5f) * tanhf(0.6f + sm0 / 0.2f);
-            const float myppt = (rain0 + (float)(y - r.y0) * rinc) / 1000.0f;
-            const float wi = myppt * coeff;
-            float sm = sm0 + myppt * (1.0f - coeff);
-            if (sm > 0.5f) sm = 0.5f;
-            soilM[i] = sm;
-            w[i] = wi;
-            fa[i] = make_float2(wi, 0.0f);
-            untiled |= wi < 0.0f || (code & (code - 1));
-        } else {
-            w[i] = -9999.0f;
-            fa[i] = make_float2(0.0f, 0.0f);
+    // two cells per thread and iteration: both cells' inputs are loaded before
+    // either is used, so each thread keeps two cells' loads in flight
+    for (int64_t r0 = ch.first + threadIdx.x; r0 < ch.end; r0 += 2 * blockDim.x) {
+        size_t i[2];
+        int y[2];
+        uint8_t mk[2] = {0, 0}, code[2] = {0, 0};
+        float sto[2], tb[2], sm0[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int64_t ri = r0 + u * blockDim.x;
+            int x;
+            i[u] = ri < ch.end ? region_cell(r, ri, W, &x, &y[u]) : 0;
+            if (ri < ch.end) {
+                mk[u] = mask[i[u]];
+                code[u] = fd[i[u]];
+                sto[u] = stone[i[u]];
+                tb[u] = totB[i[u]];
+                sm0[u] = soilM[i[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (r0 + u * blockDim.x >= ch.end) continue;
+            if (mk[u]) {
+                ++nact;
+                const float coeff =
+                    (1.0f - 0.0085f * sto[u]) * expf(-0.0025f * tb[u] / 76.5f) * tanhf(0.6f + sm0[u] / 0.2f);
+                const float myppt = (rain0 + (float)(y[u] - r.y0) * rinc) / 1000.0f;
+                const float wi = myppt * coeff;
+                float sm = sm0[u] + myppt * (1.0f - coeff);
+                if (sm > 0.5f) sm = 0.5f;
+                soilM[i[u]] = sm;
+                w[i[u]] = wi;
+                fa[i[u]] = make_float2(wi, 0.0f);
+                untiled |= wi < 0.0f || (code[u] & (code[u] - 1));
+            } else {
+                w[i[u]] = -9999.0f;
+                fa[i[u]] = make_float2(0.0f, 0.0f);
+            }
         }
     }
     if (__syncthreads_or(untiled) && threadIdx.x == 0) sc->tiled_ok = 0;
