@@ -461,7 +461,7 @@ constexpr int kTileSweeps = 2048;  // sweeps of one tile visit before it is re-q
 // candidate.  The fixpoint is unique, so the visiting order does not change the
 // result.  Only candidates (sp > 0) ever change: every other cell is a source
 // at 0.
-__global__ void __launch_bounds__(256, 5) k_plateau_relax(const double* __restrict__ z, float* sp,
+__global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict__ z, float* sp,
                                                        const int32_t* __restrict__ cand, int32_t* list_a,
                                                        int32_t* list_b, int32_t* mark, ModelConsts k,
                                                        DevScalars* sc, int pass) {
@@ -544,43 +544,32 @@ __global__ void __launch_bounds__(256, 5) k_plateau_relax(const double* __restri
             if (threadIdx.x < 9) s_act[threadIdx.x] = 0;
             __syncthreads();
             // per cell: its start value and the directions of its equal-height
-            // neighbours (none for a cell that is not a candidate or is NaN).
-            // The thread owns two runs of 4 cells: rows 4wy..4wy+3 of column lx
-            // (column runs) and columns 4(lx & 7)..+3 of row 4wy + (lx >> 3)
-            // (row runs).
-            auto eq_of = [&](int sidx) {
-                uint32_t m = 0;
-                const unsigned long long kc = s_key[sidx];
-                if (s_v[sidx] > 0.f && kc != 0) {  // a NaN cell (key 0) equals no neighbour
-#pragma unroll
-                    for (int d = 0; d < 8; ++d)
-                        if (s_key[sidx + dir_dy(d) * kPH + dir_dx(d)] == kc) m |= 1u << d;
-                }
-                return m;
-            };
+            // neighbours (none for a cell that is not a candidate or is NaN)
             float v0[4];
-            uint32_t eq[4], eqr[4];
-            const int rrow = 4 * wy + (lx >> 3), rcol = 4 * (lx & 7);
+            uint32_t eq[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int sidx = (4 * wy + q + 1) * kPH + lx + 1;
                 v0[q] = s_v[sidx];
-                eq[q] = eq_of(sidx);
-                eqr[q] = eq_of((rrow + 1) * kPH + rcol + q + 1);
+                const unsigned long long kc = s_key[sidx];
+                uint32_t m = 0;
+                if (v0[q] > 0.f && kc != 0) {  // a NaN cell (key 0) equals no neighbour
+#pragma unroll
+                    for (int d = 0; d < 8; ++d)
+                        if (s_key[sidx + dir_dy(d) * kPH + dir_dx(d)] == kc) m |= 1u << d;
+                }
+                eq[q] = m;
             }
             const bool any_eq = (eq[0] | eq[1] | eq[2] | eq[3]) != 0;
-            const bool any_eqr = (eqr[0] | eqr[1] | eqr[2] | eqr[3]) != 0;
-            // Gauss-Seidel sweeps over the runs: down the column runs, right
-            // along the row runs, up, left, in turn, so a front moves up to 4
-            // cells per sweep along either axis.  Every order of updates ends
-            // at the same fixpoint.
-            auto relax_at = [&](int sidx, uint32_t m) {
-                if (!m) return false;
+            // Gauss-Seidel sweeps, down and up the thread's rows in turn
+            auto relax = [&](int q) {
+                if (!eq[q]) return false;
+                const int sidx = (4 * wy + q + 1) * kPH + lx + 1;
                 const float cv = s_v[sidx];
                 float best = cv;
 #pragma unroll
                 for (int d = 0; d < 8; ++d) {
-                    if (!((m >> d) & 1u)) continue;
+                    if (!((eq[q] >> d) & 1u)) continue;
                     const float nv = s_v[sidx + dir_dy(d) * kPH + dir_dx(d)] + ((d & 1) ? 1.41f : 1.0f);
                     if (nv < best) best = nv;
                 }
@@ -590,39 +579,18 @@ __global__ void __launch_bounds__(256, 5) k_plateau_relax(const double* __restri
                 }
                 return false;
             };
-            auto relax = [&](int q) { return relax_at((4 * wy + q + 1) * kPH + lx + 1, eq[q]); };
-            auto relax_r = [&](int q) { return relax_at((rrow + 1) * kPH + rcol + q + 1, eqr[q]); };
             int sweep = 0;
             for (; sweep < kTileSweeps; ++sweep) {
                 bool ch = false;
-                switch (sweep & 3) {
-                    case 0:
-                        if (any_eq) {
+                if (any_eq) {
+                    if (sweep & 1) {
 #pragma unroll
-                            for (int q = 0; q < 4; ++q) ch |= relax(q);
-                        }
-                        break;
-                    case 1:
-                        if (any_eqr) {
+                        for (int q = 3; q >= 0; --q) ch |= relax(q);
+                    } else {
 #pragma unroll
-                            for (int q = 0; q < 4; ++q) ch |= relax_r(q);
-                        }
-                        break;
-                    case 2:
-                        if (any_eq) {
-#pragma unroll
-                            for (int q = 3; q >= 0; --q) ch |= relax(q);
-                        }
-                        break;
-                    default:
-                        if (any_eqr) {
-#pragma unroll
-                            for (int q = 3; q >= 0; --q) ch |= relax_r(q);
-                        }
-                        break;
+                        for (int q = 0; q < 4; ++q) ch |= relax(q);
+                    }
                 }
-                // either ownership visits every cell once: a sweep that changed
-                // nothing leaves the tile at its local fixpoint
                 if (!__syncthreads_or(ch)) break;
             }
             if (sweep == kTileSweeps && threadIdx.x == 0) s_act[4] = 1;  // not settled: visit again
