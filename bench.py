@@ -426,6 +426,50 @@ def grid_sample(args, steps=5):
             "steps": steps}
 
 
+def routing_sample():
+    """The routing stress configuration in isolation: one 8192x8192 DEM with
+    10 % of its cells in 1 m-quantised flats and 50k nested depressions; the
+    flow-direction stage (with plateau routing and sink flooding) and the
+    accumulation, SFD on the tiled path, SFD with the int32 contributing-cell
+    counts (the global wave) and MFD with slope-proportional shares, each timed
+    with events on the library's stream after one untimed run."""
+    from parallem_gb300 import lem
+    from parallem_gb300 import scenario as S
+    sc = S.config_routing(3, n=8192)
+    st = S.initial_state(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+    cells = int((st["mask"] == 1).sum())
+    out = {"workload": "routing stress 8192x8192: 10 % of cells in 1 m flats, 50k nested depressions, one step of "
+                       "flow direction and accumulation", "active_cells": cells}
+
+    def timed(g, fn):
+        fn()  # untimed: first use
+        g.set_state({"soilM": st["soilM"]})
+        g.synchronize()
+        g.record(0)
+        fn()
+        g.record(1)
+        return g.elapsed_ms(0, 1)
+
+    g = lem.Model(sc.dem, 30.0, sc.init_rain, sc.init_temp)
+    g.set_state(st)
+    out["flow_direction_ms"] = timed(g, g.flow_direction)
+    t = g.totals()
+    out.update({k: t[k] for k in ("plateau_sweeps", "merge_rounds", "label_rounds", "spill_rounds", "flood_edges",
+                                  "sinkcount", "initial_sinks", "initial_flats")})
+    out["sfd_accumulation_ms"] = timed(g, lambda: g.flow_accumulation(0))
+    out["sfd_contributing_counts_ms"] = timed(g, lambda: g.flow_accumulation(lem.STEP_CONTRIB))
+    g.close()
+    m = lem.Model(sc.dem, 30.0, sc.init_rain, sc.init_temp,
+                  params=lem.make_params(flow_direction_type=1, mfd_proportions=1))
+    m.set_state(st)
+    m.flow_direction()
+    out["mfd_accumulation_ms"] = timed(m, lambda: m.flow_accumulation(0))
+    m.close()
+    for k in ("flow_direction", "sfd_accumulation", "sfd_contributing_counts", "mfd_accumulation"):
+        out[k + "_cells_per_s"] = cells / (out[k + "_ms"] / 1e3)
+    return out
+
+
 def serve_sample(rate=20.0, requests=24, canvas=(16384, 12288), budget_gb=150.0):
     """The serving workload at one arrival rate: Poisson arrivals, sides
     log-uniform in [128, 4096], 10-500 steps, own climate series, continuously
@@ -516,7 +560,7 @@ def main():
     ap.add_argument("--no-graphs", action="store_true", help="step eagerly instead of one CUDA graph per step")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch schedule (no autotuning steps)")
     ap.add_argument("--no-extras", action="store_true",
-                    help="ensemble: skip the 4096x4096 plain-path and serving samples")
+                    help="ensemble: skip the 4096x4096, 8192x8192 routing and serving samples")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -656,9 +700,10 @@ def main():
         line["batched_over_plain"] = value / plain["value"]
     work.close()
     if args.workload == "ensemble" and not args.no_extras and world == 1:
-        # the other two workloads, measured in the same run: the single large
-        # grid on the plain path and serving at 20 requests/s
+        # the other workloads, measured in the same run: the single large grid
+        # on the plain path, the routing stress grid and serving at 20 requests/s
         line["grid_4096"] = grid_sample(args)
+        line["routing_8192"] = routing_sample()
         line["serving"] = serve_sample()
     print(json.dumps(line))
     if dist is not None:

@@ -275,7 +275,7 @@ lem_status lem_set_limits(lem_handle* h, const lem_limits* limits);
  * handle's next 1 + 4 * cycles steps (lem_step or lem_step_batch; real steps
  * of the model, launched eagerly) run the cooperative kernels with 1, 2 and 4
  * blocks per SM and with all their co-resident blocks in turn, and the
- * flow-direction kernel with TMA tiles of 8, 16, 32 and 8 rows, and time them
+ * flow-direction kernel with TMA tiles of 8, 32, 16 (the default) and 8 rows, and time them
  * with events; afterwards each keeps the block count (the tile shape) with the
  * lowest mean time if it beats the default by more than 3 %.  The default, also before
  * any tuning, is the block count every cooperative kernel can hold at once.  Results are the same under every block count.  LEM_ERR_STATE while

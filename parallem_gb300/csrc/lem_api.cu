@@ -86,7 +86,7 @@ constexpr int kTuneDefault = 2;
 constexpr double kTuneMargin = 0.97;  // a candidate replaces the default only below 97 % of its time
 // The flow-direction kernel's tile shape tried in each candidate step (an
 // index into kFdRows); the default shape is candidate kTuneDefault's.
-constexpr int kTuneFdShape[kTuneCands] = {0, 1, 2, 0};
+constexpr int kTuneFdShape[kTuneCands] = {0, 2, 1, 0};  // the default candidate takes 32 x 16 tiles
 const char* const kCoopNames[kCoopKernels] = {"k_plateau_relax", "k_flood_merge", "k_flood_jump", "k_flood_spill",
                                               "k_fat_coarse",    "k_fa_walk",     "k_sedt_coarse", "k_sed_walk"};
 struct Tuner {

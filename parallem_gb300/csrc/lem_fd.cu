@@ -325,7 +325,7 @@ struct FdTma {
 constexpr uint32_t kTmaSpin = 1u << 20;  // mbarrier polls before a wait gives up
 
 template <int ROWS>
-__global__ void __launch_bounds__(FD_BX* FD_BY)
+__global__ void __launch_bounds__(FD_BX* FD_BY, 4)
     k_flowdirs_tma(const __grid_constant__ CUtensorMap tm_z, const __grid_constant__ CUtensorMap tm_mask,
                    const __grid_constant__ CUtensorMap tm_slopes, float* __restrict__ slopes,
                    uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, float* __restrict__ sp, int32_t* plateau,
