@@ -387,6 +387,11 @@ class EnsembleWork:
                 "sample": f"{done} of the {len(self.ens)} DEMs (every fourth by size), each on its own handle with "
                           f"graph steps and its own autotuned schedule, {steps} device-timed steps each"}
 
+    def rounds(self):
+        """Rounds of the step's device loops (canvas-wide, the last step)."""
+        t = self.b.totals(self.ids[0])
+        return {k: t[k] for k in ("plateau_sweeps", "merge_rounds", "label_rounds", "spill_rounds", "flood_edges")}
+
     def config(self, args):
         sides = sorted(x.dem.shape[0] for x in self.ens)
         return {"workload": workload_name(args), "dems": len(self.ens), "active_cells": self.cells,
@@ -698,6 +703,8 @@ def main():
     if plain is not None:
         line["plain"] = plain
         line["batched_over_plain"] = value / plain["value"]
+    if hasattr(work, "rounds"):
+        line["loop_rounds"] = work.rounds()
     work.close()
     if args.workload == "ensemble" and not args.no_extras and world == 1:
         # the other workloads, measured in the same run: the single large grid
