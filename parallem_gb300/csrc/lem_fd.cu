@@ -40,6 +40,36 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
     return v;
 }
 
+// Exclusive prefix sum over a block of 256 threads; s_scan holds 9 ints;
+// *total receives the block's sum.  Every thread of the block calls it.
+__device__ __forceinline__ int block_exclusive_scan(int v, int* s_scan, int* total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_scan[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const int x = lane < 8 ? s_scan[lane] : 0;
+        int ix = x;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, ix, o);
+            if (lane >= o) ix += t;
+        }
+        if (lane < 8) s_scan[lane] = ix - x;
+        if (lane == 7) s_scan[8] = ix;
+    }
+    __syncthreads();
+    const int ex = s_scan[wid] + incl - v;
+    *total = s_scan[8];
+    __syncthreads();  // s_scan is free for the next call
+    return ex;
+}
+
 // Warp-aggregated append of `pred` lanes to list[*count].
 __device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t* list, int32_t* count, int cap,
                                             uint32_t* err) {
@@ -1013,7 +1043,9 @@ __global__ void __launch_bounds__(FE_BX* FE_BY)
 #pragma unroll
         for (int d = 0; d < 8; ++d) {
             const int32_t b = sw[ly + dir_dy(d)][lx + dir_dx(d)];
-            if (b < 0 || b == a) continue;
+            // a negative label is a pointer the jumping left when it stopped
+            // at its round cap (an error is raised): no basin to pair
+            if (a < 0 || b < 0 || b == a) continue;
             const unsigned long long kn = sk[ly + dir_dy(d)][lx + dir_dx(d)];
             if (kz == 0 || kn == 0 || kz < kn) continue;  // zs[this] >= zs[idx] is false for NaN
             const unsigned long long key = ((unsigned long long)(uint32_t)min(a, b) << 32) | (uint32_t)max(a, b);
@@ -1100,60 +1132,174 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
     }
 }
 
-// Spill heights.  The Kruskal pass of routeflow.cu:529-572 gives every basin
+// Spill heights.  The Kruskal pass of routeflow.cu:520-572 gives every basin
 // that can drain to basin 0 the smallest height h at which it connects to
-// basin 0 through boundaries no higher than h (the bottleneck distance); it is
-// computed here as the fixpoint raise[a] = min(raise[a], max(w_ab, raise[b])).
-// Minimax distance of every basin to basin 0 over the basin-pair edges
-// (Kruskal's raise, routeflow.cu:520-572, as a fixpoint: raise(a) = min over
-// edges (a, b, w) of max(w, raise(b)), basin 0 at 0).  Basins are numbered
-// compactly; every round sweeps the edge list and relaxes the edges with an
-// endpoint lowered in the previous round or earlier in this one (a stamp per
-// basin), so improvements run along several edges in one sweep while settled
-// parts of the graph cost only the stamp test.
+// basin 0 through boundaries no higher than h: its minimax distance to basin 0
+// over the basin-pair edges.  It is computed here as the fixpoint raise(a) =
+// min over edges (a, b, w) of max(w, raise(b)), basin 0 at 0, with basins
+// numbered compactly.  The kernel first groups the edges by basin (the edges
+// of basin 0 left out: nothing lowers it), then relaxes in rounds: round 1
+// sweeps the edge list for the edges of basin 0; every later round only the
+// edges of the basins lowered since the round before.
 __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __restrict__ eb,
                               const unsigned long long* __restrict__ ew, unsigned long long* raise, int32_t* comp,
                               unsigned long long* cdist, unsigned long long* cmaxw, const int32_t* __restrict__ bid,
                               const int32_t* __restrict__ blab, int32_t* stamp, unsigned long long* bdist,
-                              int32_t* euv, DevScalars* sc) {
+                              int32_t* euv, int32_t* adj_e, int32_t* adj_v, int32_t* cursor, int list_cap,
+                              DevScalars* sc) {
     if (sc->sinkcount_pass1 == 0) return;
-    cg::grid_group grid = cg::this_grid();
     const int n = sc->n_edges;
     const int nb = sc->n_basins;
+    if (nb > list_cap) {  // `cursor` holds list_cap entries
+        if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(&sc->err, ErrFlags::kCapacity);
+        return;
+    }
+    cg::grid_group grid = cg::this_grid();
+    __shared__ int s_scan[9];
     const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t gstride = (size_t)gridDim.x * blockDim.x;
-    const int32_t z = nb > 0 ? bid[0] : -1;  // basin 0 is on some edge whenever it borders a basin
+    const int lane = threadIdx.x & 31;
+    const int32_t z = nb > 0 ? bid[0] : -1;  // basin 0 is on an edge whenever it borders a basin
+    // The edges grouped by basin: offsets in comp (nb + 1 entries), chunk sums
+    // of their prefix sum in cmaxw; both are idle until the walled-in pass.
+    int32_t* const off = comp;
+    int32_t* const csum = reinterpret_cast<int32_t*>(cmaxw);
     for (size_t i = gtid; i < (size_t)nb; i += gstride) {
         bdist[i] = (int32_t)i == z ? 0ull : ~0ull;
-        stamp[i] = (int32_t)i == z ? 0 : -2;
-    }
-    for (size_t i = gtid; i < (size_t)n; i += gstride) {
-        euv[2 * i] = bid[ea[i]];
-        euv[2 * i + 1] = bid[eb[i]];
+        stamp[i] = -1;
+        cursor[i] = 0;
     }
     if (gtid == 0) sc->flag[0] = sc->flag[1] = sc->flag[2] = 0;
     grid.sync();
+    for (size_t i = gtid; i < (size_t)n; i += gstride) {  // degrees
+        const int32_t a = bid[ea[i]], b = bid[eb[i]];
+        euv[2 * i] = a;
+        euv[2 * i + 1] = b;
+        if (a != z && b != z) {
+            atomicAdd(cursor + a, 1);
+            atomicAdd(cursor + b, 1);
+        }
+    }
+    grid.sync();
+    // exclusive prefix sum of the degrees: per chunk of at least 256 basins,
+    // then over the chunk sums (block 0), then within the chunks again
+    const int chunk = max(256, (nb + (int)gridDim.x - 1) / (int)gridDim.x);
+    const int nchunks = (nb + chunk - 1) / chunk;
+    const int c0 = min(nb, (int)blockIdx.x * chunk), c1 = min(nb, c0 + chunk);
+    if ((int)blockIdx.x < nchunks) {
+        int part = 0;
+        for (int i = c0 + (int)threadIdx.x; i < c1; i += blockDim.x) part += cursor[i];
+        int total = 0;
+        block_exclusive_scan(part, s_scan, &total);
+        if (threadIdx.x == 0) csum[blockIdx.x] = total;
+    }
+    grid.sync();
+    if (blockIdx.x == 0) {
+        int carry = 0;
+        for (int b0 = 0; b0 < nchunks; b0 += blockDim.x) {
+            const int b = b0 + (int)threadIdx.x;
+            const int v = b < nchunks ? csum[b] : 0;
+            int total = 0;
+            const int ex = block_exclusive_scan(v, s_scan, &total);
+            if (b < nchunks) csum[b] = carry + ex;
+            carry += total;
+        }
+        if (threadIdx.x == 0) off[nb] = carry;
+    }
+    grid.sync();
+    if ((int)blockIdx.x < nchunks) {
+        int carry = csum[blockIdx.x];
+        for (int i0 = c0; i0 < c1; i0 += blockDim.x) {
+            const int i = i0 + (int)threadIdx.x;
+            const int v = i < c1 ? cursor[i] : 0;
+            int total = 0;
+            const int ex = block_exclusive_scan(v, s_scan, &total);
+            if (i < c1) {
+                off[i] = carry + ex;
+                cursor[i] = carry + ex;  // where the basin's next edge goes
+            }
+            carry += total;
+        }
+    }
+    grid.sync();
+    for (size_t i = gtid; i < (size_t)n; i += gstride) {
+        const int32_t a = euv[2 * i], b = euv[2 * i + 1];
+        if (a == z || b == z) continue;
+        const int pa = atomicAdd(cursor + a, 1), pb = atomicAdd(cursor + b, 1);
+        adj_e[pa] = (int32_t)i;
+        adj_v[pa] = b;
+        adj_e[pb] = (int32_t)i;
+        adj_v[pb] = a;
+    }
+    grid.sync();
+    // Round r relaxes the edges of every basin lowered in round r - 1 or
+    // earlier in round r (its stamp: the last round that lowered it), from
+    // the distance the basin has when its warp reaches it; a round that
+    // lowers nothing ends the loop.
+    const size_t warp = gtid >> 5, nwarps = gstride >> 5;
     int round = 1;
     for (;; ++round) {
-        if (gtid == 0) sc->flag[(round + 1) % 3] = 0;  // next round's flag; this round's is read after the sync
-        int changed = 0;
-        for (size_t i = gtid; i < (size_t)n; i += gstride) {
-            const int2 uv = __ldcg(reinterpret_cast<const int2*>(euv) + i);
-            const int32_t su = __ldcg(stamp + uv.x), sv = __ldcg(stamp + uv.y);
-            if (su < round - 1 && sv < round - 1) continue;
-            const unsigned long long w = ew[i];
-            const unsigned long long du = __ldcg(bdist + uv.x), dv = __ldcg(bdist + uv.y);
-            const unsigned long long cu = w > dv ? w : dv, cv = w > du ? w : du;
-            if (cu < du && atomicMin(bdist + uv.x, cu) > cu) {
-                stamp[uv.x] = round;
-                changed = 1;
+        if (gtid == 0) sc->flag[(round + 1) % 3] = 0;
+        bool lowered = false;
+        if (round == 1) {
+            for (size_t i = gtid; i < (size_t)n; i += gstride) {
+                const int2 uv = *reinterpret_cast<const int2*>(euv + 2 * i);
+                if (uv.x != z && uv.y != z) continue;
+                const int32_t v = uv.x == z ? uv.y : uv.x;
+                const unsigned long long cv = ew[i];
+                if (cv < __ldcg(bdist + v) && atomicMin(bdist + v, cv) > cv) {
+                    stamp[v] = round;
+                    lowered = true;
+                }
             }
-            if (cv < dv && atomicMin(bdist + uv.y, cv) > cv) {
-                stamp[uv.y] = round;
-                changed = 1;
+        } else {
+            // the edge lists of a warp's 32 basins that are active,
+            // concatenated and relaxed 32 edges at a time; a lane finds the
+            // basin of its edge by a search over the lanes' prefix sums
+            for (size_t u0 = warp * 32; u0 < (size_t)nb; u0 += nwarps * 32) {
+                const size_t mine = u0 + lane;
+                const bool act = mine < (size_t)nb && __ldcg(stamp + mine) >= round - 1;
+                int j0 = 0, deg = 0;
+                unsigned long long du = 0;
+                if (act) {
+                    j0 = off[mine];
+                    deg = off[mine + 1] - j0;
+                    du = __ldcg(bdist + mine);
+                }
+                int incl = deg;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                const int total = __shfl_sync(0xffffffffu, incl, 31);
+                for (int t0 = 0; t0 < total; t0 += 32) {
+                    const int t = t0 + lane;
+                    int k = 0;  // the first lane whose inclusive sum exceeds t
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const int pk = __shfl_sync(0xffffffffu, incl, k + step - 1);
+                        if (pk <= t) k += step;
+                    }
+                    const int kin = __shfl_sync(0xffffffffu, incl, k);
+                    const int kdeg = __shfl_sync(0xffffffffu, deg, k);
+                    const int kj0 = __shfl_sync(0xffffffffu, j0, k);
+                    const unsigned long long kdu = __shfl_sync(0xffffffffu, du, k);
+                    if (t < total) {
+                        const int j = kj0 + t - (kin - kdeg);
+                        const int32_t v = adj_v[j];
+                        const unsigned long long w = ew[adj_e[j]];
+                        const unsigned long long cv = w > kdu ? w : kdu;
+                        if (cv < __ldcg(bdist + v) && atomicMin(bdist + v, cv) > cv) {
+                            stamp[v] = round;
+                            lowered = true;
+                        }
+                    }
+                }
             }
         }
-        if (changed) sc->flag[round % 3] = 1;
+        if (__any_sync(0xffffffffu, lowered) && lane == 0 && __ldcg(&sc->flag[round % 3]) == 0)
+            sc->flag[round % 3] = 1;
         grid.sync();
         if (*((volatile int32_t*)&sc->flag[round % 3]) == 0) break;
         if (round >= round_cap_of(sc)) {
@@ -1270,7 +1416,8 @@ __global__ void k_flood_raise(const double* __restrict__ z, const uint8_t* __res
         const uint8_t mk = mask[c];
         const int dm = dem_at(dc, c);
         // the basin's raise is read alongside the DEM's sink count
-        const unsigned long long r = mk ? raise[ws[c]] : 0ull;
+        const int32_t lab = ws[c];  // negative only where the jumping stopped at its round cap
+        const unsigned long long r = (mk && lab >= 0) ? raise[lab] : 0ull;
         // a DEM without sinks keeps its DEM: its second pass repeats the first
         if (mk && dc.out[dm].sinkcount_pass1 != 0) {
             const unsigned long long kv = dkey(v);
@@ -1470,10 +1617,16 @@ lem_status launch_flow_direction(const DevState& s, const ModelConsts& k, const 
         int32_t* stamp = s.boff;
         unsigned long long* bdist = s.bdist;
         int32_t* euv = s.adj_v;
+        // the basin-pair table is idle after compaction: 2 * ecap int32 each
+        int32_t* adj_e = reinterpret_cast<int32_t*>(s.ekey);
+        int32_t* adj_v = reinterpret_cast<int32_t*>(s.ewt);
+        int32_t* cursor = s.pending;  // an int32 grid unused from the label jumping to the second direction pass
+        int list_cap = (int)std::min<size_t>((size_t)k.W * k.H, (size_t)INT32_MAX);  // entries of `pending`
         DevScalars* sc = s.sc;
-        void* args[] = {(void*)&ea,   (void*)&eb,    (void*)&ew,    (void*)&raise, (void*)&comp, (void*)&cdist,
-                        (void*)&cmaxw, (void*)&bidp, (void*)&blab,  (void*)&stamp, (void*)&bdist, (void*)&euv,
-                        (void*)&sc};
+        void* args[] = {(void*)&ea,    (void*)&eb,    (void*)&ew,     (void*)&raise, (void*)&comp,
+                        (void*)&cdist, (void*)&cmaxw, (void*)&bidp,   (void*)&blab,  (void*)&stamp,
+                        (void*)&bdist, (void*)&euv,   (void*)&adj_e,  (void*)&adj_v, (void*)&cursor,
+                        (void*)&list_cap, (void*)&sc};
         if ((r = coop("k_flood_spill", (const void*)k_flood_spill, s.coop_blocks[kCkSpill], args, L)) != LEM_OK) return r;
     }
     LEM_LAUNCH(L, k_flood_raise, flat_blocks(span, T, big), T, s.z, s.mask, s.ws, s.raise, s.zf, k, s.sc, s.dems,
