@@ -28,6 +28,7 @@ __host__ __device__ inline int bit_dir(uint32_t code) {
 // S, SW, W, NW, N, NE; the neighbour in direction d donates when its code has the
 // bit of the opposite direction (d + 4) % 8.  The scan order is d = 2,3,4,5,6,7,0,1.
 __host__ __device__ constexpr int scan_dir(int k) { return (k + 2) & 7; }
+__host__ __device__ constexpr int scan_index(int d) { return (d + 6) & 7; }  // k with scan_dir(k) == d
 
 // The int32 code of a masked cell is -9999 (newflow.cu:74); only its low byte 0xF1
 // (bits E, W, NW, N, NE) takes part in the bit tests of the accumulation kernels.

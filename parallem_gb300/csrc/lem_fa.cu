@@ -306,6 +306,7 @@ __global__ void __launch_bounds__(256, 8)
         uint8_t kind = kKindEnd, ext = 0;
         int16_t ptr = (int16_t)l;
         float wl = 0.f;
+        int16_t dm = 0;  // the in-tile donors: bit k for direction scan_dir(k)
         if (s_cls[hc] == kCellIn) {
             pend = 0;
 #pragma unroll
@@ -316,10 +317,12 @@ __global__ void __launch_bounds__(256, 8)
                 if (cl == kCellBlock)
                     pend |= kBlocked;
                 else if (cl == kCellIn) {
-                    if (in_tile(lx + dir_dx(d), ly + dir_dy(d)))
+                    if (in_tile(lx + dir_dx(d), ly + dir_dy(d))) {
                         ++pend;
-                    else
+                        dm |= (int16_t)(1 << scan_index(d));
+                    } else {
                         ++ext;
+                    }
                 }
             }
             const int d = bit_dir(s_code[hc]);
@@ -341,23 +344,23 @@ __global__ void __launch_bounds__(256, 8)
         s_ptr[l] = ptr;
         s_la[l] = make_float2(wl, 0.f);
         s_done[l] = 0;
+        s_oslot[l] = dm;  // the outlet slots are listed after the wave
     }
     if (threadIdx.x == 0) s_qn = 0;
     __syncthreads();
     // accumulation from inside the tile, in dependency order
     tile_wave(
         [&](int cur, int rnd) {
-            const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
+            // the in-tile donors, all loaded before the sum in scan order
+            const uint32_t dm = (uint16_t)s_oslot[cur];
+            float2 v[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                v[kk] = (dm >> kk) & 1u ? s_la[cur + tile_step(scan_dir(kk))] : make_float2(0.f, 0.f);
             float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int kk = 0; kk < 8; ++kk) {
-                const int d = scan_dir(kk);
-                const int nlx = cx + dir_dx(d), nly = cy + dir_dy(d);
-                if (!in_tile(nlx, nly)) continue;
-                const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
-                if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
-                acc = ff_add(acc, s_la[nly * kTile + nlx]);
-            }
+            for (int kk = 0; kk < 8; ++kk)
+                if ((dm >> kk) & 1u) acc = ff_add(acc, v[kk]);
             if (acc.x < 0.0f) acc = make_float2(0.f, 0.f);
             s_la[cur] = ff_add(s_la[cur], acc);
             s_done[cur] = kLaDone;

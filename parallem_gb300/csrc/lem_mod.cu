@@ -411,6 +411,7 @@ struct SedInit {
     SedLocal L;
     int32_t pend;
     int ext;
+    uint32_t dmask;  // the in-tile donors (sed_init_staged): bit k for direction scan_dir(k)
 };
 __device__ __forceinline__ SedInit sed_init(const uint8_t* s_code, const uint8_t* s_cls, int lx, int ly, int tx0,
                                             int ty0, int W, const float* __restrict__ ero,
@@ -421,6 +422,7 @@ __device__ __forceinline__ SedInit sed_init(const uint8_t* s_code, const uint8_t
     SedInit r;
     r.pend = 0;
     r.ext = 0;
+    r.dmask = 0;  // the wave of k_sedt_final derives its donors itself
     float ad = 0.f, ac = 0.f, ag = 0.f;
 #pragma unroll
     for (int kk = 0; kk < 8; ++kk) {
@@ -458,6 +460,7 @@ __device__ __forceinline__ SedInit sed_init_staged(const uint8_t* s_code, const 
     SedInit r;
     r.pend = 0;
     r.ext = 0;
+    r.dmask = 0;
     float ad = 0.f, ac = 0.f, ag = 0.f;
 #pragma unroll
     for (int kk = 0; kk < 8; ++kk) {
@@ -473,10 +476,12 @@ __device__ __forceinline__ SedInit sed_init_staged(const uint8_t* s_code, const 
         ad = __fadd_rn(ad, __fmul_rn(1.0f, __fmul_rn(s_e[nh], omd)));
         ac = __fadd_rn(ac, __fmul_rn(1.0f, __fmul_rn(s_i[nh], omc)));
         ag = __fadd_rn(ag, __fmul_rn(1.0f, __fmul_rn(s_g[nh], omg)));
-        if (in_tile(lx + dir_dx(d), ly + dir_dy(d)))
+        if (in_tile(lx + dir_dx(d), ly + dir_dy(d))) {
             ++r.pend;
-        else
+            r.dmask |= 1u << kk;
+        } else {
             ++r.ext;
+        }
     }
     r.L = sed_local(ad, ac, ag, s_e[hc], s_i[hc], s_g[hc], st0, stone0, k.ddk, k.dck, k.dgk);
     return r;
@@ -554,7 +559,7 @@ __global__ void __launch_bounds__(256, 5)
         const int ly = ly0 + 8 * q, l = ly * kTile + lx, hc = (ly + 1) * kTH + lx + 1;
         int32_t pend = kBlocked;
         uint8_t kind = kKindEnd, ext = 0, nz = 0;
-        int16_t ptr = (int16_t)l;
+        int16_t ptr = (int16_t)l, dm = 0;
         float snew = 0.f;
         cA[q] = cB[q] = cD[q] = cS[q] = 0.f;
         if (s_cls[hc] == kCellIn) {
@@ -563,6 +568,7 @@ __global__ void __launch_bounds__(256, 5)
             const SedInit in = sed_init_staged(s_code, s_cls, s_ero, s_inc, s_gel, lx, ly, soilT[g], snew, k);
             pend = in.pend;
             ext = (uint8_t)in.ext;
+            dm = (int16_t)in.dmask;
             cA[q] = in.L.A;
             cB[q] = in.L.B;
             cD[q] = in.L.dep;
@@ -589,6 +595,7 @@ __global__ void __launch_bounds__(256, 5)
         s_nz[l] = nz;
         s_flag[l] = 0;
         s_pos[l] = -1;
+        s_oslot[l] = dm;  // the outlet slots are listed after the wave
     }
     dem = __reduce_max_sync(0xffffffffu, dem);
     if ((threadIdx.x & 31) == 0 && dem >= 0) atomicMax(&s_dem, dem);
@@ -624,18 +631,17 @@ __global__ void __launch_bounds__(256, 5)
         [&](int cur, int rnd) {
             const bool taint = (s_flag[cur] & kFTaint) != 0;
             if (!taint) {
-                // every donor is inside the tile and settled
-                const int cx = cur & (kTile - 1), cy = cur / kTile, hc = (cy + 1) * kTH + cx + 1;
+                // every donor is inside the tile and settled; all of them are
+                // loaded before the sum in scan order
+                const int cx = cur & (kTile - 1), cy = cur / kTile;
+                const uint32_t dm = (uint16_t)s_oslot[cur];
+                float v[8];
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk) v[kk] = (dm >> kk) & 1u ? s_new[cur + tile_step(scan_dir(kk))] : 0.f;
                 float from = 0.f;
 #pragma unroll
-                for (int kk = 0; kk < 8; ++kk) {
-                    const int d = scan_dir(kk);
-                    const int nlx = cx + dir_dx(d), nly = cy + dir_dy(d);
-                    if (!in_tile(nlx, nly)) continue;
-                    const int nh = hc + dir_dy(d) * kTH + dir_dx(d);
-                    if (!donates(s_code[nh], d) || s_cls[nh] != kCellIn) continue;
-                    from = __fadd_rn(from, __fmul_rn(1.0f, s_new[nly * kTile + nlx]));
-                }
+                for (int kk = 0; kk < 8; ++kk)
+                    if ((dm >> kk) & 1u) from = __fadd_rn(from, __fmul_rn(1.0f, v[kk]));
                 SedLocal L;
                 L.dep = s_dep[cur];
                 L.A = s_A[cur];

@@ -190,6 +190,8 @@ constexpr uint8_t kCellIn = 1;     // a cell the wave computes
 constexpr uint8_t kCellBlock = 2;  // a donor that never completes
 
 __device__ __forceinline__ bool in_tile(int lx, int ly) { return lx >= 0 && lx < kTile && ly >= 0 && ly < kTile; }
+// index step of direction d inside a tile (row-major, kTile cells per row)
+__device__ __forceinline__ int tile_step(int d) { return dir_dy(d) * kTile + dir_dx(d); }
 
 // The outlets of a 32x32 tile (cells whose receiver lies in another tile) in
 // cell order, with each outlet's slot: warp w ballots rows 4w..4w+3, and a
@@ -237,28 +239,52 @@ __device__ __forceinline__ int ring_halo(int i) {
 // queued cell (all its donors in the tile finished), computes it with
 // op(c, round), which returns the in-tile receiver it releases (or -1), and
 // queues that receiver when c was its last donor.  Cells are queued once, in
-// an order where every donor comes before its receiver.  Every lane works on a
-// cell while the round holds one per lane, which a walk along each chain
-// cannot do.
+// an order where every donor comes before its receiver.  Rounds with at least
+// kWaveBlockMin cells (the first ones: the sources) run on every thread of the
+// block; the narrow rounds after them run on warp 0 alone, with a warp barrier
+// between rounds and the queue appended by ballot, while the block's other
+// warps wait at one block barrier (the SM runs other blocks meanwhile).
+constexpr int kWaveBlockMin = 96;
 template <class Op>
 __device__ __forceinline__ void tile_wave(const Op& op, int32_t* s_pend, int16_t* s_q, int* s_qn, int* s_end,
                                           const bool (&src)[4], int lx, int ly0) {
 #pragma unroll
     for (int q = 0; q < 4; ++q)
         if (src[q]) s_q[atomicAdd(s_qn, 1)] = (int16_t)((ly0 + 8 * q) * kTile + lx);
-    int start = 0;
-    for (int round = 0; round <= kTile * kTile; ++round) {
+    int start = 0, end = 0, round = 0;
+    for (;; ++round) {
         __syncthreads();
         if (threadIdx.x == 0) *s_end = *s_qn;
         __syncthreads();
-        const int end = *s_end;
-        if (start == end) break;
+        end = *s_end;
+        if (end - start < kWaveBlockMin) break;  // block-uniform
         for (int i = start + threadIdx.x; i < end; i += blockDim.x) {
             const int c = s_q[i];
             const int r = op(c, round);
             if (r >= 0 && atomicSub(&s_pend[r], 1) == 1) s_q[atomicAdd(s_qn, 1)] = (int16_t)r;
         }
         start = end;
+    }
+    if (threadIdx.x < 32) {
+        const unsigned below = (1u << (threadIdx.x & 31)) - 1u;
+        int qn = end;  // every append of the block rounds is in: the barrier above came after them
+        for (; start < end && round <= kTile * kTile; ++round) {
+            for (int i0 = start; i0 < end; i0 += 32) {
+                const int i = i0 + (int)threadIdx.x;
+                int r = -1;
+                if (i < end) {
+                    r = op(s_q[i], round);
+                    if (r >= 0 && atomicSub(&s_pend[r], 1) != 1) r = -1;
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, r >= 0);
+                if (r >= 0) s_q[qn + __popc(b & below)] = (int16_t)r;
+                qn += __popc(b);
+            }
+            __syncwarp();  // the round's cells and queue entries, for the next round
+            start = end;
+            end = qn;
+        }
+        if (threadIdx.x == 0) *s_qn = qn;
     }
     __syncthreads();
 }
