@@ -96,7 +96,7 @@ typedef struct lem_totals {
     int32_t outlet;          /* Data.outletcellidx after the step            */
     int32_t initial_sinks;   /* FlowDirs sink counter (routeflow.cu:778)     */
     int32_t initial_flats;   /* FlowDirs flat counter (routeflow.cu:779)     */
-    int32_t plateau_sweeps;  /* relaxation rounds of the plateau routing     */
+    int32_t plateau_sweeps;  /* 32x32 tile visits of the plateau routing     */
     int32_t flood_edges;     /* distinct basin pairs of the sink flooding    */
     int32_t fa_uncomputed;   /* masked-in cells left out of accumulation     */
     int32_t sed_uncomputed;  /* masked-in cells left out of sediment routing */

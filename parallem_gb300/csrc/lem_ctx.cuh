@@ -72,6 +72,8 @@ struct DevState {
     int32_t* list_a;    // worklists
     int32_t* list_b;
     int32_t* mark;      // worklist de-duplication epochs
+    int32_t* tq;        // the plateau routing's tile queue: entries and slot sequence numbers
+    int32_t tq_cap;     //   its slots (more than the plateau tiles)
     float2* fa;         // accumulation as an unevaluated fp32 pair (hi, lo)
     float* w;           // runoff weight
     float* slopeptr;
@@ -212,6 +214,18 @@ struct Launch {
         ++*count;
     }
 };
+
+// A slot in a list counted in shared memory, one atomic per warp; every lane
+// of the warp calls it.  -1 where pred is false.
+__device__ __forceinline__ int warp_slot(bool pred, int* s_count) {
+    const unsigned b = __ballot_sync(0xffffffffu, pred);
+    if (!b) return -1;
+    const int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(s_count, __popc(b));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return pred ? base + __popc(b & ((1u << lane) - 1)) : -1;
+}
 
 // Append with one atomic per block: every thread of the block calls it, and
 // s_cnt holds (threads of the block) / 32 + 1 ints.  block_reserve returns the

@@ -483,36 +483,83 @@ constexpr int kTileSweeps = 2048;  // sweeps of one tile visit before it is re-q
 
 // Least fixpoint of sp = min(sp, sp[n] + dc) over equal-height in-grid
 // neighbours (the route_plateausMFD loop, routeflow.cu:854-872), dc = 1 along
-// the axes and 1.41 on the diagonals.  The grid is cut into 32x32 tiles; a
-// round relaxes every queued tile to its local fixpoint in shared memory
-// (Gauss-Seidel sweeps with the halo read at the start of the visit), writes
-// back the cells that improved and queues the neighbouring tiles across every
-// border an improved cell lies on.  Round 0 queues every tile that holds a
-// candidate.  The fixpoint is unique, so the visiting order does not change the
+// the axes and 1.41 on the diagonals.  The grid is cut into 32x32 tiles and
+// the dirty tiles wait in a queue that the blocks pull from until it drains
+// (no grid barrier between visits).  A visit relaxes the tile to its local
+// fixpoint in shared memory (Gauss-Seidel sweeps over the tile's active cells,
+// with the halo read at the start of the visit), lowers the improved cells in
+// memory with atomicMin and queues each neighbouring tile that holds an
+// equal-height neighbour of one of them.  At the start every tile that holds a
+// candidate is queued.  A tile leaves the queue when a block takes it, before
+// the block reads its halo, so an improvement that lands later queues it
+// again.  The fixpoint is unique, so the visiting order does not change the
 // result.  Only candidates (sp > 0) ever change: every other cell is a source
-// at 0.
+// at 0.  Every poll of the queue is bounded, and the visits are capped at
+// lem_limits.max_rounds times the tiles queued at the start.
+constexpr int kQueueSpin = 1 << 20;  // polls of an empty but busy queue, or of an unwritten slot
+
+// The tile queue is a ring of `cap` slots with a sequence number each (a
+// bounded multi-producer multi-consumer queue): ticket p of the pushes (of the
+// takes) owns slot p % cap, free for it once the slot's number reads p (ready
+// for it once the number reads p + 1).  Tickets come from one atomicAdd each.
+struct TileQueue {
+    int32_t* val;  // [cap] entries
+    int32_t* seq;  // [cap] sequence numbers
+    int32_t* qc;   // [0] push tickets, [1] take tickets, [2] pending (queued or in a visit), [3] visits, [4] stop
+    int cap;
+    __device__ void stop(DevScalars* sc) const {
+        raise_error(&sc->err, ErrFlags::kNoConverge);
+        atomicExch(&qc[4], 1);
+    }
+    __device__ void push(int32_t t, DevScalars* sc) const {
+        atomicAdd(&qc[2], 1);
+        const int p = atomicAdd(&qc[0], 1), slot = p % cap;
+        int spin = 0;  // the slot's previous entry is taken; its taker may still be reading it
+        while (*((volatile int32_t*)&seq[slot]) != p && ++spin < kQueueSpin) __nanosleep(32);
+        if (spin >= kQueueSpin) return stop(sc);
+        val[slot] = t;
+        __threadfence();
+        atomicExch(&seq[slot], p + 1);
+    }
+    // the next tile, or -1 once nothing is queued and no visit runs (or the queue stopped)
+    __device__ int32_t take(DevScalars* sc) const {
+        const int c = atomicAdd(&qc[1], 1), slot = c % cap;
+        for (int spin = 0; spin < kQueueSpin; ++spin) {
+            if (*((volatile int32_t*)&seq[slot]) == c + 1) {
+                const int32_t v = *((volatile int32_t*)&val[slot]);
+                atomicExch(&seq[slot], c + cap);  // free for push ticket c + cap
+                return v;
+            }
+            if (*((volatile int32_t*)&qc[2]) == 0 || *((volatile int32_t*)&qc[4])) return -1;
+            __nanosleep(64);
+        }
+        stop(sc);
+        return -1;
+    }
+};
+
 __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict__ z, float* sp,
-                                                       const int32_t* __restrict__ cand, int32_t* list_a,
-                                                       int32_t* list_b, int32_t* mark, ModelConsts k,
-                                                       DevScalars* sc, int pass) {
+                                                       const int32_t* __restrict__ cand, int32_t* tq, int tq_cap,
+                                                       int32_t* mark, ModelConsts k, DevScalars* sc, int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
     cg::grid_group grid = cg::this_grid();
     __shared__ unsigned long long s_key[kPH * kPH];
     __shared__ float s_v[kPH * kPH];
+    __shared__ int16_t s_acell[kPT * kPT];  // active cells (halo index)
+    __shared__ uint8_t s_aeq[kPT * kPT];    //   directions of their equal-height neighbours
+    __shared__ float s_av0[kPT * kPT];      //   their values at the start of the visit
     __shared__ int s_act[9];
+    __shared__ int s_na, s_tile;
     const int W = k.W, H = k.H;
     const int TW = (W + kPT - 1) / kPT, TH = (H + kPT - 1) / kPT;
     const int n = sc->n_cand;
     const size_t gstride = (size_t)gridDim.x * blockDim.x;
     const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int ncap = (int)((size_t)W * H);
-    int32_t* cnt = sc->counters;  // cnt[0..2] queued tiles, triple-buffered
-    const int32_t rid0 = sc->round_id;  // marks of round r are rid0 + r + 1
-    if (gtid == 0) {
-        cnt[0] = 0;
-        cnt[1] = 0;
-        cnt[2] = 0;
-    }
+    const TileQueue tqu{tq, tq + tq_cap, sc->counters, tq_cap};
+    int32_t* const qc = tqu.qc;
+    const int32_t qid = sc->round_id + 1;  // mark of a queued tile
+    if (gtid == 0) qc[0] = qc[1] = qc[2] = qc[3] = qc[4] = 0;
+    for (size_t i = gtid; i < (size_t)tq_cap; i += gstride) tqu.seq[i] = (int32_t)i;
     grid.sync();
     for (size_t base = (size_t)blockIdx.x * blockDim.x; base < (size_t)n; base += gstride) {
         const size_t i = base + threadIdx.x;
@@ -526,26 +573,44 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
         // tile, and one lane per tile tests and sets its mark
         const unsigned peers = __match_any_sync(0xffffffffu, t);
         if (t >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1)
-            fresh = __ldcg(mark + t) != rid0 + 1 && atomicExch(mark + t, rid0 + 1) != rid0 + 1;
-        warp_append(fresh, t, list_a, &cnt[0], ncap, &sc->err);
+            fresh = __ldcg(mark + t) != qid && atomicExch(mark + t, qid) != qid;
+        // one ticket reservation per warp; the ring is empty and holds every
+        // tile, so no slot waits
+        const unsigned b = __ballot_sync(0xffffffffu, fresh);
+        const int lane = threadIdx.x & 31, leader = b ? __ffs(b) - 1 : 0;
+        int at = 0;
+        if (b && lane == leader) {
+            atomicAdd(&qc[2], __popc(b));
+            at = atomicAdd(&qc[0], __popc(b));
+        }
+        at = __shfl_sync(0xffffffffu, at, leader) + __popc(b & ((1u << lane) - 1));
+        if (fresh) {
+            tqu.val[at % tq_cap] = t;
+            __threadfence();
+            atomicExch(&tqu.seq[at % tq_cap], at + 1);
+        }
     }
     grid.sync();
+    const long long visit_cap = (long long)round_cap_of(sc) * max(1, *((volatile int32_t*)&qc[0]));
     // a thread owns 4 consecutive rows of one column: 4 * wy + q
     const int lx = threadIdx.x & 31, wy = threadIdx.x >> 5;
-    int round = 0;
-    for (;; ++round) {
-        const int32_t* in = (round & 1) ? list_b : list_a;
-        int32_t* out = (round & 1) ? list_a : list_b;
-        const int nin = *((volatile int32_t*)&cnt[round % 3]);
-        if (nin == 0) break;
-        if (round >= round_cap_of(sc)) {
-            if (gtid == 0) raise_error(&sc->err, ErrFlags::kNoConverge);
-            break;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int32_t t = tqu.take(sc);
+            if (t >= 0 && atomicAdd(&qc[3], 1) >= visit_cap) {
+                tqu.stop(sc);
+                t = -1;
+            }
+            if (t >= 0) {
+                atomicExch(mark + t, qid - 1);  // taken: a later improvement queues it again
+                __threadfence();                // before the halo is read
+            }
+            s_tile = t;
         }
-        if (gtid == 0) cnt[(round + 2) % 3] = 0;
-        const int32_t id_next = rid0 + round + 2;
-        for (int ti = blockIdx.x; ti < nin; ti += gridDim.x) {
-            const int32_t t = __ldcg(in + ti);
+        __syncthreads();
+        const int32_t t = s_tile;
+        if (t < 0) break;  // block-uniform
+        {
             const int tx0 = (t % TW) * kPT, ty0 = (t / TW) * kPT;
             // the halo in one batch of independent loads per thread
             constexpr int kLoads = (kPH * kPH + 255) / 256;
@@ -572,94 +637,95 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
                 }
             }
             if (threadIdx.x < 9) s_act[threadIdx.x] = 0;
+            if (threadIdx.x == 0) s_na = 0;
             __syncthreads();
-            // per cell: its start value and the directions of its equal-height
-            // neighbours (none for a cell that is not a candidate or is NaN)
-            float v0[4];
-            uint32_t eq[4];
+            // The tile's active cells, listed: candidates with an equal-height
+            // neighbour (a NaN cell, key 0, equals none), with the directions
+            // of those neighbours and their start values.
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int sidx = (4 * wy + q + 1) * kPH + lx + 1;
-                v0[q] = s_v[sidx];
+                const float v0 = s_v[sidx];
                 const unsigned long long kc = s_key[sidx];
                 uint32_t m = 0;
-                if (v0[q] > 0.f && kc != 0) {  // a NaN cell (key 0) equals no neighbour
+                if (v0 > 0.f && kc != 0) {
 #pragma unroll
                     for (int d = 0; d < 8; ++d)
                         if (s_key[sidx + dir_dy(d) * kPH + dir_dx(d)] == kc) m |= 1u << d;
                 }
-                eq[q] = m;
+                const int slot = warp_slot(m != 0, &s_na);
+                if (slot >= 0) {
+                    s_acell[slot] = (int16_t)sidx;
+                    s_aeq[slot] = (uint8_t)m;
+                    s_av0[slot] = v0;
+                }
             }
-            const bool any_eq = (eq[0] | eq[1] | eq[2] | eq[3]) != 0;
-            // Gauss-Seidel sweeps, down and up the thread's rows in turn
-            auto relax = [&](int q) {
-                if (!eq[q]) return false;
-                const int sidx = (4 * wy + q + 1) * kPH + lx + 1;
-                const float cv = s_v[sidx];
-                float best = cv;
-#pragma unroll
-                for (int d = 0; d < 8; ++d) {
-                    if (!((eq[q] >> d) & 1u)) continue;
-                    const float nv = s_v[sidx + dir_dy(d) * kPH + dir_dx(d)] + ((d & 1) ? 1.41f : 1.0f);
-                    if (nv < best) best = nv;
-                }
-                if (best < cv) {
-                    s_v[sidx] = best;
-                    return true;
-                }
-                return false;
-            };
+            __syncthreads();
+            const int na = s_na;
+            // Gauss-Seidel sweeps over the list, forward and backward in turn
             int sweep = 0;
             for (; sweep < kTileSweeps; ++sweep) {
                 bool ch = false;
-                if (any_eq) {
-                    if (sweep & 1) {
+                for (int i = threadIdx.x; i < na; i += blockDim.x) {
+                    const int j = (sweep & 1) ? na - 1 - i : i;
+                    const int sidx = s_acell[j];
+                    const uint32_t m = s_aeq[j];
+                    const float cv = s_v[sidx];
+                    float best = cv;
 #pragma unroll
-                        for (int q = 3; q >= 0; --q) ch |= relax(q);
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) ch |= relax(q);
+                    for (int d = 0; d < 8; ++d) {
+                        const float nv = (m >> d) & 1u ? s_v[sidx + dir_dy(d) * kPH + dir_dx(d)] + ((d & 1) ? 1.41f : 1.0f)
+                                                       : cv;
+                        best = nv < best ? nv : best;
+                    }
+                    if (best < cv) {
+                        s_v[sidx] = best;
+                        ch = true;
                     }
                 }
                 if (!__syncthreads_or(ch)) break;
             }
             if (sweep == kTileSweeps && threadIdx.x == 0) s_act[4] = 1;  // not settled: visit again
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int ly = 4 * wy + q;
-                const int gx = tx0 + lx, gy = ty0 + ly;
-                const float v = s_v[(ly + 1) * kPH + lx + 1];
-                if (gx < W && gy < H && v < v0[q]) {
-                    __stcg(sp + (size_t)gy * W + gx, v);
-                    const int ex = lx == 0 ? 0 : (lx == kPT - 1 ? 2 : 1);
-                    const int ey = ly == 0 ? 0 : (ly == kPT - 1 ? 2 : 1);
-                    if (ex != 1) s_act[3 + ex] = 1;
-                    if (ey != 1) s_act[3 * ey + 1] = 1;
-                    if (ex != 1 && ey != 1) s_act[3 * ey + ex] = 1;
+            for (int i = threadIdx.x; i < na; i += blockDim.x) {
+                const int sidx = s_acell[i];
+                const int ly = sidx / kPH - 1, lx2 = sidx % kPH - 1;
+                const int gx = tx0 + lx2, gy = ty0 + ly;
+                const float v = s_v[sidx];
+                if (gx < W && gy < H && v < s_av0[i] &&
+                    __int_as_float(atomicMin(reinterpret_cast<int*>(sp) + (size_t)gy * W + gx, __float_as_int(v))) > v) {
+                    // (the values are non-negative: their bits order as ints)
+                    // a neighbouring tile can improve only through an
+                    // equal-height neighbour of this cell that lies in it
+                    uint32_t out = 0;  // directions leaving the tile
+                    if (lx2 == 0) out |= 0xE0u;        // SW, W, NW
+                    if (lx2 == kPT - 1) out |= 0x0Eu;  // NE, E, SE
+                    if (ly == 0) out |= 0x83u;         // NW, N, NE
+                    if (ly == kPT - 1) out |= 0x38u;   // SE, S, SW
+#pragma unroll 1
+                    for (uint32_t m = s_aeq[i] & out; m; m &= m - 1) {
+                        const int d = __ffs(m) - 1;
+                        const int nx = lx2 + dir_dx(d), ny = ly + dir_dy(d);
+                        s_act[3 * (ny < 0 ? 0 : (ny >= kPT ? 2 : 1)) + (nx < 0 ? 0 : (nx >= kPT ? 2 : 1))] = 1;
+                    }
                 }
             }
+            __threadfence();  // the lowered cells, before a neighbour is queued
             __syncthreads();
             if (threadIdx.x < 9 && s_act[threadIdx.x]) {
                 const int ntx = t % TW + (int)(threadIdx.x % 3) - 1, nty = t / TW + (int)(threadIdx.x / 3) - 1;
                 if (ntx >= 0 && ntx < TW && nty >= 0 && nty < TH) {
                     const int32_t nt = nty * TW + ntx;
-                    if (atomicExch(mark + nt, id_next) != id_next) {
-                        const int pos = atomicAdd(&cnt[(round + 1) % 3], 1);
-                        if (pos < ncap)
-                            out[pos] = nt;
-                        else
-                            raise_error(&sc->err, ErrFlags::kCapacity);
-                    }
+                    if (atomicExch(mark + nt, qid) != qid) tqu.push(nt, sc);
                 }
             }
             __syncthreads();
+            if (threadIdx.x == 0) atomicSub(&qc[2], 1);  // this visit is over (its pushes came first)
         }
-        grid.sync();
     }
     grid.sync();
     if (gtid == 0) {
-        sc->plateau_sweeps += round + 1;
-        sc->round_id = rid0 + round + 2;
+        sc->plateau_sweeps += qc[3];
+        sc->round_id = qid + 1;
     }
 }
 
@@ -1547,16 +1613,15 @@ static lem_status direction_pass(const DevState& s, const ModelConsts& k, const 
                    pass);
     }
     {
-        // candidates in list_a; frontiers in list_b and `pending` (an int32 grid unused in this stage)
         float* sp = s.sp;
-        const int32_t* cand = s.list_a;
-        int32_t* la = s.list_b;
-        int32_t* lb = s.pending;
+        const int32_t* cand = s.list_a;  // the candidates
+        int32_t* tq = s.tq;
+        int tq_cap = s.tq_cap;
         int32_t* mark = s.mark;
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
-        void* args[] = {(void*)&zz, (void*)&sp, (void*)&cand, (void*)&la, (void*)&lb, (void*)&mark, (void*)&kk,
-                        (void*)&sc, (void*)&pass};
+        void* args[] = {(void*)&zz,   (void*)&sp, (void*)&cand, (void*)&tq,  (void*)&tq_cap,
+                        (void*)&mark, (void*)&kk, (void*)&sc,   (void*)&pass};
         lem_status r = coop("k_plateau_relax", (const void*)k_plateau_relax, s.coop_blocks[kCkPlateau], args, L);
         if (r != LEM_OK) return r;
     }

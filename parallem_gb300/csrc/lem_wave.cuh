@@ -54,18 +54,6 @@ __device__ __forceinline__ void wave_append(bool pred, int32_t value, int32_t* l
     }
 }
 
-// A slot in a list counted in shared memory, one atomic per warp; every lane
-// of the warp calls it.  -1 where pred is false.
-__device__ __forceinline__ int warp_slot(bool pred, int* s_count) {
-    const unsigned b = __ballot_sync(0xffffffffu, pred);
-    if (!b) return -1;
-    const int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(s_count, __popc(b));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    return pred ? base + __popc(b & ((1u << lane) - 1)) : -1;
-}
-
 // The neighbour in direction d of cell (x, y) donates to it when its code has
 // the bit of the opposite direction.
 __device__ __forceinline__ bool donates(uint8_t code_n, int d) { return (code_n & dir_bit((d + 4) & 7)) != 0; }
