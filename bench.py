@@ -131,21 +131,30 @@ def dist_env():
     return rank, world, local
 
 
-def init_dist(world, local):
+def init_dist(world, local, backend=None):
+    """One process group over the ranks (NCCL on the GPU machine; gloo where no GPU
+    is visible, as in the CPU tests)."""
     if world <= 1:
         return None
     import torch
     import torch.distributed as dist
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
+    if backend is None:
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
     return dist
+
+
+def _dist_device(dist):
+    return "cuda" if dist.get_backend() == "nccl" else "cpu"
 
 
 def reduce_max(dist, v):
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=_dist_device(dist))
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -154,7 +163,7 @@ def reduce_sum(dist, v):
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=_dist_device(dist))
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
@@ -162,6 +171,15 @@ def reduce_sum(dist, v):
 def barrier(dist):
     if dist is not None:
         dist.barrier()
+
+
+def whole_job(dist, cells, steps, ms):
+    """The whole job's throughput: the cells all replicas stepped over the
+    slowest replica's time (weak scaling: every rank steps its own DEMs).
+    Returns (cell-timesteps/s, max ms, cells of all ranks)."""
+    ms_max = reduce_max(dist, ms)
+    cells_all = reduce_sum(dist, cells)
+    return cells_all * steps / (ms_max / 1e3), ms_max, cells_all
 
 
 def cpu_sample(sc, seconds=12.0, max_steps=8, label=""):
@@ -614,9 +632,7 @@ def main():
         ms = g.elapsed_ms(0, 1)
     g.synchronize()
     launches = g.launches - launches0
-    ms_max = reduce_max(dist, ms)
-    cells_all = reduce_sum(dist, cells)
-    value = cells_all * args.steps / (ms_max / 1e3)
+    value, ms_max, cells_all = whole_job(dist, cells, args.steps, ms)
 
     # timed region 2: the same steps launched eagerly with a pair of events
     # around every kernel (the per-kernel times and the roofline's duration)
