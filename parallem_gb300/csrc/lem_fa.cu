@@ -210,6 +210,7 @@ struct FaCell {
     __device__ __forceinline__ int receivers(int32_t cur, int x, int y, int32_t* r) const {
         return code_receivers(fd, mask, cur, x, y, W, H, r);
     }
+    __device__ __forceinline__ void prefetch(int32_t) const {}
 };
 
 // The accumulation wave: every source starts it; cells follow as their last
@@ -660,6 +661,10 @@ struct CoarseCell {
         const int32_t dst = __ldg(t_dst + rc);
         r[0] = dst;
         return dst >= 0 ? 1 : 0;
+    }
+    // the receiving outlet's record, read first when this lane carries on with it
+    __device__ __forceinline__ void prefetch(int32_t o) const {
+        if (o >= 0) prefetch_l2(t_orng + o);
     }
 };
 

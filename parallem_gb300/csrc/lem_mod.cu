@@ -323,6 +323,7 @@ struct SedCell {
     __device__ __forceinline__ int receivers(int32_t cur, int x, int y, int32_t* r) const {
         return code_receivers(fd, mask, cur, x, y, W, H, r);
     }
+    __device__ __forceinline__ void prefetch(int32_t) const {}
 };
 
 // The sediment wave: every source starts it; cells follow as their last donor
@@ -993,6 +994,10 @@ struct SedCoarse {
         r[0] = dst;
         return dst >= 0 ? 1 : 0;
     }
+    // the receiving outlet's record, read first when this warp carries on with it
+    __device__ __forceinline__ void prefetch(int32_t o) const {
+        if (o >= 0) prefetch_l2(t_orng + o);
+    }
 };
 
 __global__ void __launch_bounds__(256)
@@ -1360,10 +1365,7 @@ __global__ void k_mod_reset(DevScalars* sc, DemCtx dc, int tiled) {
 }  // namespace
 
 lem_status launch_erosion(const DevState& s, const ModelConsts& k, uint32_t flags, const Launch& L) {
-    const size_t N = (size_t)k.W * k.H;
     const int T = 256;
-    size_t nb = (N + T - 1) / T;
-    const int blocks = (int)(nb > 152 * 32 ? 152 * 32 : nb);
     const float* prop = (k.flow_type != 0 && k.mfd_props) ? s.prop : nullptr;
     const int tiled = (k.flow_type == 0 && !prop) ? 1 : 0;
     LEM_LAUNCH(L, k_mod_reset, (s.dems.n + 127) / 128, 128, s.sc, s.dems, tiled);

@@ -141,10 +141,13 @@ __device__ int wave_walk(const Op& op, int32_t* pending, int32_t* list_a, int32_
             int nspill = 0;
             if (cur >= 0) {
                 const int x = cur % W, y = cur / W;
-                op.cell(cur, x, y);
-                ++done;
+                // the receivers first: they read static data only, so their
+                // loads overlap the cell's own chain of loads
                 int32_t rcv[8];
                 const int nr = op.receivers(cur, x, y, rcv);
+                for (int j = 0; j < nr; ++j) op.prefetch(rcv[j]);
+                op.cell(cur, x, y);
+                ++done;
                 int32_t next = -1;
                 for (int j = 0; j < nr; ++j) {
                     const int32_t r = rcv[j];
@@ -319,13 +322,18 @@ __device__ void wave_walk_warp(const Op& op, int32_t* pending, int32_t* list_a, 
             if (cur < 0) break;
             for (size_t chain = 0; cur >= 0 && chain <= N; ++chain) {
                 const int x = cur % W, y = cur / W;
+                // the receivers first (static data): their loads overlap the node's
+                int32_t rcv[8];
+                int nr = 0;
+                if (lane == 0) {
+                    nr = op.receivers(cur, x, y, rcv);
+                    for (int j = 0; j < nr; ++j) op.prefetch(rcv[j]);
+                }
                 __syncwarp();
                 op.cell_warp(cur, x, y, lane);
                 __syncwarp();
                 int32_t next = -1;
                 if (lane == 0) {
-                    int32_t rcv[8];
-                    const int nr = op.receivers(cur, x, y, rcv);
                     for (int j = 0; j < nr; ++j) {
                         if (dec_acq_rel(pending + rcv[j]) == 1) {
                             if (next < 0) {
@@ -343,6 +351,9 @@ __device__ void wave_walk_warp(const Op& op, int32_t* pending, int32_t* list_a, 
         grid.sync();
     }
 }
+
+// Brings the line holding p into L2 (a hint: no value is read).
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // Receivers of cell (x, y) by its direction code: in-grid, in-catchment cells.
 __device__ __forceinline__ int code_receivers(const uint8_t* __restrict__ fd, const uint8_t* __restrict__ mask,
