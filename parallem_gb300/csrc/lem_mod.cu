@@ -914,6 +914,13 @@ __global__ void __launch_bounds__(256, 5)
 // One outlet of the coarse sediment wave, a warp per outlet: its program
 // level by level (nodes of one tile-wave round depend only on earlier rounds,
 // and the program lists them by round), then its own stores by lane 0.
+// Gathered program of one outlet, per warp: the nodes' coefficients, the
+// first slot of each node's inputs, and per input either its mapped value
+// (an input from another tile, final when the outlet is ready) or its map and
+// the feeding node.  Programs larger than this take the inputs from memory.
+constexpr int kGatherNodes = 64;
+constexpr int kGatherInputs = 96;
+
 struct SedCoarse {
     const uint8_t* fd;
     const int32_t* t_orng;
@@ -927,7 +934,11 @@ struct SedCoarse {
     float* stone;
     float* fines;
     float* soilT;
-    float* s_vals;  // kProgLocal values per warp of the block
+    float* s_vals;    // kProgLocal values per warp of the block
+    float4* s_abc;    // kGatherNodes per warp
+    int16_t* s_ib;    // kGatherNodes per warp: first input slot of the node
+    float4* s_imap;   // kGatherInputs per warp: mapped value (.x) or map
+    int32_t* s_iref;  // kGatherInputs per warp: 0 (mapped value) or the feeding node (negative)
     int W, TW;
     __device__ __forceinline__ void cell_warp(int32_t o, int x, int y, int lane) const {
         const int rng = __ldg(t_orng + o);
@@ -936,13 +947,61 @@ struct SedCoarse {
         const int t = (y / kTile) * TW + x / kTile;
         const size_t nbase = (size_t)t * kTile * kTile + (rng >> 16);
         const size_t pool = (size_t)t * kPool;
-        float* vals = s_vals + (threadIdx.x >> 5) * kProgLocal;
+        const int wq = threadIdx.x >> 5;
+        float* vals = s_vals + wq * kProgLocal;
+        float4* abc = s_abc + wq * kGatherNodes;
+        int16_t* ib = s_ib + wq * kGatherNodes;
+        float4* imap = s_imap + wq * kGatherInputs;
+        int32_t* iref = s_iref + wq * kGatherInputs;
+        // Gather: every node's coefficients and inputs in one batch of loads,
+        // instead of a chain of loads per level of the program.
+        bool gathered = cnt <= kGatherNodes;
+        for (int c0 = 0, in0 = 0; gathered && c0 < cnt; c0 += 32) {
+            const int j = c0 + lane;
+            int nin = 0, start = 0;
+            float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (j < cnt) {
+                r = __ldg(p_abc + nbase + j);
+                const int meta = __float_as_int(r.w);
+                start = meta & 2047;
+                nin = (meta >> 11) & 15;
+            }
+            int incl = nin;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            if (in0 + total > kGatherInputs) {
+                gathered = false;  // warp-uniform
+                break;
+            }
+            const int b0 = in0 + incl - nin;
+            if (j < cnt) {
+                abc[j] = r;
+                ib[j] = (int16_t)b0;
+            }
+            for (int jr = 0; jr < nin; ++jr) {
+                const int32_t ref = __ldg(p_ref + pool + start + jr);
+                const float4 mp = __ldg(p_map + pool + start + jr);
+                if (ref >= 0) {
+                    imap[b0 + jr] = make_float4(map_apply(mp, __ldcg(stone + ref)), 0.f, 0.f, 0.f);
+                    iref[b0 + jr] = 0;
+                } else {
+                    imap[b0 + jr] = mp;
+                    iref[b0 + jr] = ref;
+                }
+            }
+            in0 += total;
+        }
+        __syncwarp();
         for (int i = 0; i < cnt;) {
             const int j = i + lane;
             float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
             int meta = -1;
             if (j < cnt) {
-                r = __ldg(p_abc + nbase + j);
+                r = gathered ? abc[j] : __ldg(p_abc + nbase + j);
                 meta = __float_as_int(r.w);
             }
             const int lvl0 = __shfl_sync(0xffffffffu, meta >> 16, 0);
@@ -954,17 +1013,27 @@ struct SedCoarse {
                 const int start = meta & 2047, nin = (meta >> 11) & 15;
                 const bool nz = (meta >> 15) & 1;
                 float from = r.z;
-                for (int jr = 0; jr < nin; ++jr) {
-                    const int32_t ref = __ldg(p_ref + pool + start + jr);
-                    const float4 mp = __ldg(p_map + pool + start + jr);
-                    float v;
-                    if (ref >= 0)
-                        v = __ldcg(stone + ref);
-                    else if (-ref - 1 < kProgLocal)
-                        v = vals[-ref - 1];
-                    else
-                        v = __ldcg(p_val + nbase - ref - 1);
-                    from = __fadd_rn(from, __fmul_rn(1.0f, map_apply(mp, v)));
+                if (gathered) {
+                    const int b0 = ib[j];
+                    for (int jr = 0; jr < nin; ++jr) {
+                        const int32_t ref = iref[b0 + jr];
+                        const float4 mp = imap[b0 + jr];
+                        const float v = ref == 0 ? mp.x : map_apply(mp, vals[-ref - 1]);
+                        from = __fadd_rn(from, __fmul_rn(1.0f, v));
+                    }
+                } else {
+                    for (int jr = 0; jr < nin; ++jr) {
+                        const int32_t ref = __ldg(p_ref + pool + start + jr);
+                        const float4 mp = __ldg(p_map + pool + start + jr);
+                        float v;
+                        if (ref >= 0)
+                            v = __ldcg(stone + ref);
+                        else if (-ref - 1 < kProgLocal)
+                            v = vals[-ref - 1];
+                        else
+                            v = __ldcg(p_val + nbase - ref - 1);
+                        from = __fadd_rn(from, __fmul_rn(1.0f, map_apply(mp, v)));
+                    }
                 }
                 const float sn = nz ? sed_mix(r.x, r.y, from) : r.x;
                 if (j < kProgLocal) vals[j] = sn;
@@ -986,6 +1055,7 @@ struct SedCoarse {
             }
             soilT[o] = out.y;
         }
+        __syncwarp();  // the gather buffers are reused by the warp's next node
     }
     __device__ __forceinline__ int receivers(int32_t o, int x, int y, int32_t* r) const {
         const int d = bit_dir(__ldg(fd + o));
@@ -1008,9 +1078,13 @@ __global__ void __launch_bounds__(256)
                   float* soilT, int32_t* t_pend, int32_t* list_a, int32_t* list_b, ModelConsts k, DevScalars* sc) {
     if (!sc->sed_tiled_ok) return;
     __shared__ float s_vals[8 * kProgLocal];
+    __shared__ float4 s_abc[8 * kGatherNodes];
+    __shared__ int16_t s_ib[8 * kGatherNodes];
+    __shared__ float4 s_imap[8 * kGatherInputs];
+    __shared__ int32_t s_iref[8 * kGatherInputs];
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->counters[0] = sc->tile_src;
-    const SedCoarse op{fd, t_orng, t_dst, t_out, p_abc, p_ref, p_map, p_val, depo, stone, fines, soilT, s_vals,
-                       k.W, (k.W + kTile - 1) / kTile};
+    const SedCoarse op{fd,    t_orng, t_dst, t_out,  p_abc, p_ref,  p_map,  p_val,  depo,          stone,
+                       fines, soilT,  s_vals, s_abc, s_ib,  s_imap, s_iref, k.W,    (k.W + kTile - 1) / kTile};
     wave_walk_warp(op, t_pend, list_a, list_b, k.W, k.H, sc);
 }
 
