@@ -351,19 +351,41 @@ class EnsembleWork:
             lem._check(L.lem_dem_set_climate(self.b.h, k, C.byref(clim)), "lem_dem_set_climate")
             h2d += C.sizeof(clim)
         lem._check(L.lem_step_batch(self.b.h, 0), "lem_step_batch")
+        # writegrids: fd, fa, dem every 50 steps, erosion grids every 100.  The
+        # grids leave through the asynchronous export (a snapshot on the step
+        # stream, the copy to the host on the second stream); while a step runs
+        # the host receives a share of the grids exported earlier, so the copies
+        # and conversions overlap the steps, and all of them complete inside the
+        # timed region.
+        exports = getattr(self, "exports", [])
+        if exports:
+            take = -(-len(exports) // max(1, 50 - j % 50))
+            for e in exports[:take]:
+                d2h += sum(a.nbytes for a in e.wait().values())
+            self.exports = exports[take:]
         n = len(self.ids)
         tot = (lem.Totals * n)()
         lem._check(L.lem_dem_get_totals_n(self.b.h, (C.c_int32 * n)(*self.ids), n, tot), "lem_dem_get_totals_n")
         d2h += C.sizeof(tot)  # every DEM's budget row of the step
         if j % 50 == 0:
-            for k in self.ids:
-                for f in ("fd", "fa", "dem"):
-                    d2h += self.b.get(k, f).nbytes
-        if j % 100 == 0:
-            for k in self.ids:
-                for f in ("ero", "inci", "geli", "depo"):
-                    d2h += self.b.get(k, f).nbytes
+            d2h += self.e2e_finish()
+            names = ("fd", "fa", "dem") + (("ero", "inci", "geli", "depo") if j % 100 == 0 else ())
+            self.exports = [self.b.export(k, names) for k in self.ids]
         return h2d, d2h
+
+    def e2e_warm(self):
+        """One untimed export of the largest field set of every DEM: the pinned
+        host buffers the timed exports reuse."""
+        self.exports = [self.b.export(k, ("fd", "fa", "dem", "ero", "inci", "geli", "depo")) for k in self.ids]
+        self.e2e_finish()
+
+    def e2e_finish(self):
+        """Waits for the grids still on their way; returns the bytes the host received."""
+        d2h = 0
+        for e in getattr(self, "exports", []):
+            d2h += sum(a.nbytes for a in e.wait().values())
+        self.exports = []
+        return d2h
 
     def plain_sample(self, args, steps=5, budget_s=25.0):
         """The plain path on the same DEMs, one handle and one grid at a time:
@@ -648,6 +670,9 @@ def main():
     g.synchronize()
 
     # timed region 3: end to end through the C ABI with host buffers
+    if hasattr(work, "e2e_warm"):
+        work.e2e_warm()
+        g.synchronize()
     barrier(dist)
     h2d = d2h = 0
     t0 = time.perf_counter()
@@ -655,6 +680,8 @@ def main():
         a, b = work.e2e_step(i, j)
         h2d += a
         d2h += b
+    if hasattr(work, "e2e_finish"):
+        d2h += work.e2e_finish()
     g.synchronize()
     e2e_s = reduce_max(dist, time.perf_counter() - t0)
     e2e = cells_all * e2e_steps / e2e_s

@@ -1247,14 +1247,18 @@ lem_status lem_dem_export(lem_handle* h, int32_t id, const lem_field* fields, in
         delete e;
         return x;
     };
-    // pinned host staging, reused from earlier exports when one is large enough
+    // pinned host staging, reused from earlier exports: the smallest free
+    // buffer that is large enough (exports of DEMs of many sizes keep theirs)
+    size_t best = h->pinned_free.size();
     for (size_t k = 0; k < h->pinned_free.size(); ++k)
-        if (h->pinned_free[k].second >= e->bytes) {
-            e->host = h->pinned_free[k].first;
-            e->host_cap = h->pinned_free[k].second;
-            h->pinned_free.erase(h->pinned_free.begin() + k);
-            break;
-        }
+        if (h->pinned_free[k].second >= e->bytes &&
+            (best == h->pinned_free.size() || h->pinned_free[k].second < h->pinned_free[best].second))
+            best = k;
+    if (best < h->pinned_free.size()) {
+        e->host = h->pinned_free[best].first;
+        e->host_cap = h->pinned_free[best].second;
+        h->pinned_free.erase(h->pinned_free.begin() + best);
+    }
     if (!e->host) {
         if (cudaHostAlloc(&e->host, e->bytes, cudaHostAllocDefault) != cudaSuccess) return fail(LEM_ERR_NOMEM);
         e->host_cap = e->bytes;
