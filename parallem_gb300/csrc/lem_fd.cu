@@ -1060,7 +1060,8 @@ __device__ __forceinline__ void edge_insert(unsigned long long* ekey, unsigned l
 }
 
 constexpr int FE_BX = 32, FE_BY = 8;
-constexpr int kEdgeSlots = 128;  // block-local pair table (a 32x8 tile borders few basin pairs)
+constexpr int kEdgeSlotsLog2 = 7;
+constexpr int kEdgeSlots = 1 << kEdgeSlotsLog2;  // block-local pair table (a 32x8 tile borders few basin pairs)
 
 // identify_watershed_boundary_write_backMFD (newflow.cu:787-877): the minimum
 // boundary height per unordered basin pair, in an open-addressing table.  A
@@ -1115,7 +1116,7 @@ __global__ void __launch_bounds__(FE_BX* FE_BY)
             const unsigned long long kn = sk[ly + dir_dy(d)][lx + dir_dx(d)];
             if (kz == 0 || kn == 0 || kz < kn) continue;  // zs[this] >= zs[idx] is false for NaN
             const unsigned long long key = ((unsigned long long)(uint32_t)min(a, b) << 32) | (uint32_t)max(a, b);
-            uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 57);
+            uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - kEdgeSlotsLog2));
             bool done = false;
             for (int p = 0; p < kEdgeSlots; ++p) {
                 const unsigned long long cur = atomicCAS(&tkey[h], ~0ull, key);

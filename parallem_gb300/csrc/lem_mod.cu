@@ -635,7 +635,6 @@ __global__ void __launch_bounds__(256, 5)
             if (!taint) {
                 // every donor is inside the tile and settled; all of them are
                 // loaded before the sum in scan order
-                const int cx = cur & (kTile - 1), cy = cur / kTile;
                 const uint32_t dm = (uint16_t)s_oslot[cur];
                 float v[8];
 #pragma unroll
@@ -644,15 +643,8 @@ __global__ void __launch_bounds__(256, 5)
 #pragma unroll
                 for (int kk = 0; kk < 8; ++kk)
                     if ((dm >> kk) & 1u) from = __fadd_rn(from, __fmul_rn(1.0f, v[kk]));
-                SedLocal L;
-                L.dep = s_dep[cur];
-                L.A = s_A[cur];
-                L.B = s_B[cur];
-                L.stn = s_stn[cur];
-                L.nz = s_nz[cur] != 0;
-                const float sn = L.nz ? sed_mix(L.A, L.B, from) : s_new[cur];
-                s_new[cur] = sn;
-                sed_store((size_t)(ty0 + cy) * W + tx0 + cx, L, sn, depo, stone, fines, soilT);
+                // the cell's outputs are stored after the wave, coalesced
+                if (s_nz[cur]) s_new[cur] = sed_mix(s_A[cur], s_B[cur], from);
                 s_flag[cur] = kFDone;
                 ++done;
             } else {
@@ -663,6 +655,20 @@ __global__ void __launch_bounds__(256, 5)
             return s_kind[cur] == kKindIn ? (int)s_ptr[cur] : -1;
         },
         s_pend, s_q, &s_qn, &s_qend, src, lx, ly0);
+    // the settled cells' outputs (sed_store), one coalesced pass
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ly = ly0 + 8 * q, l = ly * kTile + lx;
+        if (s_flag[l] != kFDone) continue;
+        const size_t g = (size_t)(ty0 + ly) * W + tx0 + lx;
+        depo[g] = s_dep[l];
+        if (s_nz[l]) {
+            const float sn = s_new[l];
+            __stcg(stone + g, sn);
+            fines[g] = __fsub_rn(100.0f, sn);
+        }
+        soilT[g] = s_stn[l];
+    }
     for (int it = 0; it < 10; ++it) {  // in-tile paths are shorter than 2^10 cells
         bool ch = false;
 #pragma unroll
