@@ -630,6 +630,7 @@ lem_status create_common(const lem_grid_desc* grid, const lem_params* params, in
     ALLOC(s.list_a, N);
     ALLOC(s.list_b, N);
     ALLOC(s.mark, N);
+    ALLOC(s.eqm, N);
     {
         const int64_t ptiles = (int64_t)((k.W + 31) / 32) * ((k.H + 31) / 32);  // plateau tiles (32x32)
         s.tq_cap = (int32_t)(2 * ptiles + 32);

@@ -72,6 +72,7 @@ struct DevState {
     int32_t* list_a;    // worklists
     int32_t* list_b;
     int32_t* mark;      // worklist de-duplication epochs
+    uint8_t* eqm;       // per plateau candidate: directions of its equal-height neighbours
     int32_t* tq;        // the plateau routing's tile queue: entries and slot sequence numbers
     int32_t tq_cap;     //   its slots (more than the plateau tiles)
     float2* fa;         // accumulation as an unevaluated fp32 pair (hi, lo)

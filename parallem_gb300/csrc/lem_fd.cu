@@ -114,6 +114,7 @@ struct FdCell {
     uint8_t cs = kMaskedCode, cm = kMaskedCode;  // SFD and MFD codes
     int is_sink = 0, is_flat = 0;
     bool is_cand = false, has_equal = false;
+    uint8_t eqm = 0;                            // directions of the equal-height neighbours
     unsigned long long low = ~0ull;             // the cell's key when it is in the catchment
 };
 
@@ -141,7 +142,10 @@ __device__ __forceinline__ FdCell fd_cell(const unsigned long long* __restrict__
             const unsigned long long kn = skey[nb(d)];
             if (kn == 0) continue;
             if (ks < kn) up += 1;
-            if (ks == kn) flat += 1;
+            if (ks == kn) {
+                flat += 1;
+                o.eqm |= (uint8_t)(1u << d);
+            }
             if (ks > kn && kn != knd) {
                 const float s = est(d);
                 set_slope(sa, sb, d, s);  // kept unless the fp64 arithmetic below replaces it
@@ -271,8 +275,9 @@ __device__ __forceinline__ void fd_counters(int is_sink, int is_flat, unsigned l
 // counters and lowest elevation; pass 2 writes codes only.
 __global__ void __launch_bounds__(FD_BX* FD_BY)
     k_flowdirs(const double* __restrict__ z, const uint8_t* __restrict__ mask, float* __restrict__ slopes,
-               uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, float* __restrict__ sp, int32_t* plateau,
-               ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts, int pass) {
+               uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, float* __restrict__ sp,
+               uint8_t* __restrict__ eqm, int32_t* plateau, ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts,
+               int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
     constexpr int P = FD_BX + 2;
     __shared__ unsigned long long skey[(FD_BY + 2) * P];
@@ -314,6 +319,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY)
         sfd[self] = c.cs;
         mfd[self] = c.cm;
         sp[self] = c.is_cand ? kFar : 0.f;
+        if (c.is_cand) eqm[self] = c.eqm;  // read by the plateau routing for its candidates only
     }
     // Only a candidate with an equal-height neighbour can be routed: the others
     // (single-cell pits, NaN cells) keep 2e7 and no direction, and stay off
@@ -358,8 +364,9 @@ template <int ROWS>
 __global__ void __launch_bounds__(FD_BX* FD_BY, 4)
     k_flowdirs_tma(const __grid_constant__ CUtensorMap tm_z, const __grid_constant__ CUtensorMap tm_mask,
                    const __grid_constant__ CUtensorMap tm_slopes, float* __restrict__ slopes,
-                   uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, float* __restrict__ sp, int32_t* plateau,
-                   ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts, int pass) {
+                   uint8_t* __restrict__ sfd, uint8_t* __restrict__ mfd, float* __restrict__ sp,
+                   uint8_t* __restrict__ eqm, int32_t* plateau, ModelConsts k, DevScalars* sc, DemCtx dc, TileSet ts,
+                   int pass) {
     using L = FdTma<ROWS>;
     constexpr int SPT = kTile / ROWS;  // strips per tile
     constexpr int P = L::kStageW;
@@ -461,6 +468,7 @@ __global__ void __launch_bounds__(FD_BX* FD_BY, 4)
                 sfd[self] = c.cs;
                 mfd[self] = c.cm;
                 sp[self] = c.is_cand ? kFar : 0.f;
+                if (c.is_cand) eqm[self] = c.eqm;  // read by the plateau routing for its candidates only
             }
             block_append(c.is_cand && c.has_equal, (int32_t)self, plateau, &sc->n_cand, (int)((size_t)W * H),
                          &sc->err, s_cnt);
@@ -538,12 +546,11 @@ struct TileQueue {
     }
 };
 
-__global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict__ z, float* sp,
+__global__ void __launch_bounds__(256) k_plateau_relax(const uint8_t* __restrict__ eqm, float* sp,
                                                        const int32_t* __restrict__ cand, int32_t* tq, int tq_cap,
                                                        int32_t* mark, ModelConsts k, DevScalars* sc, int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
     cg::grid_group grid = cg::this_grid();
-    __shared__ unsigned long long s_key[kPH * kPH];
     __shared__ float s_v[kPH * kPH];
     __shared__ int16_t s_acell[kPT * kPT];  // active cells (halo index)
     __shared__ uint8_t s_aeq[kPT * kPT];    //   directions of their equal-height neighbours
@@ -612,47 +619,40 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const double* __restrict_
         if (t < 0) break;  // block-uniform
         {
             const int tx0 = (t % TW) * kPT, ty0 = (t / TW) * kPT;
-            // the halo in one batch of independent loads per thread
+            // the distances of the tile and its halo, in one batch of
+            // independent loads per thread, with the equal-height masks of
+            // the thread's own cells (k_flowdirs stores them for candidates)
             constexpr int kLoads = (kPH * kPH + 255) / 256;
-            unsigned long long kk[kLoads];
             float vv[kLoads];
 #pragma unroll
             for (int i = 0; i < kLoads; ++i) {
                 const int j = threadIdx.x + 256 * i;
                 const int gx = tx0 - 1 + j % kPH, gy = ty0 - 1 + j / kPH;
-                kk[i] = 0;  // outside the grid: equal to no cell
-                vv[i] = 0.f;
-                if (j < kPH * kPH && gx >= 0 && gx < W && gy >= 0 && gy < H) {
-                    const size_t g = (size_t)gy * W + gx;
-                    kk[i] = dkey(z[g]);
-                    vv[i] = __ldcg(sp + g);
-                }
+                vv[i] = 0.f;  // outside the grid: a source, and no cell's equal neighbour
+                if (j < kPH * kPH && gx >= 0 && gx < W && gy >= 0 && gy < H) vv[i] = __ldcg(sp + (size_t)gy * W + gx);
+            }
+            uint32_t m4[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int gx = tx0 + lx, gy = ty0 + 4 * wy + q;
+                m4[q] = gx < W && gy < H ? eqm[(size_t)gy * W + gx] : 0u;
             }
 #pragma unroll
             for (int i = 0; i < kLoads; ++i) {
                 const int j = threadIdx.x + 256 * i;
-                if (j < kPH * kPH) {
-                    s_key[j] = kk[i];
-                    s_v[j] = vv[i];
-                }
+                if (j < kPH * kPH) s_v[j] = vv[i];
             }
             if (threadIdx.x < 9) s_act[threadIdx.x] = 0;
             if (threadIdx.x == 0) s_na = 0;
             __syncthreads();
-            // The tile's active cells, listed: candidates with an equal-height
-            // neighbour (a NaN cell, key 0, equals none), with the directions
-            // of those neighbours and their start values.
+            // The tile's active cells, listed: candidates (start value above 0)
+            // with an equal-height neighbour (a NaN cell, key 0, has none),
+            // with the directions of those neighbours and their start values.
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int sidx = (4 * wy + q + 1) * kPH + lx + 1;
                 const float v0 = s_v[sidx];
-                const unsigned long long kc = s_key[sidx];
-                uint32_t m = 0;
-                if (v0 > 0.f && kc != 0) {
-#pragma unroll
-                    for (int d = 0; d < 8; ++d)
-                        if (s_key[sidx + dir_dy(d) * kPH + dir_dx(d)] == kc) m |= 1u << d;
-                }
+                const uint32_t m = v0 > 0.f ? m4[q] : 0u;
                 const int slot = warp_slot(m != 0, &s_na);
                 if (slot >= 0) {
                     s_acell[slot] = (int16_t)sidx;
@@ -1585,7 +1585,7 @@ static lem_status launch_flowdirs_tma(const DevState& s, const ModelConsts& k, c
     L.pre("k_flowdirs");
     k_flowdirs_tma<ROWS><<<blocks, dim3(FD_BX, FD_BY), FdTma<ROWS>::kSmem, L.st>>>(
         pass == 1 ? m.z[shape] : m.zf[shape], m.mask[shape], m.slopes[shape], pass == 1 ? s.slopes : nullptr, s.sfd,
-        s.mfd, s.sp, s.list_a, k, s.sc, s.dems, ts, pass);
+        s.mfd, s.sp, s.eqm, s.list_a, k, s.sc, s.dems, ts, pass);
     L.post();
     LEM_CUDA_TRY(cudaGetLastError());
     return LEM_OK;
@@ -1610,18 +1610,19 @@ static lem_status direction_pass(const DevState& s, const ModelConsts& k, const 
         }
         if (r != LEM_OK) return r;
     } else {
-        LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, s.sp, s.list_a, k, s.sc, s.dems, ts,
-                   pass);
+        LEM_LAUNCH(L, k_flowdirs, fdg, fdb, zz, s.mask, slopes, s.sfd, s.mfd, s.sp, s.eqm, s.list_a, k, s.sc, s.dems,
+                   ts, pass);
     }
     {
         float* sp = s.sp;
+        const uint8_t* eqm = s.eqm;
         const int32_t* cand = s.list_a;  // the candidates
         int32_t* tq = s.tq;
         int tq_cap = s.tq_cap;
         int32_t* mark = s.mark;
         ModelConsts kk = k;
         DevScalars* sc = s.sc;
-        void* args[] = {(void*)&zz,   (void*)&sp, (void*)&cand, (void*)&tq,  (void*)&tq_cap,
+        void* args[] = {(void*)&eqm,  (void*)&sp, (void*)&cand, (void*)&tq,  (void*)&tq_cap,
                         (void*)&mark, (void*)&kk, (void*)&sc,   (void*)&pass};
         lem_status r = coop("k_plateau_relax", (const void*)k_plateau_relax, s.coop_blocks[kCkPlateau], args, L);
         if (r != LEM_OK) return r;
