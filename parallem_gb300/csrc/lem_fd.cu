@@ -732,11 +732,11 @@ __global__ void __launch_bounds__(256) k_plateau_relax(const uint8_t* __restrict
 // Final direction of a routed plateau cell: the first direction whose
 // equal-height neighbour attains the cell's distance; pass 1 also stores the
 // 1e-4 slope on that direction (newflow.cu:339-346).
-__global__ void k_plateau_final(const double* __restrict__ z, const float* __restrict__ sp,
+__global__ void k_plateau_final(const uint8_t* __restrict__ eqm, const float* __restrict__ sp,
                                 const int32_t* __restrict__ cand, uint8_t* sfd, uint8_t* mfd, float* slopes,
                                 ModelConsts k, DevScalars* sc, int pass) {
     if (pass == 2 && sc->sinkcount_pass1 == 0) return;
-    const int W = k.W, H = k.H;
+    const int W = k.W;
     const int n = sc->n_cand;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n;
          i += (size_t)gridDim.x * blockDim.x) {
@@ -744,25 +744,18 @@ __global__ void k_plateau_final(const double* __restrict__ z, const float* __res
         const float v = sp[c];
         if (!(v < kFar)) continue;
         const int x = c % W, y = c / W;
-        const unsigned long long kc = dkey(z[c]);
-        if (kc == 0) continue;
-        // the neighbours' heights and distances in one batch of loads
-        unsigned long long kn[8];
+        // the equal-height neighbours (k_flowdirs' mask: in the grid, NaN equal
+        // to none) and their distances in one batch of loads
+        const uint32_t eq = eqm[c];
         float vn[8];
 #pragma unroll
         for (int d = 0; d < 8; ++d) {
-            const int nx = x + dir_dx(d), ny = y + dir_dy(d);
-            kn[d] = 0;  // outside the grid: equal to no cell
             vn[d] = 0.f;
-            if (nx >= 0 && nx < W && ny >= 0 && ny < H) {
-                const size_t nb = (size_t)ny * W + nx;
-                kn[d] = dkey(z[nb]);
-                vn[d] = sp[nb];
-            }
+            if ((eq >> d) & 1u) vn[d] = sp[(size_t)(y + dir_dy(d)) * W + x + dir_dx(d)];
         }
 #pragma unroll
         for (int d = 0; d < 8; ++d) {
-            if (kn[d] != kc || vn[d] + ((d & 1) ? 1.41f : 1.0f) != v) continue;
+            if (!((eq >> d) & 1u) || vn[d] + ((d & 1) ? 1.41f : 1.0f) != v) continue;
             sfd[c] = (uint8_t)dir_bit(d);
             mfd[c] = (uint8_t)dir_bit(d);
             if (slopes) slopes[8 * (size_t)c + d] = 0.0001f;
@@ -1627,7 +1620,7 @@ static lem_status direction_pass(const DevState& s, const ModelConsts& k, const 
         lem_status r = coop("k_plateau_relax", (const void*)k_plateau_relax, s.coop_blocks[kCkPlateau], args, L);
         if (r != LEM_OK) return r;
     }
-    LEM_LAUNCH(L, k_plateau_final, flat_blocks(span, T, big), T, zz, s.sp, s.list_a, s.sfd, s.mfd, slopes, k, s.sc,
+    LEM_LAUNCH(L, k_plateau_final, flat_blocks(span, T, big), T, s.eqm, s.sp, s.list_a, s.sfd, s.mfd, slopes, k, s.sc,
                pass);
     return LEM_OK;
 }
