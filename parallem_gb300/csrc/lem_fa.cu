@@ -704,19 +704,30 @@ __global__ void __launch_bounds__(256)
         const size_t tb = (size_t)t * kTile * kTile, pool = (size_t)t * kTilePool;
         float2* s_X = s_val;      // node sums
         int32_t* s_ok = s_pend;  // node valid
+        // (the second wave's arrays are free here) per node: its largest input
+        // node + 1 and its number of input nodes, and up to four input nodes
+        int16_t* s_nin = s_q;                                     // (largest + 1) | count << 11
+        int16_t* s_in4 = reinterpret_cast<int16_t*>(s_hval);      // [4 * node]
         for (int n = threadIdx.x; n < nn; n += blockDim.x) {
             const int meta = n_meta[tb + n];
             const int start = meta & 2047, nin = meta >> 11;
             float2 acc = make_float2(0.f, 0.f);
-            int ok = 1;
+            int ok = 1, top = 0, cnt = 0;
             for (int j = 0; j < nin; ++j) {
                 const int32_t ref = n_ref[pool + start + j];
-                if (ref < 0) continue;
+                if (ref < 0) {  // an input node: added in the pass below
+                    const int u = -ref - 1;
+                    if (cnt < 4) s_in4[4 * n + cnt] = (int16_t)u;
+                    ++cnt;
+                    top = u + 1 > top ? u + 1 : top;
+                    continue;
+                }
                 acc = ff_add(acc, __ldcg(fa + ref));
                 ok &= t_pend[ref] == 0;
             }
             s_X[n] = acc;
             s_ok[n] = ok;
+            s_nin[n] = (int16_t)(top | (cnt << 11));
         }
         __syncthreads();
         if (threadIdx.x < 32) {
@@ -725,25 +736,29 @@ __global__ void __launch_bounds__(256)
             const int lane = threadIdx.x;
             for (int i = 0; i < nn;) {
                 const int n = i + lane;
-                int meta = 0;
-                bool dep = false;
-                if (n < nn) {
-                    meta = n_meta[tb + n];
-                    for (int j = 0; j < (meta >> 11); ++j) {
-                        const int32_t ref = n_ref[pool + (meta & 2047) + j];
-                        if (ref < 0 && -ref - 1 >= i) dep = true;
-                    }
-                }
+                int info = 0;
+                if (n < nn) info = s_nin[n];
+                const bool dep = n < nn && (info & 2047) - 1 >= i;
                 const unsigned b = __ballot_sync(0xffffffffu, dep);
                 const int run = b ? __ffs(b) - 1 : 32;  // lane 0's inputs all lie before i
                 if (lane < run && n < nn) {
                     float2 acc = s_X[n];
                     int ok = s_ok[n];
-                    for (int j = 0; j < (meta >> 11); ++j) {
-                        const int32_t ref = n_ref[pool + (meta & 2047) + j];
-                        if (ref >= 0) continue;
-                        acc = ff_add(acc, s_X[-ref - 1]);
-                        ok &= s_ok[-ref - 1];
+                    const int cnt = info >> 11;
+                    if (cnt <= 4) {
+                        for (int j = 0; j < cnt; ++j) {
+                            const int u = s_in4[4 * n + j];
+                            acc = ff_add(acc, s_X[u]);
+                            ok &= s_ok[u];
+                        }
+                    } else {  // more input nodes than kept: from memory, in the same order
+                        const int meta = n_meta[tb + n];
+                        for (int j = 0; j < (meta >> 11); ++j) {
+                            const int32_t ref = n_ref[pool + (meta & 2047) + j];
+                            if (ref >= 0) continue;
+                            acc = ff_add(acc, s_X[-ref - 1]);
+                            ok &= s_ok[-ref - 1];
+                        }
                     }
                     s_X[n] = acc;
                     s_ok[n] = ok;
