@@ -1109,24 +1109,36 @@ __global__ void __launch_bounds__(256, 6)
     const int nf = t_fcnt[t];
     const size_t fbase = (size_t)t * kTile * kTile;
     bool stalled = false;  // an outlet whose program never ran (a donor upstream never completes)
-    if (nf >= 0)
-        for (int i = threadIdx.x; i < nf; i += blockDim.x) {
-            const int4 e = f_idx[fbase + i];
-            stalled |= t_pend[e.z] != 0 || e.y < 0;
+    // a thread's slots (a tile has at most kTile * kTile), kept for both passes
+    int4 ev[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = (int)threadIdx.x + 256 * q;
+        ev[q] = make_int4(0, 0, 0, kFinOutlet);
+        if (nf >= 0 && i < nf) {
+            ev[q] = f_idx[fbase + i];
+            stalled |= t_pend[ev[q].z] != 0 || ev[q].y < 0;
         }
+    }
     if (nf >= 0 && !__syncthreads_or(stalled)) {
         // every waiting cell is a program node or lies on a chain below one:
         // its stone is the map of that node's value
         int done = 0;
-        for (int i = threadIdx.x; i < nf; i += blockDim.x) {
-            const int4 e = f_idx[fbase + i];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = (int)threadIdx.x + 256 * q;
+            if (i >= nf) continue;
+            const int4 e = ev[q];
             ++done;
             if (e.w & kFinOutlet) continue;
             const float2 ds = f_ds[fbase + i];
+            const bool nz = (e.w & kFinNz) != 0;
+            const float4 mp = nz ? f_map[fbase + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float pv = nz ? __ldcg(p_val + e.y) : 0.f;
             depo[e.x] = ds.x;
             soilT[e.x] = ds.y;
-            if (e.w & kFinNz) {
-                const float sn = map_apply(f_map[fbase + i], __ldcg(p_val + e.y));
+            if (nz) {
+                const float sn = map_apply(mp, pv);
                 __stcg(stone + e.x, sn);
                 fines[e.x] = __fsub_rn(100.0f, sn);
             }
