@@ -1198,7 +1198,7 @@ __global__ void k_flood_compact(const unsigned long long* __restrict__ ekey, con
 // over the basin-pair edges.  It is computed here as the fixpoint raise(a) =
 // min over edges (a, b, w) of max(w, raise(b)), basin 0 at 0, with basins
 // numbered compactly.  The kernel first groups the edges by basin (the edges
-// of basin 0 left out: nothing lowers it), then relaxes in rounds: round 1
+// of basin 0 left out: nothing lowers it), then relaxes in rounds: the first
 // sweeps the edge list for the edges of basin 0; every later round only the
 // edges of the basins lowered since the round before.
 __global__ void k_flood_spill(const int32_t* __restrict__ ea, const int32_t* __restrict__ eb,
